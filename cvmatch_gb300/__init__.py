@@ -1,0 +1,300 @@
+"""cvmatch_gb300 -- GB300 (sm_103a) TM_CCOEFF_NORMED template matching.
+
+The host-side mirror of cvmatch's public Go API over the C ABI in
+include/cvmatch_gpu.h (library: cvmatch_gb300/_build/libcvmatch_gpu.so):
+
+    Match(parent, sub)          -> (minV, minX, minY, maxV, maxX, maxY)   cvmatch.go:75
+    MatchMap(parent, sub)       -> (res, w, h)                            cvmatch.go:100
+    MatchGray(parent, sub)      -> six-tuple                              cvmatch.go:128
+    NewMatcher(sub) / NewGrayMatcher(sub) -> Matcher; Matcher.Find(parent) matcher.go:45-130
+    NewFleet(*matchers) -> Fleet; Fleet.FindAll(parent) -> [Result]        fleet.go:85-332
+
+Images are numpy uint8 arrays: H x W x 4 for RGBA (the *image.RGBA case),
+H x W for 8-bit gray (the *image.Gray / YCbCr Y-plane case).  Row strides
+are honoured, so a numpy slice is a sub-image exactly like
+image.RGBA.SubImage.  Argument errors raise CvmatchError carrying the
+reference's panic text.  There is no CPU path: every call runs the CUDA
+library, and a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from collections import namedtuple
+
+import numpy as np
+
+__all__ = ["Match", "MatchMap", "MatchGray", "NewMatcher", "NewGrayMatcher", "NewFleet", "Matcher",
+           "Fleet", "Result", "CvmatchError", "Threads", "Impl", "rgba_to_gray", "alpha_const",
+           "match_u8", "library_path", "lib"]
+
+# The Go package's knobs, kept for API compatibility.  The GPU path has no
+# worker count: Threads is accepted and ignored (results never depended on
+# it, threads_test.go:62-81).
+Threads = 0
+Impl = "gb300"
+
+Result = namedtuple("Result", ["MinV", "MinX", "MinY", "MaxV", "MaxX", "MaxY"])
+
+
+class CvmatchError(ValueError):
+    """A call the reference would answer with a panic (the message is the
+    reference's panic text), or a CUDA failure (code CVM_ERR_CUDA)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class _CResult(C.Structure):
+    _fields_ = [("min_v", C.c_float), ("min_x", C.c_int32), ("min_y", C.c_int32),
+                ("max_v", C.c_float), ("max_x", C.c_int32), ("max_y", C.c_int32)]
+
+    def tuple(self):
+        return (self.min_v, self.min_x, self.min_y, self.max_v, self.max_x, self.max_y)
+
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_build", "libcvmatch_gpu.so")
+
+
+def lib():
+    """Loads the CUDA library, compiling it first when it is missing or
+    older than its sources (the same nvcc build __graft_entry__.build runs)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            from . import build as _build
+            path = _build.build()
+            L = C.CDLL(path)
+            vp, i32, i64, u8p = C.c_void_p, C.c_int, C.c_int64, C.c_void_p
+            R = C.POINTER(_CResult)
+            L.cvm_last_error.argtypes = [C.c_char_p, C.c_size_t]
+            L.cvm_last_error.restype = C.c_size_t
+            img_args = [u8p, i64, i32, i32, u8p, i64, i32, i32]
+            L.cvm_match.argtypes = img_args + [R]
+            L.cvm_match_map.argtypes = img_args + [vp]
+            L.cvm_match_gray.argtypes = img_args + [R]
+            L.cvm_match_gray_rgba.argtypes = img_args + [R]
+            L.cvm_match_u8.argtypes = img_args + [i32, i32, vp, R]
+            L.cvm_match_u8_device.argtypes = img_args + [i32, i32, vp, vp, vp]
+            L.cvm_match_device.argtypes = img_args + [vp, vp, vp]
+            L.cvm_rgba_to_gray.argtypes = [u8p, i64, i32, i32, vp]
+            L.cvm_alpha_const.argtypes = [u8p, i64, i32, i32, C.POINTER(C.c_int)]
+            L.cvm_matcher_new.argtypes = [u8p, i64, i32, i32, i32, C.POINTER(vp)]
+            L.cvm_matcher_find.argtypes = [vp, u8p, i64, i32, i32, R]
+            L.cvm_matcher_find_device.argtypes = [vp, u8p, i64, i32, i32, vp, vp]
+            L.cvm_matcher_free.argtypes = [vp]
+            L.cvm_matcher_free.restype = None
+            L.cvm_fleet_new.argtypes = [C.POINTER(vp), i32, C.POINTER(vp)]
+            L.cvm_fleet_find_all.argtypes = [vp, u8p, i64, i32, i32, vp]
+            L.cvm_fleet_find_all_device.argtypes = [vp, u8p, i64, i32, i32, vp, vp]
+            L.cvm_fleet_free.argtypes = [vp]
+            L.cvm_fleet_free.restype = None
+            L.cvm_host_alloc.argtypes = [C.c_size_t]
+            L.cvm_host_alloc.restype = vp
+            L.cvm_host_free.argtypes = [vp]
+            L.cvm_host_free.restype = None
+            L.cvm_launch_count.restype = C.c_uint64
+            L.cvm_version.restype = C.c_char_p
+            _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        lib().cvm_last_error(buf, len(buf))
+        raise CvmatchError(rc, buf.value.decode(errors="replace"))
+
+
+def _view(img, channels: int):
+    """(pointer, byte stride, width, height) of an image array."""
+    if img is None:
+        raise CvmatchError(5, "cvmatch: nil image")
+    a = np.asarray(img)
+    if a.dtype != np.uint8:
+        raise TypeError("cvmatch_gb300: images are uint8 arrays")
+    if channels == 4:
+        if a.ndim != 3 or a.shape[2] != 4:
+            raise TypeError("cvmatch_gb300: RGBA images are H x W x 4 arrays")
+        ok = a.strides[2] == 1 and a.strides[1] == 4
+    else:
+        if a.ndim != 2:
+            raise TypeError("cvmatch_gb300: gray images are H x W arrays")
+        ok = a.strides[1] == 1
+    h, w = a.shape[0], a.shape[1]
+    if h == 0 or w == 0:
+        raise CvmatchError(6, "cvmatch: empty image")
+    if not ok or a.strides[0] < w * channels:
+        a = np.ascontiguousarray(a)
+    return a, a.ctypes.data, a.strides[0], w, h
+
+
+def _is_rgba(img) -> bool:
+    a = np.asarray(img)
+    return a.ndim == 3 and a.shape[2] == 4
+
+
+def Match(parent, sub):
+    """Match (cvmatch.go:75-94): RGBA TM_CCOEFF_NORMED min/max locations."""
+    pa, pp, ps, pw, ph = _view(parent, 4)
+    sa, sp, ss, sw, sh = _view(sub, 4)
+    r = _CResult()
+    _check(lib().cvm_match(pp, ps, pw, ph, sp, ss, sw, sh, C.byref(r)))
+    return r.tuple()
+
+
+def MatchMap(parent, sub):
+    """MatchMap (cvmatch.go:100-117): the full response map (rows x cols)."""
+    pa, pp, ps, pw, ph = _view(parent, 4)
+    sa, sp, ss, sw, sh = _view(sub, 4)
+    w, h = pw - sw + 1, ph - sh + 1
+    res = np.empty((max(h, 1), max(w, 1)), np.float32)
+    _check(lib().cvm_match_map(pp, ps, pw, ph, sp, ss, sw, sh, res.ctypes.data))
+    return res, w, h
+
+
+def rgba_to_gray(img) -> np.ndarray:
+    """rgbToGray (cvmatch.go:222-240) on the device."""
+    a, p, s, w, h = _view(img, 4)
+    out = np.empty((h, w), np.uint8)
+    _check(lib().cvm_rgba_to_gray(p, s, w, h, out.ctypes.data))
+    return out
+
+
+def alpha_const(img) -> bool:
+    """alphaConst (cvmatch.go:146-168) on the device."""
+    a, p, s, w, h = _view(img, 4)
+    v = C.c_int()
+    _check(lib().cvm_alpha_const(p, s, w, h, C.byref(v)))
+    return bool(v.value)
+
+
+def _gray(img):
+    return rgba_to_gray(img) if _is_rgba(img) else img
+
+
+def MatchGray(parent, sub):
+    """MatchGray (cvmatch.go:128-139): gray planes are used as they are,
+    RGBA inputs are converted with OpenCV's fixed-point weights."""
+    r = _CResult()
+    if _is_rgba(parent) and _is_rgba(sub):
+        pa, pp, ps, pw, ph = _view(parent, 4)
+        sa, sp, ss, sw, sh = _view(sub, 4)
+        _check(lib().cvm_match_gray_rgba(pp, ps, pw, ph, sp, ss, sw, sh, C.byref(r)))
+        return r.tuple()
+    pa, pp, ps, pw, ph = _view(_gray(parent), 1)
+    sa, sp, ss, sw, sh = _view(_gray(sub), 1)
+    _check(lib().cvm_match_gray(pp, ps, pw, ph, sp, ss, sw, sh, C.byref(r)))
+    return r.tuple()
+
+
+def match_u8(img, tpl, cn: int, want_map: bool = True):
+    """matchU8 (impl.go:1126-1155) on raw views: img/tpl are H x W (step 1)
+    or H x W x step arrays; returns (six-tuple, map or None)."""
+    img = np.asarray(img)
+    tpl = np.asarray(tpl)
+    step = 1 if img.ndim == 2 else img.shape[2]
+    tstep = 1 if tpl.ndim == 2 else tpl.shape[2]
+    if step != tstep:
+        raise CvmatchError(1, "cvmatch_gb300: image and template steps differ")
+    ia = np.ascontiguousarray(img) if (img.ndim == 3 and img.strides[1] != step) or img.strides[-1] != 1 else img
+    ta = np.ascontiguousarray(tpl) if (tpl.ndim == 3 and tpl.strides[1] != step) or tpl.strides[-1] != 1 else tpl
+    ih, iw = ia.shape[0], ia.shape[1]
+    th, tw = ta.shape[0], ta.shape[1]
+    rw, rh = iw - tw + 1, ih - th + 1
+    res = np.empty((rh, rw), np.float32) if want_map and rw > 0 and rh > 0 else None
+    r = _CResult()
+    _check(lib().cvm_match_u8(ia.ctypes.data, ia.strides[0], iw, ih, ta.ctypes.data, ta.strides[0], tw, th,
+                              cn, step, res.ctypes.data if res is not None else None, C.byref(r)))
+    return r.tuple(), res
+
+
+class Matcher:
+    """A prepared template (matcher.go:25-40).  Find is bit-identical to
+    Match (colour) or MatchGray (gray) on the same parent."""
+
+    def __init__(self, sub, step: int):
+        self._step = step
+        a, p, s, w, h = _view(sub, step)
+        h_ = C.c_void_p()
+        _check(lib().cvm_matcher_new(p, s, w, h, step, C.byref(h_)))
+        self._h = h_
+        self.w, self.h = w, h
+
+    def Find(self, parent):
+        if self._step == 1:
+            parent = _gray(parent)
+        a, p, s, w, h = _view(parent, self._step)
+        r = _CResult()
+        _check(lib().cvm_matcher_find(self._h, p, s, w, h, C.byref(r)))
+        return r.tuple()
+
+    def find_device(self, d_parent: int, pstride: int, pw: int, ph: int, d_out: int, stream: int = 0):
+        """Queues Find on a device-resident parent; writes one result struct
+        (24 bytes) at d_out.  Pointers are raw device addresses."""
+        _check(lib().cvm_matcher_find_device(self._h, d_parent, pstride, pw, ph, d_out, stream or None))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.cvm_matcher_free(h)
+            self._h = None
+
+
+def NewMatcher(sub) -> Matcher:
+    """NewMatcher (matcher.go:45-53): colour, Match semantics."""
+    return Matcher(sub, 4)
+
+
+def NewGrayMatcher(sub) -> Matcher:
+    """NewGrayMatcher (matcher.go:57-64): MatchGray semantics."""
+    return Matcher(_gray(sub), 1)
+
+
+class Fleet:
+    """Many prepared matchers against one frame (fleet.go:19-50)."""
+
+    def __init__(self, ms):
+        if len(ms) == 0:
+            raise CvmatchError(3, "cvmatch: empty fleet")
+        self._ms = list(ms)  # keeps the member handles alive (fleet.go:89-92)
+        arr = (C.c_void_p * len(ms))(*[m._h.value for m in ms])
+        h_ = C.c_void_p()
+        _check(lib().cvm_fleet_new(arr, len(ms), C.byref(h_)))
+        self._h = h_
+        self._step = ms[0]._step
+
+    def FindAll(self, parent):
+        if self._step == 1:
+            parent = _gray(parent)
+        a, p, s, w, h = _view(parent, self._step)
+        out = (_CResult * len(self._ms))()
+        _check(lib().cvm_fleet_find_all(self._h, p, s, w, h, out))
+        return [Result(*o.tuple()) for o in out]
+
+    def find_all_device(self, d_parent: int, pstride: int, pw: int, ph: int, d_out: int, stream: int = 0):
+        _check(lib().cvm_fleet_find_all_device(self._h, d_parent, pstride, pw, ph, d_out, stream or None))
+
+    def __len__(self):
+        return len(self._ms)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.cvm_fleet_free(h)
+            self._h = None
+
+
+def NewFleet(*ms) -> Fleet:
+    """NewFleet (fleet.go:85-101)."""
+    if len(ms) == 1 and isinstance(ms[0], (list, tuple)):
+        ms = tuple(ms[0])
+    return Fleet(ms)

@@ -1,0 +1,1084 @@
+// cvm_api.cpp -- host orchestration and the C ABI of cvmatch_gpu.h.
+//
+// Every public entry point funnels into one of two device pipelines:
+//   run_solo   Match / MatchMap / MatchGray / matchU8 / Matcher.Find
+//              (impl.go:1126-1155, matcher.go:83-130)
+//   run_fleet  Fleet.FindAll (fleet.go:176-332)
+// Both queue kernels on a stream and allocate their per-call workspace
+// from a stream-ordered memory pool, so nothing synchronises until the
+// host-buffer wrappers read their results back.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <atomic>
+
+#include "cvm_internal.h"
+#include "cvm_plan.h"
+
+namespace cvm {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+thread_local std::string t_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+#define CVM_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(CVM_ERR_CUDA, "cvmatch_gpu: %s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CVM_TRY(expr)        \
+    do {                     \
+        int rc_ = (expr);    \
+        if (rc_ != CVM_OK) return rc_; \
+    } while (0)
+
+// ------------------------------------------------------------ device
+
+struct DeviceState {
+    std::once_flag once;
+    int status = CVM_OK;
+    std::string msg;
+    int device = 0;
+    cudaMemPool_t pool = nullptr;
+    std::mutex triMu;
+    std::map<int, float2 *> tri;  // log2 n -> device twiddle table
+};
+
+DeviceState &dev() {
+    static DeviceState d;
+    return d;
+}
+
+int ensure_device() {
+    DeviceState &d = dev();
+    std::call_once(d.once, [&d]() {
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess || count == 0) {
+            d.status = CVM_ERR_NO_DEVICE;
+            d.msg = std::string("cvmatch_gpu: no CUDA device: ") + cudaGetErrorString(e);
+            return;
+        }
+        cudaGetDevice(&d.device);
+        cudaDeviceProp prop;
+        cudaGetDeviceProperties(&prop, d.device);
+        if (prop.major != 10 || prop.minor != 3) {
+            d.status = CVM_ERR_NO_DEVICE;
+            char b[160];
+            snprintf(b, sizeof b, "cvmatch_gpu: built for sm_103a, device %d is sm_%d%d", d.device,
+                     prop.major, prop.minor);
+            d.msg = b;
+            return;
+        }
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = d.device;
+        e = cudaMemPoolCreate(&d.pool, &props);
+        if (e != cudaSuccess) {
+            d.status = CVM_ERR_CUDA;
+            d.msg = std::string("cvmatch_gpu: cudaMemPoolCreate: ") + cudaGetErrorString(e);
+            return;
+        }
+        uint64_t keep = UINT64_MAX;  // keep freed workspace cached for the next call
+        cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    });
+    if (d.status != CVM_OK) return fail(d.status, "%s", d.msg.c_str());
+    return CVM_OK;
+}
+
+// Per-thread non-blocking stream for the host-buffer entry points.
+cudaStream_t thread_stream() {
+    thread_local cudaStream_t s = nullptr;
+    if (!s) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    return s;
+}
+
+const float2 *dev_tri(int n) {
+    DeviceState &d = dev();
+    std::lock_guard<std::mutex> lk(d.triMu);
+    const int l = ilog2(n);
+    auto it = d.tri.find(l);
+    if (it != d.tri.end()) return it->second;
+    std::vector<float> t = tri_twiddles(n);
+    if (t.empty()) t.assign(2, 0.f);
+    float2 *p = nullptr;
+    if (cudaMalloc(&p, t.size() * sizeof(float)) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    d.tri[l] = p;
+    return p;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Bump allocator over one pool allocation.
+struct Arena {
+    char *base = nullptr;
+    size_t used = 0;
+    template <typename T>
+    T *take(size_t count) {
+        T *p = reinterpret_cast<T *>(base + used);
+        used += align_up(count * sizeof(T), 256);
+        return p;
+    }
+    static size_t bytes(size_t count, size_t elem) { return align_up(count * elem, 256); }
+};
+
+struct PoolBuf {
+    void *p = nullptr;
+    cudaStream_t st = nullptr;
+    ~PoolBuf() {
+        if (p) cudaFreeAsync(p, st);
+    }
+};
+
+int pool_alloc(PoolBuf &b, size_t bytes, cudaStream_t st) {
+    b.st = st;
+    CVM_CUDA(cudaMallocFromPoolAsync(&b.p, bytes ? bytes : 256, dev().pool, st));
+    return CVM_OK;
+}
+
+// Largest transforms the shared-memory kernels take (inverse rows hold a
+// dftW row plus its accumulators; the column pass one dftH strip).
+constexpr int kMaxDftW = 8192;
+constexpr int kMaxDftH = 16384;
+
+// ------------------------------------------------------------- geometry
+
+// A plan with its tile grid and plan classes (main / shrunk last band).
+struct Geom {
+    Plan p;
+    int dh2 = 0;
+    TileGeom g;
+    int nclass = 1;
+    FftClass fc[2];
+    int ctas[2] = {0, 0}, pairs[2] = {0, 0};
+    int partOff[2] = {0, 0};
+    int nparts = 0;
+};
+
+int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G) {
+    G.p = make_plan(tw, th, rw, rh);
+    if (G.p.dftW > kMaxDftW || G.p.dftH > kMaxDftH)
+        return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: tile transform %dx%d exceeds the supported %dx%d",
+                    G.p.dftW, G.p.dftH, kMaxDftW, kMaxDftH);
+    G.dh2 = shrink_dh(G.p, rh, shrinkTH);
+    TileGeom &g = G.g;
+    g.ntx = (rw + G.p.blockW - 1) / G.p.blockW;
+    g.nty = (rh + G.p.blockH - 1) / G.p.blockH;
+    g.blockW = G.p.blockW;
+    g.blockH = G.p.blockH;
+    g.rwT = rw;
+    g.rhT = rh;
+    g.twL = tw;
+    g.thL = th;
+    g.tileFirst = 0;
+    const int hwp = (int)align_up(G.p.hw, 16);
+    const float2 *triW = dev_tri(G.p.dftW);
+    if (!triW) return fail(CVM_ERR_CUDA, "cvmatch_gpu: twiddle table allocation failed");
+    const int ntiles = g.ntx * g.nty;
+    G.nclass = G.dh2 > 0 ? 2 : 1;
+    for (int c = 0; c < G.nclass; c++) {
+        FftClass &f = G.fc[c];
+        f.n = G.p.dftW;
+        f.log2n = ilog2(G.p.dftW);
+        f.hw = G.p.hw;
+        f.hwp = hwp;
+        f.dftH = c == 0 ? G.p.dftH : G.dh2;
+        f.log2H = ilog2(f.dftH);
+        f.triW = triW;
+        f.triH = dev_tri(f.dftH);
+        if (!f.triH) return fail(CVM_ERR_CUDA, "cvmatch_gpu: twiddle table allocation failed");
+        if (G.nclass == 1) {
+            f.tileFirst = 0;
+            f.ntiles = ntiles;
+        } else if (c == 0) {
+            f.tileFirst = 0;
+            f.ntiles = ntiles - g.ntx;
+        } else {
+            f.tileFirst = ntiles - g.ntx;
+            f.ntiles = g.ntx;
+        }
+        G.ctas[c] = inv_rows_ctas_per_tile(f, &G.pairs[c]);
+    }
+    G.nparts = 0;
+    for (int c = 0; c < G.nclass; c++) {
+        G.partOff[c] = G.nparts;
+        G.nparts += G.fc[c].ntiles * G.ctas[c];
+    }
+    return CVM_OK;
+}
+
+// Geometry that loads one template as a single tile (template spectra).
+void template_geom(const Geom &G, int tw, int th, TileGeom &tg, FftClass &tf) {
+    tg = TileGeom();
+    tg.twL = tw;
+    tg.thL = th;
+    tf = G.fc[0];
+    tf.tileFirst = 0;
+    tf.ntiles = 1;
+}
+
+size_t spec_elems(const FftClass &f, int cnS) { return (size_t)f.ntiles * cnS * f.dftH * f.hwp; }
+size_t tspec_elems(const FftClass &f, int cnS) { return (size_t)cnS * f.dftH * f.hwp; }
+
+// Template spectra on plan G for cnS channels: forward rows, forward
+// columns scaled by 1/(dftW*dftH) (impl.go:535-553), then the shrunk-band
+// gather (impl.go:591-610).  cnDev limits the channels on the device.
+int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step, int tw, int th,
+                int cnS, const int *cnDev, float2 *ts0, float2 *ts1, cudaStream_t st) {
+    TileGeom tg;
+    FftClass tf;
+    template_geom(G, tw, th, tg, tf);
+    CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st));
+    const float scale = 1.0f / (float(G.p.dftW) * float(G.p.dftH));
+    MemberSet none;
+    memset(&none, 0, sizeof none);
+    CVM_CUDA(launch_cols(0, ts0, ts0, cnS, tg, tf, 0, cnS, cnDev, scale, none, 1, st));
+    if (G.nclass == 2) CVM_CUDA(launch_shrink_gather(ts0, G.p.dftH, ts1, G.dh2, tf.hwp, cnS, st));
+    return CVM_OK;
+}
+
+SatPlanes sat_layout(int iw, int ih, int cnS) {
+    SatPlanes S;
+    S.iw = iw;
+    S.ih = ih;
+    S.nsum = cnS;
+    S.pitch = (long long)align_up((size_t)iw + 1, 32);
+    return S;
+}
+
+size_t sat_bytes(const SatPlanes &S) {
+    const size_t plane = (size_t)S.pitch * (S.ih + 1);
+    return S.nsum * Arena::bytes(plane, 4) + (S.nsum == 4 ? 2 : 1) * Arena::bytes(plane, 8);
+}
+
+void sat_carve(SatPlanes &S, Arena &A) {
+    const size_t plane = (size_t)S.pitch * (S.ih + 1);
+    for (int k = 0; k < S.nsum; k++) S.sum[k] = A.take<unsigned int>(plane);
+    S.sq = A.take<unsigned long long>(plane);
+    S.sqA = S.nsum == 4 ? A.take<unsigned long long>(plane) : nullptr;
+}
+
+// ---------------------------------------------------------- solo pipeline
+
+struct TemplateCache;  // a Matcher's per-geometry state
+
+struct SoloJob {
+    const uint8_t *img;
+    long long istride;
+    int iw, ih, step;
+    int mode;     // 0: cn fixed; 1: colour, cn 3/4 decided by the alpha planes
+    int cnFixed;
+    const uint8_t *tpl;  // device template pixels (one-shot) -- or nullptr with cache
+    long long tstride;
+    int tw, th;
+    const Geom *G;                // cached geometry (Matcher) or nullptr
+    const float2 *cachedTs[2];    // cached template spectra
+    const DevParams *cachedP;     // cached template statistics
+    float *map;
+    cvm_result *out;
+};
+
+int run_solo(const SoloJob &J, cudaStream_t st) {
+    const int rw = J.iw - J.tw + 1, rh = J.ih - J.th + 1;
+    Geom local;
+    const Geom *G = J.G;
+    if (!G) {
+        CVM_TRY(make_geom(J.tw, J.th, rw, rh, J.th, local));
+        G = &local;
+    }
+    const int cnS = J.mode == 1 ? 4 : J.cnFixed;
+    SatPlanes S = sat_layout(J.iw, J.ih, cnS);
+    size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
+                   Arena::bytes(G->nparts, sizeof(Partial)) + sat_bytes(S);
+    for (int c = 0; c < G->nclass; c++) {
+        bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
+        if (!J.cachedP) bytes += Arena::bytes(tspec_elems(G->fc[c], cnS), sizeof(float2));
+    }
+    PoolBuf buf;
+    CVM_TRY(pool_alloc(buf, bytes, st));
+    Arena A;
+    A.base = static_cast<char *>(buf.p);
+    DevParams *P = A.take<DevParams>(1);
+    DevFrame *F = A.take<DevFrame>(1);
+    Partial *parts = A.take<Partial>(G->nparts);
+    sat_carve(S, A);
+    float2 *spec[2] = {nullptr, nullptr};
+    const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
+    float2 *tsOwn[2] = {nullptr, nullptr};
+    for (int c = 0; c < G->nclass; c++) {
+        spec[c] = A.take<float2>(spec_elems(G->fc[c], cnS));
+        if (!J.cachedP) {
+            tsOwn[c] = A.take<float2>(tspec_elems(G->fc[c], cnS));
+            ts[c] = tsOwn[c];
+        }
+    }
+    CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
+    if (J.cachedP) {
+        CVM_CUDA(cudaMemcpyAsync(P, J.cachedP, sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
+    } else {
+        DevParams init;
+        memset(&init, 0, sizeof init);
+        init.mode = J.mode;
+        init.cnFixed = J.cnFixed;
+        init.tw = J.tw;
+        init.th = J.th;
+        CVM_CUDA(upload_bytes(P, &init, sizeof init, st));
+        CVM_CUDA(launch_tpl_stats(J.tpl, J.tstride, J.tw, J.th, J.step, cnS, P, st));
+    }
+    CVM_CUDA(launch_sat(J.img, J.istride, J.step, S, J.mode == 1 ? &F->alphaMismatch : nullptr, st));
+    CVM_CUDA(launch_params_finalize(P, 1, F, st));
+    if (!J.cachedP)
+        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], st));
+    MemberSet ms;
+    memset(&ms, 0, sizeof ms);
+    ms.solo.tspec[0] = ts[0];
+    ms.solo.tspec[1] = ts[1];
+    ms.solo.pIdx = 0;
+    ms.solo.tw = J.tw;
+    ms.solo.th = J.th;
+    ms.solo.rw = rw;
+    ms.solo.rh = rh;
+    ms.solo.partBase = 0;
+    ms.solo.outIdx = 0;
+    ms.params = P;
+    ms.map = J.map;
+    for (int c = 0; c < G->nclass; c++) {
+        const FftClass &f = G->fc[c];
+        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, f, spec[c], cnS, st));
+        ms.scratch[c] = spec[c];
+        ms.scratchStride[c] = 0;
+        CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
+        CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, S, parts, G->partOff[c], G->ctas[c],
+                                 G->pairs[c], st));
+    }
+    CVM_CUDA(launch_extrema_final(ms, 1, parts, G->nparts, J.out, st));
+    return CVM_OK;
+}
+
+// ---------------------------------------------------------- validation
+
+int check_match_args(int iw, int ih, long long istride, long long tstride, int tw, int th, int cn,
+                     int step) {
+    if (cn < 1 || cn > 4 || step < cn || tw < 1 || th < 1 || tw > iw || th > ih ||
+        istride < (long long)iw * step || tstride < (long long)tw * step)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d, cn=%d step=%d)", tw, th,
+                    iw, ih, cn, step);
+    if ((int64_t)tw * th > stats_cap(cn))
+        return fail(CVM_ERR_STATS_CAP,
+                    "cvmatch: template area %dx%d exceeds the exact-statistics bound for cn=%d", tw, th, cn);
+    return CVM_OK;
+}
+
+// alphaConst on the host (cvmatch.go:146-168).  Only the validation of
+// Match needs it on the host: its error text and its statistics cap depend
+// on the channel count the alpha planes select (cvmatch.go:82-86).
+bool host_alpha_const(const uint8_t *pix, long long stride, int w, int h) {
+    const uint8_t a = pix[3];
+    for (int y = 0; y < h; y++) {
+        const uint8_t *row = pix + (long long)y * stride;
+        for (int x = 0; x < w; x++)
+            if (row[4 * x + 3] != a) return false;
+    }
+    return true;
+}
+
+// matchU8's argument checks for Match's RGBA inputs.  The device decides
+// the channel count; the host repeats the alpha scan only when the check
+// itself depends on it (a failing size check, or an area above the cn=4
+// statistics cap).
+int check_match_rgba(const uint8_t *parent, long long pstride, int pw, int ph, const uint8_t *sub,
+                     long long sstride, int sw, int sh) {
+    const bool sizesOk = sw <= pw && sh <= ph && pstride >= (long long)pw * 4 && sstride >= (long long)sw * 4;
+    if (sizesOk && (int64_t)sw * sh <= stats_cap(4)) return CVM_OK;
+    int cn = 4;
+    if (pstride >= (long long)pw * 4 && sstride >= (long long)sw * 4 && host_alpha_const(parent, pstride, pw, ph) &&
+        host_alpha_const(sub, sstride, sw, sh))
+        cn = 3;
+    return check_match_args(pw, ph, pstride, sstride, sw, sh, cn, 4);
+}
+
+int check_image(const void *p, int w, int h) {
+    if (!p) return fail(CVM_ERR_NIL_IMAGE, "cvmatch: nil image");
+    if (w <= 0 || h <= 0) return fail(CVM_ERR_EMPTY_IMAGE, "cvmatch: empty image");
+    return CVM_OK;
+}
+
+// Copies a host image to a device buffer with a 128-byte aligned pitch.
+int upload_image(PoolBuf &b, const uint8_t *src, long long stride, int w, int h, int bpp,
+                 long long *pitch, cudaStream_t st) {
+    const size_t row = (size_t)w * bpp;
+    *pitch = (long long)align_up(row, 128);
+    CVM_TRY(pool_alloc(b, (size_t)*pitch * h, st));
+    CVM_CUDA(cudaMemcpy2DAsync(b.p, (size_t)*pitch, src, (size_t)stride, row, h, cudaMemcpyHostToDevice, st));
+    return CVM_OK;
+}
+
+// One-shot host-buffer match: upload both images, run, read back.
+int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8_t *tpl, long long tstride,
+              int tw, int th, int mode, int cnFixed, int step, int grayFromRgba, float *map,
+              cvm_result *out) {
+    CVM_TRY(ensure_device());
+    cudaStream_t st = thread_stream();
+    PoolBuf bi, bt, gi, gt, bm, bo;
+    long long ip, tp;
+    const int bpp = grayFromRgba ? 4 : step;
+    CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, st));
+    CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st));
+    const uint8_t *dImg = static_cast<const uint8_t *>(bi.p), *dTpl = static_cast<const uint8_t *>(bt.p);
+    if (grayFromRgba) {
+        long long gp = (long long)align_up((size_t)iw, 128), gtp = (long long)align_up((size_t)tw, 128);
+        CVM_TRY(pool_alloc(gi, (size_t)gp * ih, st));
+        CVM_TRY(pool_alloc(gt, (size_t)gtp * th, st));
+        CVM_CUDA(launch_gray(dImg, ip, iw, ih, static_cast<uint8_t *>(gi.p), gp, st));
+        CVM_CUDA(launch_gray(dTpl, tp, tw, th, static_cast<uint8_t *>(gt.p), gtp, st));
+        dImg = static_cast<const uint8_t *>(gi.p);
+        dTpl = static_cast<const uint8_t *>(gt.p);
+        ip = gp;
+        tp = gtp;
+    }
+    const int rw = iw - tw + 1, rh = ih - th + 1;
+    float *dMap = nullptr;
+    if (map) {
+        CVM_TRY(pool_alloc(bm, (size_t)rw * rh * sizeof(float), st));
+        dMap = static_cast<float *>(bm.p);
+    }
+    CVM_TRY(pool_alloc(bo, sizeof(cvm_result), st));
+    SoloJob J;
+    memset(&J, 0, sizeof J);
+    J.img = dImg;
+    J.istride = ip;
+    J.iw = iw;
+    J.ih = ih;
+    J.step = step;
+    J.mode = mode;
+    J.cnFixed = cnFixed;
+    J.tpl = dTpl;
+    J.tstride = tp;
+    J.tw = tw;
+    J.th = th;
+    J.map = dMap;
+    J.out = static_cast<cvm_result *>(bo.p);
+    CVM_TRY(run_solo(J, st));
+    if (map) CVM_CUDA(cudaMemcpyAsync(map, dMap, (size_t)rw * rh * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaMemcpyAsync(out, bo.p, sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    return CVM_OK;
+}
+
+const cvm_result kFlatResult = {1.f, 0, 0, 1.f, 0, 0};
+
+}  // namespace
+}  // namespace cvm
+
+using namespace cvm;
+
+// ================================================================ Matcher
+
+struct MatcherGeom {
+    int rw = 0, rh = 0;
+    Geom G;
+    float2 *ts[2] = {nullptr, nullptr};
+    ~MatcherGeom() {
+        for (auto p : ts)
+            if (p) cudaFree(p);
+    }
+};
+
+struct cvm_matcher {
+    int w = 0, h = 0, step = 0;
+    bool aConst = false;
+    int64_t tsum[4] = {0, 0, 0, 0};
+    int64_t varSum = 0;
+    uint8_t *dPix = nullptr;    // compact device copy, stride w*step
+    DevParams *dP = nullptr;    // template statistics (raw sums), computed once
+    std::mutex mu;
+    std::shared_ptr<MatcherGeom> geom;
+    ~cvm_matcher() {
+        if (dPix) cudaFree(dPix);
+        if (dP) cudaFree(dP);
+    }
+};
+
+namespace {
+
+// The Matcher's cached plan and spectra for one result size, built once
+// under the handle's lock (the double-checked cache of matcher.go:114-126).
+int matcher_geom(cvm_matcher *m, int rw, int rh, std::shared_ptr<MatcherGeom> &out) {
+    std::lock_guard<std::mutex> lk(m->mu);
+    if (m->geom && m->geom->rw == rw && m->geom->rh == rh) {
+        out = m->geom;
+        return CVM_OK;
+    }
+    auto g = std::make_shared<MatcherGeom>();
+    g->rw = rw;
+    g->rh = rh;
+    CVM_TRY(make_geom(m->w, m->h, rw, rh, m->h, g->G));
+    const int cnS = m->step;  // colour: all four channels (cn is decided per frame)
+    for (int c = 0; c < g->G.nclass; c++)
+        CVM_CUDA(cudaMalloc(&g->ts[c], tspec_elems(g->G.fc[c], cnS) * sizeof(float2)));
+    cudaStream_t st = thread_stream();
+    CVM_TRY(build_tspec(g->G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, cnS, nullptr, g->ts[0],
+                        g->ts[1], st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    m->geom = g;
+    out = g;
+    return CVM_OK;
+}
+
+int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, int pw, int ph,
+                     cvm_result *dOut, cudaStream_t st) {
+    if (m->w > pw || m->h > ph)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", m->w, m->h, pw, ph);
+    if (pstride < (long long)pw * m->step)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", m->w, m->h, pw, ph);
+    if (m->varSum == 0) {
+        CVM_CUDA(upload_bytes(dOut, &kFlatResult, sizeof kFlatResult, st));
+        return CVM_OK;
+    }
+    const int rw = pw - m->w + 1, rh = ph - m->h + 1;
+    std::shared_ptr<MatcherGeom> g;
+    CVM_TRY(matcher_geom(m, rw, rh, g));
+    SoloJob J;
+    memset(&J, 0, sizeof J);
+    J.img = dParent;
+    J.istride = pstride;
+    J.iw = pw;
+    J.ih = ph;
+    J.step = m->step;
+    J.mode = m->step == 4 ? 1 : 0;
+    J.cnFixed = 1;
+    J.tw = m->w;
+    J.th = m->h;
+    J.G = &g->G;
+    J.cachedTs[0] = g->ts[0];
+    J.cachedTs[1] = g->ts[1];
+    J.cachedP = m->dP;
+    J.out = dOut;
+    return run_solo(J, st);
+}
+
+}  // namespace
+
+// ================================================================== Fleet
+
+struct FleetBucketGeom {
+    Geom G;
+    int cnS = 1;
+    std::vector<float2 *> ts;     // per member: class 0, class 1 (owned)
+    DevMember *table = nullptr;   // bucket members in bucket order
+    std::vector<int> members;
+    size_t memberScratch[2] = {0, 0};
+    ~FleetBucketGeom() {
+        for (auto p : ts)
+            if (p) cudaFree(p);
+        if (table) cudaFree(table);
+    }
+};
+
+struct FleetGeom {
+    int pw = 0, ph = 0;
+    std::vector<std::unique_ptr<FleetBucketGeom>> bg;
+};
+
+struct cvm_fleet {
+    std::vector<cvm_matcher *> ms;
+    int step = 0;
+    std::vector<Bucket> buckets;
+    DevParams *dP = nullptr;  // per member template statistics
+    std::mutex mu;
+    std::shared_ptr<FleetGeom> geom;
+    ~cvm_fleet() {
+        if (dP) cudaFree(dP);
+    }
+};
+
+namespace {
+
+// Budget for one wave of member tails' column-pass output.
+constexpr size_t kWaveBytes = size_t(512) << 20;
+
+// Per parent size: every bucket's plan and every member's spectrum on its
+// bucket's plan (buildGeom, fleet.go:337-390), plus the device member
+// tables the tail kernels index.
+int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
+    std::lock_guard<std::mutex> lk(f->mu);
+    if (f->geom && f->geom->pw == pw && f->geom->ph == ph) {
+        out = f->geom;
+        return CVM_OK;
+    }
+    auto fg = std::make_shared<FleetGeom>();
+    fg->pw = pw;
+    fg->ph = ph;
+    cudaStream_t st = thread_stream();
+    for (const Bucket &b : f->buckets) {
+        auto bg = std::make_unique<FleetBucketGeom>();
+        const int rwF = pw - b.tw + 1, rhF = ph - b.th + 1;
+        CVM_TRY(make_geom(b.tw, b.th, rwF, rhF, b.th, bg->G));
+        bg->cnS = f->step;
+        bg->members = b.members;
+        const Geom &G = bg->G;
+        std::vector<DevMember> tab(b.members.size());
+        for (size_t pos = 0; pos < b.members.size(); pos++) {
+            cvm_matcher *m = f->ms[b.members[pos]];
+            float2 *t[2] = {nullptr, nullptr};
+            for (int c = 0; c < G.nclass; c++) {
+                CVM_CUDA(cudaMalloc(&t[c], tspec_elems(G.fc[c], bg->cnS) * sizeof(float2)));
+                bg->ts.push_back(t[c]);
+            }
+            CVM_TRY(build_tspec(G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, bg->cnS, nullptr,
+                                t[0], t[1], st));
+            DevMember &d = tab[pos];
+            memset(&d, 0, sizeof d);
+            d.tspec[0] = t[0];
+            d.tspec[1] = t[1];
+            d.pIdx = b.members[pos];
+            d.tw = m->w;
+            d.th = m->h;
+            d.rw = pw - m->w + 1;
+            d.rh = ph - m->h + 1;
+            d.partBase = (int)pos * G.nparts;
+            d.outIdx = b.members[pos];
+        }
+        CVM_CUDA(cudaMalloc(&bg->table, tab.size() * sizeof(DevMember)));
+        CVM_CUDA(cudaMemcpy(bg->table, tab.data(), tab.size() * sizeof(DevMember), cudaMemcpyHostToDevice));
+        for (int c = 0; c < G.nclass; c++) bg->memberScratch[c] = spec_elems(G.fc[c], bg->cnS);
+        fg->bg.push_back(std::move(bg));
+    }
+    CVM_CUDA(cudaStreamSynchronize(st));
+    f->geom = fg;
+    out = fg;
+    return CVM_OK;
+}
+
+int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int pw, int ph, cvm_result *dOut,
+                   cudaStream_t st) {
+    const int n = (int)f->ms.size();
+    for (int i = 0; i < n; i++) {
+        cvm_matcher *m = f->ms[i];
+        if (m->w > pw || m->h > ph)
+            return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", m->w, m->h, pw, ph);
+    }
+    if (pstride < (long long)pw * f->step)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", f->ms[0]->w, f->ms[0]->h, pw, ph);
+    for (int i = 0; i < n; i++)
+        if (f->ms[i]->varSum == 0) CVM_CUDA(upload_bytes(dOut + i, &kFlatResult, sizeof kFlatResult, st));
+    if (f->buckets.empty()) return CVM_OK;
+    std::shared_ptr<FleetGeom> fg;
+    CVM_TRY(fleet_geom(f, pw, ph, fg));
+    const int cnS = f->step;
+    SatPlanes S = sat_layout(pw, ph, cnS);
+    size_t frameBytes = 0, partBytes = 0, waveBytes = 0;
+    std::vector<int> wave(fg->bg.size());
+    for (size_t b = 0; b < fg->bg.size(); b++) {
+        const FleetBucketGeom &bg = *fg->bg[b];
+        size_t fb = 0, per = 0;
+        for (int c = 0; c < bg.G.nclass; c++) {
+            fb += Arena::bytes(spec_elems(bg.G.fc[c], cnS), sizeof(float2));
+            per += bg.memberScratch[c] * sizeof(float2);
+        }
+        frameBytes = std::max(frameBytes, fb);
+        partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * bg.G.nparts, sizeof(Partial)));
+        int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
+        w = std::min<int>(w, (int)bg.members.size());
+        wave[b] = w;
+        size_t wb = 0;
+        for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));
+        waveBytes = std::max(waveBytes, wb);
+    }
+    const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) + sat_bytes(S) +
+                         frameBytes + partBytes + waveBytes;
+    PoolBuf buf;
+    CVM_TRY(pool_alloc(buf, bytes, st));
+    Arena A;
+    A.base = static_cast<char *>(buf.p);
+    DevParams *P = A.take<DevParams>(n);
+    DevFrame *F = A.take<DevFrame>(1);
+    sat_carve(S, A);
+    char *frameBase = A.base + A.used;
+    A.used += frameBytes;
+    Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
+    A.used += partBytes;
+    char *waveBase = A.base + A.used;
+    CVM_CUDA(cudaMemcpyAsync(P, f->dP, n * sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
+    CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
+    CVM_CUDA(launch_sat(dParent, pstride, f->step, S, f->step == 4 ? &F->alphaMismatch : nullptr, st));
+    CVM_CUDA(launch_params_finalize(P, n, F, st));
+    for (size_t b = 0; b < fg->bg.size(); b++) {
+        const FleetBucketGeom &bg = *fg->bg[b];
+        const Geom &G = bg.G;
+        float2 *frame[2] = {nullptr, nullptr};
+        float2 *scratch[2] = {nullptr, nullptr};
+        {
+            Arena fa;
+            fa.base = frameBase;
+            Arena wa;
+            wa.base = waveBase;
+            for (int c = 0; c < G.nclass; c++) {
+                frame[c] = fa.take<float2>(spec_elems(G.fc[c], cnS));
+                scratch[c] = wa.take<float2>((size_t)wave[b] * bg.memberScratch[c]);
+            }
+        }
+        // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
+        for (int c = 0; c < G.nclass; c++) {
+            CVM_CUDA(launch_fwd_rows(dParent, pstride, f->step, cnS, &F->cnMax, G.g, G.fc[c], frame[c], cnS, st));
+            MemberSet none;
+            memset(&none, 0, sizeof none);
+            CVM_CUDA(launch_cols(0, frame[c], frame[c], cnS, G.g, G.fc[c], c, cnS, &F->cnMax, 1.0f, none, 1, st));
+        }
+        // Phase 2: member tails in waves (fleet.go:265-328).
+        MemberSet ms;
+        memset(&ms, 0, sizeof ms);
+        ms.table = bg.table;
+        ms.params = P;
+        for (int c = 0; c < G.nclass; c++) {
+            ms.scratch[c] = scratch[c];
+            ms.scratchStride[c] = bg.memberScratch[c];
+        }
+        const int nm = (int)bg.members.size();
+        for (int w0 = 0; w0 < nm; w0 += wave[b]) {
+            const int nw = std::min(wave[b], nm - w0);
+            ms.first = w0;
+            for (int c = 0; c < G.nclass; c++) {
+                CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
+                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, S, parts, G.partOff[c], G.ctas[c],
+                                         G.pairs[c], st));
+            }
+        }
+        ms.first = 0;
+        CVM_CUDA(launch_extrema_final(ms, nm, parts, G.nparts, dOut, st));
+    }
+    return CVM_OK;
+}
+
+}  // namespace
+
+// ================================================================= C ABI
+
+extern "C" {
+
+size_t cvm_last_error(char *buf, size_t len) {
+    const std::string &e = t_err;
+    if (buf && len > 0) {
+        const size_t c = e.size() < len - 1 ? e.size() : len - 1;
+        memcpy(buf, e.data(), c);
+        buf[c] = 0;
+    }
+    return e.size();
+}
+
+int cvm_match(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride, int sw,
+              int sh, cvm_result *out) {
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(check_image(sub, sw, sh));
+    CVM_TRY(check_match_rgba(parent, pstride, pw, ph, sub, sstride, sw, sh));
+    return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 1, 4, 4, 0, nullptr, out);
+}
+
+int cvm_match_map(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride,
+                  int sw, int sh, float *map) {
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(check_image(sub, sw, sh));
+    CVM_TRY(check_match_rgba(parent, pstride, pw, ph, sub, sstride, sw, sh));
+    if (!map) return fail(CVM_ERR_ARGS, "cvmatch_gpu: MatchMap needs a map buffer");
+    cvm_result r;
+    return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 1, 4, 4, 0, map, &r);
+}
+
+int cvm_match_gray(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride,
+                   int sw, int sh, cvm_result *out) {
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(check_image(sub, sw, sh));
+    CVM_TRY(check_match_args(pw, ph, pstride, sstride, sw, sh, 1, 1));
+    return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 0, 1, 1, 0, nullptr, out);
+}
+
+int cvm_match_gray_rgba(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub,
+                        int64_t sstride, int sw, int sh, cvm_result *out) {
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(check_image(sub, sw, sh));
+    if (pstride < (int64_t)pw * 4 || sstride < (int64_t)sw * 4)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d, cn=1 step=1)", sw, sh, pw, ph);
+    CVM_TRY(check_match_args(pw, ph, (int64_t)pw, (int64_t)sw, sw, sh, 1, 1));
+    return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 0, 1, 1, 1, nullptr, out);
+}
+
+int cvm_match_u8(const uint8_t *img, int64_t istride, int iw, int ih, const uint8_t *tpl, int64_t tstride, int tw,
+                 int th, int cn, int step, float *map, cvm_result *out) {
+    CVM_TRY(check_match_args(iw, ih, istride, tstride, tw, th, cn, step));
+    if (!img || !tpl) return fail(CVM_ERR_NIL_IMAGE, "cvmatch: nil image");
+    return host_solo(img, istride, iw, ih, tpl, tstride, tw, th, 0, cn, step, 0, map, out);
+}
+
+int cvm_match_u8_device(const uint8_t *d_img, int64_t istride, int iw, int ih, const uint8_t *d_tpl,
+                        int64_t tstride, int tw, int th, int cn, int step, float *d_map, cvm_result *d_out,
+                        void *stream) {
+    CVM_TRY(check_match_args(iw, ih, istride, tstride, tw, th, cn, step));
+    CVM_TRY(ensure_device());
+    SoloJob J;
+    memset(&J, 0, sizeof J);
+    J.img = d_img;
+    J.istride = istride;
+    J.iw = iw;
+    J.ih = ih;
+    J.step = step;
+    J.mode = 0;
+    J.cnFixed = cn;
+    J.tpl = d_tpl;
+    J.tstride = tstride;
+    J.tw = tw;
+    J.th = th;
+    J.map = d_map;
+    J.out = d_out;
+    return run_solo(J, static_cast<cudaStream_t>(stream));
+}
+
+int cvm_match_device(const uint8_t *d_parent, int64_t pstride, int pw, int ph, const uint8_t *d_sub,
+                     int64_t sstride, int sw, int sh, float *d_map, cvm_result *d_out, void *stream) {
+    CVM_TRY(check_image(d_parent, pw, ph));
+    CVM_TRY(check_image(d_sub, sw, sh));
+    CVM_TRY(check_match_args(pw, ph, pstride, sstride, sw, sh, 4, 4));
+    CVM_TRY(ensure_device());
+    SoloJob J;
+    memset(&J, 0, sizeof J);
+    J.img = d_parent;
+    J.istride = pstride;
+    J.iw = pw;
+    J.ih = ph;
+    J.step = 4;
+    J.mode = 1;
+    J.cnFixed = 4;
+    J.tpl = d_sub;
+    J.tstride = sstride;
+    J.tw = sw;
+    J.th = sh;
+    J.map = d_map;
+    J.out = d_out;
+    return run_solo(J, static_cast<cudaStream_t>(stream));
+}
+
+int cvm_rgba_to_gray(const uint8_t *pix, int64_t stride, int w, int h, uint8_t *out) {
+    CVM_TRY(check_image(pix, w, h));
+    if (stride < (int64_t)w * 4) return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*4");
+    CVM_TRY(ensure_device());
+    cudaStream_t st = thread_stream();
+    PoolBuf bi, bo;
+    long long ip;
+    CVM_TRY(upload_image(bi, pix, stride, w, h, 4, &ip, st));
+    CVM_TRY(pool_alloc(bo, (size_t)w * h, st));
+    CVM_CUDA(launch_gray(static_cast<const uint8_t *>(bi.p), ip, w, h, static_cast<uint8_t *>(bo.p), w, st));
+    CVM_CUDA(cudaMemcpyAsync(out, bo.p, (size_t)w * h, cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    return CVM_OK;
+}
+
+int cvm_alpha_const(const uint8_t *pix, int64_t stride, int w, int h, int *out) {
+    CVM_TRY(check_image(pix, w, h));
+    if (stride < (int64_t)w * 4) return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*4");
+    CVM_TRY(ensure_device());
+    cudaStream_t st = thread_stream();
+    PoolBuf bi, bf;
+    long long ip;
+    CVM_TRY(upload_image(bi, pix, stride, w, h, 4, &ip, st));
+    CVM_TRY(pool_alloc(bf, sizeof(unsigned int), st));
+    CVM_CUDA(cudaMemsetAsync(bf.p, 0, sizeof(unsigned int), st));
+    CVM_CUDA(launch_alpha_scan(static_cast<const uint8_t *>(bi.p), ip, w, h, static_cast<unsigned int *>(bf.p), st));
+    unsigned int mism = 0;
+    CVM_CUDA(cudaMemcpyAsync(&mism, bf.p, sizeof mism, cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    *out = mism == 0;
+    return CVM_OK;
+}
+
+int cvm_matcher_new(const uint8_t *pix, int64_t stride, int w, int h, int step, cvm_matcher **out) {
+    CVM_TRY(check_image(pix, w, h));
+    if (step != 1 && step != 4) return fail(CVM_ERR_ARGS, "cvmatch_gpu: matcher step must be 1 or 4");
+    if (stride < (int64_t)w * step) return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*step");
+    if ((int64_t)w * h > stats_cap(step))
+        return fail(CVM_ERR_STATS_CAP, "cvmatch: template area %dx%d exceeds the exact-statistics bound", w, h);
+    CVM_TRY(ensure_device());
+    std::unique_ptr<cvm_matcher> m(new cvm_matcher());
+    m->w = w;
+    m->h = h;
+    m->step = step;
+    // Exact statistics over step channels (matcher.go:75) and the template
+    // alpha scan (matcher.go:49).
+    const int64_t area = (int64_t)w * h;
+    bool aconst = true;
+    for (int k = 0; k < step; k++) {
+        int64_t s = 0, s2 = 0;
+        for (int y = 0; y < h; y++) {
+            const uint8_t *row = pix + (int64_t)y * stride + k;
+            for (int x = 0; x < w; x++) {
+                const int64_t v = row[(int64_t)x * step];
+                s += v;
+                s2 += v * v;
+            }
+        }
+        m->tsum[k] = s;
+        m->varSum += area * s2 - s * s;
+    }
+    if (step == 4)
+        for (int y = 0; y < h && aconst; y++)
+            for (int x = 0; x < w; x++)
+                if (pix[(int64_t)y * stride + 4 * x + 3] != pix[3]) {
+                    aconst = false;
+                    break;
+                }
+    m->aConst = aconst;
+    cudaStream_t st = thread_stream();
+    CVM_CUDA(cudaMalloc(&m->dPix, (size_t)w * h * step));
+    CVM_CUDA(cudaMemcpy2DAsync(m->dPix, (size_t)w * step, pix, (size_t)stride, (size_t)w * step, h,
+                               cudaMemcpyHostToDevice, st));
+    CVM_CUDA(cudaMalloc(&m->dP, sizeof(DevParams)));
+    DevParams init;
+    memset(&init, 0, sizeof init);
+    init.mode = step == 4 ? 1 : 0;
+    init.cnFixed = step == 4 ? 4 : 1;
+    init.tw = w;
+    init.th = h;
+    CVM_CUDA(upload_bytes(m->dP, &init, sizeof init, st));
+    CVM_CUDA(launch_tpl_stats(m->dPix, (long long)w * step, w, h, step, step, m->dP, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    *out = m.release();
+    return CVM_OK;
+}
+
+int cvm_matcher_find(cvm_matcher *m, const uint8_t *parent, int64_t pstride, int pw, int ph, cvm_result *out) {
+    if (!m) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil matcher");
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(ensure_device());
+    if (m->w > pw || m->h > ph)
+        return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", m->w, m->h, pw, ph);
+    if (m->varSum == 0) {
+        *out = kFlatResult;
+        return CVM_OK;
+    }
+    cudaStream_t st = thread_stream();
+    PoolBuf bi, bo;
+    long long ip;
+    CVM_TRY(upload_image(bi, parent, pstride, pw, ph, m->step, &ip, st));
+    CVM_TRY(pool_alloc(bo, sizeof(cvm_result), st));
+    CVM_TRY(matcher_find_dev(m, static_cast<const uint8_t *>(bi.p), ip, pw, ph, static_cast<cvm_result *>(bo.p), st));
+    CVM_CUDA(cudaMemcpyAsync(out, bo.p, sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    return CVM_OK;
+}
+
+int cvm_matcher_find_device(cvm_matcher *m, const uint8_t *d_parent, int64_t pstride, int pw, int ph,
+                            cvm_result *d_out, void *stream) {
+    if (!m) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil matcher");
+    CVM_TRY(check_image(d_parent, pw, ph));
+    CVM_TRY(ensure_device());
+    return matcher_find_dev(m, d_parent, pstride, pw, ph, d_out, static_cast<cudaStream_t>(stream));
+}
+
+void cvm_matcher_free(cvm_matcher *m) { delete m; }
+
+int cvm_fleet_new(cvm_matcher *const *ms, int n, cvm_fleet **out) {
+    if (n <= 0 || !ms) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    CVM_TRY(ensure_device());
+    std::unique_ptr<cvm_fleet> f(new cvm_fleet());
+    f->ms.assign(ms, ms + n);
+    f->step = ms[0]->step;
+    for (cvm_matcher *m : f->ms)
+        if (m->step != f->step) return fail(CVM_ERR_MIXED_FLEET, "cvmatch: fleet mixes color and gray matchers");
+    std::vector<MemberShape> shapes;
+    for (cvm_matcher *m : f->ms) shapes.push_back(MemberShape{m->w, m->h, m->varSum == 0});
+    f->buckets = bucketize(shapes);
+    CVM_CUDA(cudaMalloc(&f->dP, n * sizeof(DevParams)));
+    for (int i = 0; i < n; i++)
+        CVM_CUDA(cudaMemcpy(f->dP + i, f->ms[i]->dP, sizeof(DevParams), cudaMemcpyDeviceToDevice));
+    *out = f.release();
+    return CVM_OK;
+}
+
+int cvm_fleet_find_all(cvm_fleet *f, const uint8_t *parent, int64_t pstride, int pw, int ph, cvm_result *out) {
+    if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(ensure_device());
+    const int n = (int)f->ms.size();
+    for (int i = 0; i < n; i++)
+        if (f->ms[i]->w > pw || f->ms[i]->h > ph)
+            return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", f->ms[i]->w, f->ms[i]->h, pw,
+                        ph);
+    cudaStream_t st = thread_stream();
+    PoolBuf bi, bo;
+    long long ip;
+    CVM_TRY(upload_image(bi, parent, pstride, pw, ph, f->step, &ip, st));
+    CVM_TRY(pool_alloc(bo, n * sizeof(cvm_result), st));
+    CVM_TRY(fleet_find_dev(f, static_cast<const uint8_t *>(bi.p), ip, pw, ph, static_cast<cvm_result *>(bo.p), st));
+    CVM_CUDA(cudaMemcpyAsync(out, bo.p, n * sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
+    CVM_CUDA(cudaStreamSynchronize(st));
+    return CVM_OK;
+}
+
+int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pstride, int pw, int ph,
+                              cvm_result *d_out, void *stream) {
+    if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    CVM_TRY(check_image(d_parent, pw, ph));
+    CVM_TRY(ensure_device());
+    return fleet_find_dev(f, d_parent, pstride, pw, ph, d_out, static_cast<cudaStream_t>(stream));
+}
+
+void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]) {
+    if (tw < 1 || th < 1 || rw < 1 || rh < 1 || !out)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: plan needs positive template and result sizes");
+    const Plan p = make_plan(tw, th, rw, rh);
+    out[0] = p.dftW;
+    out[1] = p.dftH;
+    out[2] = p.blockW;
+    out[3] = p.blockH;
+    out[4] = shrink_dh(p, rh, th);
+    out[5] = ((rw + p.blockW - 1) / p.blockW) * ((rh + p.blockH - 1) / p.blockH);
+    return CVM_OK;
+}
+
+void *cvm_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void cvm_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+uint64_t cvm_launch_count(void) { return g_launches.load(); }
+
+void cvm_profile_enable(int on) { profile_enable(on); }
+
+int cvm_profile_read(int i, char *name, size_t len, double *ms_total, uint64_t *launches) {
+    unsigned long long n = 0;
+    const int rc = profile_read(i, name, len, ms_total, &n);
+    if (rc == 0 && launches) *launches = n;
+    return rc;
+}
+
+const char *cvm_version(void) { return "cvmatch_gpu 0.1 (sm_103a, reference-exact FP32 radix-4)"; }
+
+}  // extern "C"

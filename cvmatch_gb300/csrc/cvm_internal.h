@@ -1,0 +1,163 @@
+// cvm_internal.h -- structures shared by the host orchestration
+// (cvm_api.cpp, cvm_plan.cpp) and the sm_103a kernels (cvm_kernels.cu).
+//
+// Data layout in HBM (one frame, one bucket/plan class):
+//   frame        u8, device copy of the caller's image, pitch = stride
+//   SAT planes   (ih+1) x pitch32 summed-area tables of every channel
+//                (u32, modular: every window sum is < 2^32) and of the
+//                squared pixels (u64); row/column 0 are zero
+//   spectra      per tile t and channel k a dftH x hwp complex64 slab
+//                (hwp = dftW/2+1 rounded up to 16): the forward rows
+//                kernel writes logical spectrum row L at slot brev(L),
+//                the column kernel leaves spatial row y at slot brev(y)
+//                (the reference's storage relabelling, radix4cols.go:12-24)
+//   partials     one (min,max,index) record per inverse-rows CTA
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "cvmatch_gpu.h"
+
+namespace cvm {
+
+// newGoPlan's result (impl.go:227-295).
+struct Plan {
+    int dftW = 0, dftH = 0, hw = 0, blockW = 0, blockH = 0;
+    int64_t cost = 0;
+};
+
+// Tile grid of one correlation: tiles of blockW x blockH results over the
+// rwT x rhT result extent of the template the grid was planned for
+// (twL x thL, the bucket maxima for a fleet).
+struct TileGeom {
+    int ntx = 1, nty = 1;
+    int blockW = 1, blockH = 1;
+    int rwT = 1, rhT = 1;
+    int twL = 1, thL = 1;
+    int tileFirst = 0;  // first tile of the launch (plan class)
+};
+
+// One plan class: either every tile (no shrunk last band) or the tiles
+// above the last band (main), or the last band at the shrunk height.
+struct FftClass {
+    int n = 0, log2n = 0;    // row transform (dftW)
+    int hw = 0, hwp = 0;     // spectrum width and padded row stride
+    int dftH = 0, log2H = 0; // column transform
+    const float2 *triW = nullptr, *triH = nullptr;
+    int tileFirst = 0, ntiles = 0;
+};
+
+// Template statistics and the tail constants derived from them.  The raw
+// per-channel sums are exact; finalize() derives the rest once the
+// effective channel count is known on the device.
+struct DevParams {
+    unsigned long long tsum[4];   // sum of template bytes per channel
+    unsigned long long tsq[4];    // sum of squared bytes per channel
+    unsigned int alphaMismatch;   // template alpha plane not constant
+    int mode;                     // 0: cn fixed (cnFixed); 1: colour, cn 3/4 by alpha
+    int cnFixed;
+    int tw, th;
+    // derived by k_params_finalize
+    int cn;
+    int flat;
+    long long varSum;
+    float templNorm, numScale, varScale;
+};
+
+// Per-frame flags written on the device.
+struct DevFrame {
+    unsigned int alphaMismatch;  // parent alpha plane not constant
+    int cnMax;                   // largest effective cn among the members
+    int pad[2];
+};
+
+struct SatPlanes {
+    unsigned int *sum[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long *sq = nullptr;   // sum over the first min(cnS,3) channels (all when cnS<4)
+    unsigned long long *sqA = nullptr;  // channel-3 squares when cnS == 4
+    long long pitch = 0;                // elements per plane row
+    int nsum = 0;                       // number of sum planes (cnS)
+    int iw = 0, ih = 0;
+};
+
+// One correlation target of the tail kernels: a solo match or one fleet
+// member.  tspec is indexed by plan class (0 main, 1 shrunk last band).
+// Per-call state is addressed by index (pIdx into the launch's params
+// array, the wave slot into the launch's scratch), so a fleet's member
+// table is built once per geometry and reused by every call.
+struct DevMember {
+    const float2 *tspec[2];    // template spectrum, [ch][dftH][hwp], natural rows
+    int pIdx;                  // index into the launch's DevParams array
+    int tw, th, rw, rh;
+    int partBase;              // first partial record of this member
+    int outIdx;                // result slot
+    int pad;
+};
+
+// Where the tail kernels find their targets: a device member table
+// (fleets) or one member passed by value (solo matches).
+struct MemberSet {
+    const DevMember *table;    // nullptr: use `solo`
+    DevMember solo;
+    int first;                 // first table entry of this launch (wave)
+    DevParams *params;
+    float2 *scratch[2];        // column-pass output, per wave slot
+    size_t scratchStride[2];   // elements between wave slots
+    float *map;                // optional score map (solo only)
+};
+
+struct Partial {
+    float minV, maxV;
+    long long minI, maxI;
+};
+
+// ----------------------------------------------------------- launches
+// All launch wrappers queue work on `st` and return the launch status.
+
+cudaError_t launch_gray(const uint8_t *src, long long sstride, int w, int h, uint8_t *dst,
+                        long long dstride, cudaStream_t st);
+cudaError_t launch_alpha_scan(const uint8_t *img, long long stride, int w, int h,
+                              unsigned int *mismatch, cudaStream_t st);
+cudaError_t launch_tpl_stats(const uint8_t *tpl, long long tstride, int tw, int th, int step,
+                             int cnStats, DevParams *P, cudaStream_t st);
+cudaError_t launch_params_finalize(DevParams *P, int n, DevFrame *F, cudaStream_t st);
+cudaError_t launch_sat(const uint8_t *img, long long istride, int step, const SatPlanes &S,
+                       unsigned int *alphaMismatch, cudaStream_t st);
+// Forward row pass of every tile of `fc` (or of a template: geometry with
+// one 1x1 block whose loads are the template's tw x th).
+cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
+                            const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
+                            int cnS, cudaStream_t st);
+// Column pass.  mode 0: forward only, natural output (template spectra with
+// `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
+// conj-multiply + inverse, in place on the members' scratch (solo match);
+// mode 2: conj-multiply + inverse from a forward frame cache `in` into each
+// member's scratch (fleet tails).  nmembers targets from ms.
+cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
+                        const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
+                        const MemberSet &ms, int nmembers, cudaStream_t st);
+// Inverse rows + channel accumulation + normalization + partial extrema.
+cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS,
+                            const MemberSet &ms, int nmembers, const SatPlanes &S,
+                            Partial *partials, int partOffset, int ctasPerTile, int pairsPerCta,
+                            cudaStream_t st);
+int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta);
+cudaError_t launch_extrema_final(const MemberSet &ms, int nmembers, const Partial *partials,
+                                 int nparts, cvm_result *out, cudaStream_t st);
+// Stores small host values into device memory through kernel arguments
+// (stream ordered, no host buffer lifetime to manage).
+cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st);
+cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int dh2, int hwp, int cnS,
+                                 cudaStream_t st);
+
+// kernel-launch counter (exported by cvm_launch_count)
+void count_launches(unsigned n);
+
+// per-kernel event timing (exported by cvm_profile_enable/cvm_profile_read)
+void profile_enable(int on);
+int profile_read(int i, char *name, size_t len, double *ms, unsigned long long *count);
+
+}  // namespace cvm

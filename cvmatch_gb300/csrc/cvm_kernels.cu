@@ -1,0 +1,1116 @@
+// cvm_kernels.cu -- sm_103a kernels of the TM_CCOEFF_NORMED path.
+//
+// Arithmetic contract: every float operation below is an explicitly
+// rounded IEEE op (__fadd_rn/__fsub_rn/__fmul_rn/__fdiv_rn/__fsqrt_rn,
+// and the file is built with -fmad=false), grouped exactly like the
+// reference's pinned sequence: the radix-4 butterfly and no-FMA complex
+// multiply of radix4.go:17-32 and 80-149, the R2C untangle of
+// impl.go:331-341, the conj-multiply of impl.go:376-388, the C2R combine of
+// impl.go:405-413 and the normalisation tail of impl.go:816-849.  The
+// schedule (which thread runs which butterfly, the storage order of
+// intermediate rows) is free; the per-element op sequence is not.  The
+// result is the reference's output bit for bit.
+//
+// Kernels (bytes that bound each are per launch; see the design notes):
+//   k_gray            rgbToGray (cvmatch.go:222-240)
+//   k_alpha_scan      alphaConst (cvmatch.go:146-168)
+//   k_tpl_stats       templStats (impl.go:1063-1079), exact u64 atomics
+//   k_params_finalize cn choice (cvmatch.go:82-85, matcher.go:103-112) and the
+//                     templNorm / numScale / varScale constants (impl.go:867-873, 1087)
+//   k_sat_rows/cols   exact summed-area tables replacing colBuildGo/colSlideGo
+//                     (impl.go:708-805)
+//   k_fwd_rows        forwardRowPair (impl.go:301-344) for every tile row pair
+//   k_cols            colsR4Go forward / mulConjGo / colsR4Go inverse
+//                     (radix4cols.go:111-125, impl.go:376-388)
+//   k_inv_rows        inverseRowPair (impl.go:394-444) + channel accumulation
+//                     + normOne (impl.go:825-849) + first-occurrence extrema
+//   k_extrema_final   band merge (impl.go:1104-1112) over CTA partials
+//   k_shrink_gather   shrinkInto (impl.go:591-610)
+#include <cfloat>
+#include <cstdio>
+#include <climits>
+#include <cstdint>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cvm_internal.h"
+
+namespace cvm {
+
+// ------------------------------------------------------------ profiler
+// Optional per-kernel timing: when enabled, every launch is bracketed by a
+// pair of events recorded on its own stream; reading the totals
+// synchronises on the recorded events.  Off by default (no events).
+namespace prof {
+struct Rec {
+    const char *name;
+    cudaEvent_t a, b;
+};
+std::mutex mu;
+bool on = false;
+std::vector<Rec> recs;
+struct Total {
+    std::string name;
+    double ms = 0;
+    unsigned long long n = 0;
+};
+std::vector<Total> totals;
+
+int begin(const char *name, cudaStream_t st) {
+    if (!on) return -1;
+    Rec r{name, nullptr, nullptr};
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, st);
+    std::lock_guard<std::mutex> lk(mu);
+    recs.push_back(r);
+    return (int)recs.size() - 1;
+}
+
+void end(int idx, cudaStream_t st) {
+    if (idx < 0) return;
+    std::lock_guard<std::mutex> lk(mu);
+    cudaEventRecord(recs[idx].b, st);
+}
+
+void collect() {
+    std::lock_guard<std::mutex> lk(mu);
+    for (Rec &r : recs) {
+        cudaEventSynchronize(r.b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+        Total *t = nullptr;
+        for (Total &x : totals)
+            if (x.name == r.name) t = &x;
+        if (!t) {
+            totals.push_back(Total{r.name, 0, 0});
+            t = &totals.back();
+        }
+        t->ms += ms;
+        t->n += 1;
+    }
+    recs.clear();
+}
+}  // namespace prof
+
+struct ProfScope {
+    int idx;
+    cudaStream_t st;
+    ProfScope(const char *name, cudaStream_t s) : idx(prof::begin(name, s)), st(s) {}
+    ~ProfScope() { prof::end(idx, st); }
+};
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int brev_bits(int x, int log2n) {
+    return log2n == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - log2n));
+}
+
+// mulPlain (radix4.go:80-85): four single-rounded products, two sums.
+__device__ __forceinline__ float2 cmul_plain(float2 v, float2 w) {
+    float a = __fmul_rn(v.x, w.x), b = __fmul_rn(v.y, w.y);
+    float c = __fmul_rn(v.x, w.y), d = __fmul_rn(v.y, w.x);
+    return make_float2(__fsub_rn(a, b), __fadd_rn(c, d));
+}
+
+// One radix-4 butterfly (radix4.go:126-147); pa/pc/pb/pd are rows r, r+h,
+// r+2h, r+3h.  The inverse conjugates the twiddles and flips the rotation.
+template <bool INV>
+__device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2 *pd, float2 bw,
+                                      float2 cw, float2 dw) {
+    if (INV) {
+        bw.y = -bw.y;
+        cw.y = -cw.y;
+        dw.y = -dw.y;
+    }
+    const float2 av = *pa;
+    const float2 tb = cmul_plain(*pb, bw);
+    const float2 tc = cmul_plain(*pc, cw);
+    const float2 td = cmul_plain(*pd, dw);
+    const float s0x = __fadd_rn(av.x, tc.x), s0y = __fadd_rn(av.y, tc.y);
+    const float s1x = __fsub_rn(av.x, tc.x), s1y = __fsub_rn(av.y, tc.y);
+    const float s2x = __fadd_rn(tb.x, td.x), s2y = __fadd_rn(tb.y, td.y);
+    const float s3x = __fsub_rn(tb.x, td.x), s3y = __fsub_rn(tb.y, td.y);
+    float rr, ri;
+    if (INV) {
+        rr = -s3y;
+        ri = s3x;
+    } else {
+        rr = s3y;
+        ri = -s3x;
+    }
+    *pa = make_float2(__fadd_rn(s0x, s2x), __fadd_rn(s0y, s2y));
+    *pc = make_float2(__fadd_rn(s1x, rr), __fadd_rn(s1y, ri));
+    *pb = make_float2(__fsub_rn(s0x, s2x), __fsub_rn(s0y, s2y));
+    *pd = make_float2(__fsub_rn(s1x, rr), __fsub_rn(s1y, ri));
+}
+
+// The radix-4 cascade (fftR4Scalar, radix4.go:106-149) over `lines`
+// contiguous rows of n elements (row stride ld) in shared memory, input in
+// bit-reversed order.  Each stage is one barrier-separated sweep; a thread
+// owns whole butterflies.
+template <bool INV>
+__device__ void fft_lines(float2 *s, int n, int log2n, int lines, int ld,
+                          const float2 *__restrict__ tri) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    int h = 1;
+    if (log2n & 1) {
+        const int half = n >> 1;
+        const int tot = half * lines;
+        for (int b = tid; b < tot; b += nt) {
+            const int line = b >> (log2n - 1);
+            const int i = (b & (half - 1)) << 1;
+            float2 *a = s + line * ld + i;
+            const float2 u = a[0], v = a[1];
+            a[0] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+            a[1] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+        }
+        __syncthreads();
+        h = 2;
+    }
+    const float2 *t = tri;
+    for (; 4 * h <= n; h <<= 2) {
+        const int quarter = n >> 2;
+        const int tot = quarter * lines;
+        for (int b = tid; b < tot; b += nt) {
+            const int line = b >> (log2n - 2);
+            const int q = b & (quarter - 1);
+            const int j = q & (h - 1);
+            float2 *a = s + line * ld + ((q - j) << 2) + j;
+            bfly4<INV>(a, a + h, a + 2 * h, a + 3 * h, __ldg(t + j), __ldg(t + h + j),
+                       __ldg(t + 2 * h + j));
+        }
+        t += 3 * h;
+        __syncthreads();
+    }
+}
+
+// The column twin (colsR4Go, radix4cols.go:35-125) on a [n x SC] strip in
+// shared memory, element (row r, column c) at s[r*SC + c].  RMAP conjugates
+// every row access by the bit reversal (the inverse path's rmap = brev).
+template <bool INV, bool RMAP>
+__device__ void fft_cols(float2 *s, int n, int log2n, int SC, int logSC,
+                         const float2 *__restrict__ tri) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    int h = 1;
+    if (log2n & 1) {
+        const int tot = (n >> 1) << logSC;
+        for (int b = tid; b < tot; b += nt) {
+            const int c = b & (SC - 1);
+            const int r = (b >> logSC) << 1;
+            int i0 = r, i1 = r + 1;
+            if (RMAP) {
+                i0 = brev_bits(i0, log2n);
+                i1 = brev_bits(i1, log2n);
+            }
+            float2 *p = s + i0 * SC + c, *q = s + i1 * SC + c;
+            const float2 u = *p, v = *q;
+            *p = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+            *q = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+        }
+        __syncthreads();
+        h = 2;
+    }
+    const float2 *t = tri;
+    for (; 4 * h <= n; h <<= 2) {
+        const int tot = (n >> 2) << logSC;
+        for (int b = tid; b < tot; b += nt) {
+            const int c = b & (SC - 1);
+            const int q = b >> logSC;
+            const int j = q & (h - 1);
+            const int r = ((q - j) << 2) + j;
+            int i0 = r, i1 = r + h, i2 = r + 2 * h, i3 = r + 3 * h;
+            if (RMAP) {
+                i0 = brev_bits(i0, log2n);
+                i1 = brev_bits(i1, log2n);
+                i2 = brev_bits(i2, log2n);
+                i3 = brev_bits(i3, log2n);
+            }
+            bfly4<INV>(s + i0 * SC + c, s + i1 * SC + c, s + i2 * SC + c, s + i3 * SC + c,
+                       __ldg(t + j), __ldg(t + h + j), __ldg(t + 2 * h + j));
+        }
+        t += 3 * h;
+        __syncthreads();
+    }
+}
+
+struct TileBox {
+    int x0, y0, bw, bh, loadW, loadH;
+};
+
+__device__ __forceinline__ TileBox tile_box(const TileGeom &g, int tile) {
+    TileBox b;
+    const int tx = tile % g.ntx, ty = tile / g.ntx;
+    b.x0 = tx * g.blockW;
+    b.y0 = ty * g.blockH;
+    b.bw = min(g.blockW, g.rwT - b.x0);
+    b.bh = min(g.blockH, g.rhT - b.y0);
+    b.loadW = b.bw + g.twL - 1;
+    b.loadH = b.bh + g.thL - 1;
+    return b;
+}
+
+// ------------------------------------------------------------ gray/alpha
+
+__global__ void k_gray(const uint8_t *__restrict__ src, long long sstride, int w, int h,
+                       uint8_t *__restrict__ dst, long long dstride) {
+    const int y = blockIdx.y;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < w; x += gridDim.x * blockDim.x) {
+        const uint8_t *p = src + (long long)y * sstride + 4LL * x;
+        const uint32_t r = p[0], g = p[1], b = p[2];
+        dst[(long long)y * dstride + x] = (uint8_t)((4899u * r + 9617u * g + 1868u * b + 8192u) >> 14);
+    }
+}
+
+__global__ void k_alpha_scan(const uint8_t *__restrict__ img, long long stride, int w, int h,
+                             unsigned int *mismatch) {
+    const uint8_t a0 = img[3];
+    const int y = blockIdx.y;
+    bool bad = false;
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < w; x += gridDim.x * blockDim.x)
+        bad |= img[(long long)y * stride + 4LL * x + 3] != a0;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(mismatch, 1u);
+}
+
+// ------------------------------------------------------------ statistics
+
+// Exact per-channel template sums and squared sums (templStats,
+// impl.go:1063-1079) plus the template's alpha-constancy flag.
+__global__ void k_tpl_stats(const uint8_t *__restrict__ tpl, long long tstride, int tw, int th,
+                            int step, int cnStats, DevParams *P) {
+    unsigned long long s[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+    bool bad = false;
+    const uint8_t a0 = step == 4 ? tpl[3] : 0;
+    const long long total = (long long)tw * th;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / tw), x = (int)(i - (long long)y * tw);
+        const uint8_t *p = tpl + (long long)y * tstride + (long long)x * step;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (k < cnStats) {
+                const unsigned v = p[k];
+                s[k] += v;
+                q[k] += v * v;
+            }
+        if (step == 4) bad |= p[3] != a0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+            q[k] += __shfl_down_sync(0xffffffffu, q[k], o);
+        }
+    const bool anyBad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < cnStats; k++) {
+            if (s[k]) atomicAdd(&P->tsum[k], s[k]);
+            if (q[k]) atomicAdd(&P->tsq[k], q[k]);
+        }
+        if (anyBad) atomicOr(&P->alphaMismatch, 1u);
+    }
+}
+
+// Chooses the effective channel count and derives the tail constants with
+// the reference's double-precision sequences (impl.go:867-873, 1087).
+__global__ void k_params_finalize(DevParams *P, int n, DevFrame *F) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    DevParams &p = P[i];
+    int cn = p.cnFixed;
+    if (p.mode == 1) cn = (p.alphaMismatch == 0 && F->alphaMismatch == 0) ? 3 : 4;
+    const long long area = (long long)p.tw * p.th;
+    long long vs = 0;
+    for (int k = 0; k < cn; k++) {
+        const long long s = (long long)p.tsum[k];
+        vs += area * (long long)p.tsq[k] - s * s;
+    }
+    p.cn = cn;
+    p.varSum = vs;
+    p.flat = vs == 0;
+    const double ad = __dmul_rn((double)p.tw, (double)p.th);
+    p.templNorm = __double2float_rn(__dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad)));
+    p.varScale = __double2float_rn(__ddiv_rn(1.0, ad));
+    p.numScale = cn == 1 ? __double2float_rn(__ddiv_rn(__ll2double_rn((long long)p.tsum[0]), ad))
+                         : p.varScale;
+    if (!p.flat) atomicMax(&F->cnMax, cn);
+}
+
+// ----------------------------------------------------------------- SAT
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const T u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+// Row prefix sums: one warp per image row, 32 pixels per step with a
+// carried total.  Writes plane row y+1 (column 0 and plane row 0 are 0).
+// Also flags a non-constant alpha plane (alphaConst).
+__global__ void k_sat_rows(const uint8_t *__restrict__ img, long long istride, int step,
+                           SatPlanes S, unsigned int *alphaMismatch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = blockIdx.x * (blockDim.x >> 5) + warp;
+    const long long P = S.pitch;
+    if (blockIdx.x == 0 && warp == 0) {
+        for (int x = lane; x <= S.iw; x += 32) {
+            for (int k = 0; k < S.nsum; k++) S.sum[k][x] = 0u;
+            S.sq[x] = 0ull;
+            if (S.sqA) S.sqA[x] = 0ull;
+        }
+    }
+    if (y >= S.ih) return;
+    const uint8_t *row = img + (long long)y * istride;
+    const long long o = (long long)(y + 1) * P;
+    if (lane == 0) {
+        for (int k = 0; k < S.nsum; k++) S.sum[k][o] = 0u;
+        S.sq[o] = 0ull;
+        if (S.sqA) S.sqA[o] = 0ull;
+    }
+    const uint8_t a0 = img[3];
+    const int nsq = S.nsum < 4 ? S.nsum : 3;
+    unsigned int carry[4] = {0u, 0u, 0u, 0u};
+    unsigned long long carrySq = 0ull, carryA = 0ull;
+    bool bad = false;
+    for (int xb = 0; xb < S.iw; xb += 32) {
+        const int x = xb + lane;
+        unsigned int v[4] = {0u, 0u, 0u, 0u};
+        if (x < S.iw) {
+            const uint8_t *p = row + (long long)x * step;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (k < S.nsum) v[k] = p[k];
+            if (alphaMismatch && step == 4) bad |= p[3] != a0;
+        }
+        unsigned long long sq = 0ull;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (k < nsq) sq += (unsigned long long)(v[k] * v[k]);
+        unsigned long long sa = S.sqA ? (unsigned long long)(v[3] * v[3]) : 0ull;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (k < S.nsum) {
+                const unsigned int incl = warp_incl_scan(v[k]) + carry[k];
+                if (x < S.iw) S.sum[k][o + x + 1] = incl;
+                carry[k] = __shfl_sync(0xffffffffu, incl, 31);
+            }
+        {
+            const unsigned long long incl = warp_incl_scan(sq) + carrySq;
+            if (x < S.iw) S.sq[o + x + 1] = incl;
+            carrySq = __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (S.sqA) {
+            const unsigned long long incl = warp_incl_scan(sa) + carryA;
+            if (x < S.iw) S.sqA[o + x + 1] = incl;
+            carryA = __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    if (alphaMismatch && __any_sync(0xffffffffu, bad) && lane == 0) atomicOr(alphaMismatch, 1u);
+}
+
+// Column prefix sums over plane rows 1..ih: a CTA owns 32 columns of one
+// plane and splits the rows into kChunks chunks (two passes).
+constexpr int kSatChunks = 16;
+
+template <typename T>
+struct PlanePtrs {
+    T *p[4];
+};
+
+template <typename T>
+__global__ void k_sat_cols(PlanePtrs<T> planes, long long pitch, int iw, int ih) {
+    __shared__ T part[kSatChunks][32];
+    T *plane = planes.p[blockIdx.y];
+    const int c = threadIdx.x & 31, chunk = threadIdx.x >> 5;
+    const int x = blockIdx.x * 32 + c + 1;  // plane column
+    const int R = (ih + kSatChunks - 1) / kSatChunks;
+    const int r0 = 1 + chunk * R, r1 = min(ih, chunk * R + R);  // plane rows r0..r1
+    T acc = 0;
+    if (x <= iw)
+        for (int r = r0; r <= r1; r++) acc += plane[(long long)r * pitch + x];
+    part[chunk][c] = acc;
+    __syncthreads();
+    if (x > iw) return;
+    T run = 0;
+    for (int k = 0; k < chunk; k++) run += part[k][c];
+    for (int r = r0; r <= r1; r++) {
+        T *e = plane + (long long)r * pitch + x;
+        run += *e;
+        *e = run;
+    }
+}
+
+// --------------------------------------------------------- forward rows
+
+// forwardRowPair (impl.go:301-344) for P row pairs x C channels of one
+// tile: pack two image rows into one complex row, transform, untangle into
+// the two real-row spectra at their bit-reversed column-FFT slots.
+__global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, int step,
+                           int chanCount, const int *cnDev, int chanFirst, int chanGroup, TileGeom g,
+                           FftClass fc, float2 *__restrict__ spec, int cnS, int pairsPerCta) {
+    extern __shared__ float2 smem[];
+    const int tile = fc.tileFirst + blockIdx.y;
+    const TileBox b = tile_box(g, tile);
+    const int nrows = min(b.loadH, fc.dftH);
+    const int pair0 = blockIdx.x * pairsPerCta;
+    if (2 * pair0 >= nrows) return;
+    const int cnEff = cnDev ? min(*cnDev, chanCount) : chanCount;
+    const int cn = min(cnEff - chanFirst, chanGroup);  // channels of this launch's group
+    if (cn <= 0) return;
+    const int P = min(pairsPerCta, (nrows - 2 * pair0 + 1) >> 1);
+    const int lines = P * cn;
+    const int n = fc.n, log2n = fc.log2n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long rowBase = (long long)b.y0 * istride + (long long)b.x0 * step;
+    for (int idx = tid; idx < lines * n; idx += nt) {
+        const int line = idx >> log2n, x = idx & (n - 1);
+        const int p = line / cn, k = chanFirst + line - p * cn;
+        const int r = 2 * (pair0 + p);
+        float2 v = make_float2(0.f, 0.f);
+        if (x < b.loadW) {
+            const uint8_t *pa = img + rowBase + (long long)r * istride + (long long)x * step + k;
+            v.x = (float)pa[0];
+            if (r + 1 < b.loadH) v.y = (float)pa[istride];
+        }
+        smem[line * n + brev_bits(x, log2n)] = v;
+    }
+    __syncthreads();
+    fft_lines<false>(smem, n, log2n, lines, n, fc.triW);
+    const int hw = fc.hw, mask = n - 1;
+    const size_t chanStride = (size_t)fc.dftH * fc.hwp;
+    float2 *tbase = spec + (size_t)(tile - fc.tileFirst) * cnS * chanStride;
+    for (int idx = tid; idx < lines * hw; idx += nt) {
+        const int line = idx / hw, kk = idx - line * hw;
+        const int p = line / cn, k = chanFirst + line - p * cn;
+        const int r = 2 * (pair0 + p);
+        const float2 zk = smem[line * n + kk], zn = smem[line * n + ((n - kk) & mask)];
+        float2 *cb = tbase + (size_t)k * chanStride;
+        cb[(size_t)brev_bits(r, fc.log2H) * fc.hwp + kk] =
+            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
+        cb[(size_t)brev_bits(r + 1, fc.log2H) * fc.hwp + kk] =
+            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zn.y)), __fmul_rn(0.5f, __fsub_rn(zn.x, zk.x)));
+    }
+}
+
+// --------------------------------------------------------------- columns
+
+struct ColsArgs {
+    int mode;
+    const float2 *in;
+    float2 *out;
+    int cnS;
+    TileGeom g;
+    FftClass fc;
+    int cls;
+    int chanCount;
+    const int *cnDev;
+    float scale;
+    MemberSet ms;
+    int SC, logSC;
+};
+
+__device__ __forceinline__ const DevMember &member_of(const MemberSet &ms, int slot) {
+    return ms.table ? ms.table[ms.first + slot] : ms.solo;
+}
+
+// Column pass over one [dftH x SC] strip of one (member, tile, channel).
+__global__ void k_cols(ColsArgs a) {
+    extern __shared__ float2 smem[];
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.z % fc.ntiles;
+    const int slot = blockIdx.z / fc.ntiles;
+    const int tile = fc.tileFirst + tileLocal;
+    const int k = blockIdx.y;
+    const DevMember *m = a.mode == 0 ? nullptr : &member_of(a.ms, slot);
+    const DevParams *Pm = m ? a.ms.params + m->pIdx : nullptr;
+    int cn;
+    if (m)
+        cn = Pm->cn;
+    else
+        cn = a.cnDev ? min(*a.cnDev, a.chanCount) : a.chanCount;
+    if (k >= cn) return;
+    if (Pm && Pm->flat) return;
+    const int SC = a.SC, logSC = a.logSC;
+    const int c0 = blockIdx.x * SC;
+    const int H = fc.dftH, log2H = fc.log2H, hwp = fc.hwp;
+    const int wv = min(SC, fc.hw - c0);
+    const size_t chanStride = (size_t)H * hwp;
+    const TileBox b = tile_box(a.g, tile);
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    const float2 *src = a.in + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+    if (a.mode == 2) {
+        // Natural-order forward spectrum of the frame tile.
+        for (int idx = tid; idx < (H << logSC); idx += nt) {
+            const int r = idx >> logSC, c = idx & (SC - 1);
+            smem[idx] = c < wv ? src[(size_t)r * hwp + c] : make_float2(0.f, 0.f);
+        }
+    } else {
+        // Forward-rows output: logical row brev(s) sits at slot s; rows at or
+        // past `loaded` were never written and are zero (impl.go:352-356).
+        const int loaded = min(H, (b.loadH + 1) & ~1);
+        for (int idx = tid; idx < (H << logSC); idx += nt) {
+            const int s = idx >> logSC, c = idx & (SC - 1);
+            float2 v = make_float2(0.f, 0.f);
+            if (c < wv && brev_bits(s, log2H) < loaded) v = src[(size_t)s * hwp + c];
+            smem[idx] = v;
+        }
+    }
+    __syncthreads();
+    if (a.mode != 2) fft_cols<false, false>(smem, H, log2H, SC, logSC, fc.triH);
+    if (a.mode == 0) {
+        float2 *dst = a.out + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+        const float sc = a.scale;
+        for (int idx = tid; idx < (H << logSC); idx += nt) {
+            const int r = idx >> logSC, c = idx & (SC - 1);
+            if (c < wv) {
+                float2 v = smem[idx];
+                if (sc != 1.0f) v = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+                dst[(size_t)r * hwp + c] = v;
+            }
+        }
+        return;
+    }
+    // spec *= conj(tspec) (mulConjGo, impl.go:376-388), natural order.
+    const float2 *ts = m->tspec[a.cls] + (size_t)k * chanStride + c0;
+    for (int idx = tid; idx < (H << logSC); idx += nt) {
+        const int r = idx >> logSC, c = idx & (SC - 1);
+        if (c < wv) {
+            const float2 av = smem[idx], bv = __ldg(ts + (size_t)r * hwp + c);
+            const float re = __fadd_rn(__fmul_rn(av.x, bv.x), __fmul_rn(av.y, bv.y));
+            const float im = __fsub_rn(__fmul_rn(av.y, bv.x), __fmul_rn(av.x, bv.y));
+            smem[idx] = make_float2(re, im);
+        }
+    }
+    __syncthreads();
+    fft_cols<true, true>(smem, H, log2H, SC, logSC, fc.triH);
+    // Spatial row y now sits at slot brev(y); the inverse rows read rows
+    // y < bh (rounded up to the row pair).
+    const int ty = tile / a.g.ntx;
+    const int bh = (ty == a.g.nty - 1) ? m->rh - b.y0 : a.g.blockH;
+    const int rowsOut = min(H, (bh + 1) & ~1);
+    float2 *dst = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] +
+                  ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+    for (int idx = tid; idx < (H << logSC); idx += nt) {
+        const int s = idx >> logSC, c = idx & (SC - 1);
+        if (c < wv && brev_bits(s, log2H) < rowsOut) dst[(size_t)s * hwp + c] = smem[idx];
+    }
+}
+
+// ------------------------------------------------------- inverse rows
+
+__device__ __forceinline__ long long win_u32(const unsigned int *__restrict__ p, long long P, int X,
+                                             int Y, int tw, int th) {
+    const unsigned int a = __ldg(p + (long long)(Y + th) * P + X + tw);
+    const unsigned int b = __ldg(p + (long long)(Y + th) * P + X);
+    const unsigned int c = __ldg(p + (long long)Y * P + X + tw);
+    const unsigned int d = __ldg(p + (long long)Y * P + X);
+    return (long long)(unsigned int)(a - b - c + d);
+}
+
+__device__ __forceinline__ long long win_u64(const unsigned long long *__restrict__ p, long long P,
+                                             int X, int Y, int tw, int th) {
+    const unsigned long long a = __ldg(p + (long long)(Y + th) * P + X + tw);
+    const unsigned long long b = __ldg(p + (long long)(Y + th) * P + X);
+    const unsigned long long c = __ldg(p + (long long)Y * P + X + tw);
+    const unsigned long long d = __ldg(p + (long long)Y * P + X);
+    return (long long)(a - b - c + d);
+}
+
+// float32(float64(v)) (impl.go:902-1009): two roundings, as pinned.
+__device__ __forceinline__ float f32_via_f64(long long v) {
+    return __double2float_rn(__ll2double_rn(v));
+}
+
+// normOne (impl.go:825-849).
+__device__ __forceinline__ float norm_one(float num, float lane0, float idiff, float s2,
+                                          float numScale, float varScale, float templNorm) {
+    const float eps = 1.1920928955078125e-06f;  // 10 * 2^-23, exact in float32
+    num = __fsub_rn(num, __fmul_rn(lane0, numScale));
+    const float diff2 = __fmul_rn(idiff, varScale);
+    float lim = __fmul_rn(eps, s2);
+    if (lim > 0.5f) lim = 0.5f;
+    float den = 0.f;
+    if (diff2 > lim) den = __fmul_rn(__fsqrt_rn(diff2), templNorm);
+    const float an = fabsf(num);
+    if (an < den) return __fdiv_rn(num, den);
+    if (an < __fmul_rn(den, 1.125f)) return num > 0.f ? 1.f : -1.f;
+    return 0.f;
+}
+
+struct Ext {
+    float minV, maxV;
+    long long minI, maxI;
+};
+
+__device__ __forceinline__ void ext_init(Ext &e) {
+    e.minV = FLT_MAX;
+    e.maxV = -FLT_MAX;
+    e.minI = LLONG_MAX;
+    e.maxI = LLONG_MAX;
+}
+
+// First occurrence in raster order with strict compares (impl.go:1023-1047,
+// 1104-1112): a smaller value, or an equal value at a smaller index.
+__device__ __forceinline__ void ext_add(Ext &e, float v, long long i) {
+    if (v < e.minV || (v == e.minV && i < e.minI)) {
+        e.minV = v;
+        e.minI = i;
+    }
+    if (v > e.maxV || (v == e.maxV && i < e.maxI)) {
+        e.maxV = v;
+        e.maxI = i;
+    }
+}
+
+__device__ __forceinline__ void ext_merge(Ext &e, const Ext &o) {
+    if (o.minV < e.minV || (o.minV == e.minV && o.minI < e.minI)) {
+        e.minV = o.minV;
+        e.minI = o.minI;
+    }
+    if (o.maxV > e.maxV || (o.maxV == e.maxV && o.maxI < e.maxI)) {
+        e.maxV = o.maxV;
+        e.maxI = o.maxI;
+    }
+}
+
+__device__ void ext_block_reduce(Ext &e, Ext *sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        Ext t;
+        t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
+        t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
+        t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
+        t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
+        ext_merge(e, t);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[warp] = e;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        if (lane < nw)
+            e = sh[lane];
+        else
+            ext_init(e);
+        for (int o = 16; o > 0; o >>= 1) {
+            Ext t;
+            t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
+            t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
+            t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
+            t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
+            ext_merge(e, t);
+        }
+    }
+}
+
+struct InvArgs {
+    TileGeom g;
+    FftClass fc;
+    int cls, cnS;
+    MemberSet ms;
+    SatPlanes S;
+    Partial *partials;
+    int ctasPerTile, pairsPerCta, partOffset;
+};
+
+// inverseRowPair (impl.go:394-444) for P row pairs of one (member, tile),
+// all channels accumulated in channel order, then normOne per element and
+// the CTA's first-occurrence extrema.
+__global__ void k_inv_rows(InvArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ Ext shExt[kThreads / 32];
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.y;
+    const int tile = fc.tileFirst + tileLocal;
+    const int slot = blockIdx.z;
+    const DevMember &m = member_of(a.ms, slot);
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    const TileBox tb = tile_box(a.g, tile);
+    const int tx = tile % a.g.ntx, ty = tile / a.g.ntx;
+    const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
+    const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
+    const int pair0 = blockIdx.x * a.pairsPerCta;
+    const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    Ext e;
+    ext_init(e);
+    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * n);  // [P][2][n]
+    if (P > 0) {
+        const int cn = Pm.cn;
+        const bool flat = Pm.flat != 0;
+        const size_t chanStride = (size_t)fc.dftH * hwp;
+        const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
+        if (!flat) {
+            for (int k = 0; k < cn; k++) {
+                const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
+                for (int idx = tid; idx < P * n; idx += nt) {
+                    const int p = idx >> log2n, kk = idx & (n - 1);
+                    const int r = 2 * (pair0 + p);
+                    const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
+                    const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
+                    float2 z;
+                    if (kk < hw) {
+                        const float2 u = sa[kk], v = sb[kk];
+                        z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+                    } else {
+                        const int mm = n - kk;
+                        const float2 u = sa[mm], v = sb[mm];
+                        z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+                    }
+                    smem[p * n + brev_bits(kk, log2n)] = z;
+                }
+                __syncthreads();
+                fft_lines<true>(smem, n, log2n, P, n, fc.triW);
+                for (int idx = tid; idx < P * bw; idx += nt) {
+                    const int p = idx / bw, x = idx - p * bw;
+                    const float2 z = smem[p * n + x];
+                    float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
+                    if (k == 0) {
+                        *a0 = z.x;
+                        *a1 = z.y;
+                    } else {
+                        *a0 = __fadd_rn(*a0, z.x);
+                        *a1 = __fadd_rn(*a1, z.y);
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // Normalisation + extrema over the P row pairs.
+        const long long area = (long long)m.tw * m.th;
+        const SatPlanes &S = a.S;
+        for (int idx = tid; idx < 2 * P * bw; idx += nt) {
+            const int rr = idx / bw, x = idx - rr * bw;
+            const int r = 2 * pair0 + rr;
+            if (r >= bh) continue;
+            const int X = tb.x0 + x, Y = tb.y0 + r;
+            float score;
+            if (flat) {
+                score = 1.f;
+            } else {
+                const float corr = acc[(size_t)rr * n + x];
+                long long s[4] = {0, 0, 0, 0};
+                long long cross = 0, sq = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (k < cn) {
+                        s[k] = win_u32(S.sum[k], S.pitch, X, Y, m.tw, m.th);
+                        cross += s[k] * (long long)Pm.tsum[k];
+                        sq += s[k] * s[k];
+                    }
+                long long s2 = win_u64(S.sq, S.pitch, X, Y, m.tw, m.th);
+                if (cn == 4) s2 += win_u64(S.sqA, S.pitch, X, Y, m.tw, m.th);
+                const long long lane0 = cn == 1 ? s[0] : cross;
+                score = norm_one(corr, f32_via_f64(lane0), f32_via_f64(area * s2 - sq), f32_via_f64(s2),
+                                 Pm.numScale, Pm.varScale, Pm.templNorm);
+            }
+            const long long li = (long long)Y * m.rw + X;
+            if (a.ms.map) a.ms.map[li] = score;
+            ext_add(e, score, li);
+        }
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (tid == 0) {
+        Partial &o = a.partials[m.partBase + a.partOffset + blockIdx.y * a.ctasPerTile + blockIdx.x];
+        o.minV = e.minV;
+        o.maxV = e.maxV;
+        o.minI = e.minI;
+        o.maxI = e.maxI;
+    }
+}
+
+__global__ void k_extrema_final(MemberSet ms, const Partial *partials, int nparts, cvm_result *out) {
+    __shared__ Ext shExt[kThreads / 32];
+    const DevMember &m = member_of(ms, blockIdx.x);
+    Ext e;
+    ext_init(e);
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        const Partial &p = partials[m.partBase + i];
+        Ext o;
+        o.minV = p.minV;
+        o.maxV = p.maxV;
+        o.minI = p.minI;
+        o.maxI = p.maxI;
+        ext_merge(e, o);
+    }
+    ext_block_reduce(e, shExt);
+    if (threadIdx.x == 0) {
+        cvm_result r;
+        r.min_v = e.minV;
+        r.max_v = e.maxV;
+        r.min_x = (int32_t)(e.minI % m.rw);
+        r.min_y = (int32_t)(e.minI / m.rw);
+        r.max_x = (int32_t)(e.maxI % m.rw);
+        r.max_y = (int32_t)(e.maxI / m.rw);
+        out[m.outIdx] = r;
+    }
+}
+
+// Small host values to device memory through kernel arguments.
+struct UploadBlob {
+    unsigned char bytes[3072];
+};
+
+__global__ void k_upload(unsigned char *dst, UploadBlob b, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = b.bytes[i];
+}
+
+// shrinkInto (impl.go:591-610): the shrunk band's spectrum is the
+// stride-2^s row gather of the full one times 2^s (exact).
+__global__ void k_shrink_gather(const float2 *__restrict__ src, int dftH, float2 *__restrict__ dst,
+                                int dh2, int hwp, int cnS) {
+    const int shift = __ffs(dftH) - __ffs(dh2);
+    const float up = (float)(1 << shift);
+    const long long total = (long long)cnS * dh2 * hwp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % hwp);
+        const long long kr = i / hwp;
+        const int r = (int)(kr % dh2), k = (int)(kr / dh2);
+        const float2 v = src[((size_t)k * dftH + ((size_t)r << shift)) * hwp + x];
+        dst[i] = make_float2(__fmul_rn(v.x, up), __fmul_rn(v.y, up));
+    }
+}
+
+template <typename K>
+void set_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int ilog2i(int v) {
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return l;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- launches
+
+cudaError_t launch_gray(const uint8_t *src, long long sstride, int w, int h, uint8_t *dst,
+                        long long dstride, cudaStream_t st) {
+    dim3 grid((w + kThreads - 1) / kThreads, h);
+    ProfScope ps("k_gray", st);
+    k_gray<<<grid, kThreads, 0, st>>>(src, sstride, w, h, dst, dstride);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_scan(const uint8_t *img, long long stride, int w, int h,
+                              unsigned int *mismatch, cudaStream_t st) {
+    dim3 grid((w + kThreads - 1) / kThreads, h);
+    ProfScope ps("k_alpha_scan", st);
+    k_alpha_scan<<<grid, kThreads, 0, st>>>(img, stride, w, h, mismatch);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tpl_stats(const uint8_t *tpl, long long tstride, int tw, int th, int step,
+                             int cnStats, DevParams *P, cudaStream_t st) {
+    const long long total = (long long)tw * th;
+    int blocks = (int)((total + kThreads - 1) / kThreads);
+    if (blocks > 1024) blocks = 1024;
+    ProfScope ps("k_tpl_stats", st);
+    k_tpl_stats<<<blocks, kThreads, 0, st>>>(tpl, tstride, tw, th, step, cnStats, P);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_params_finalize(DevParams *P, int n, DevFrame *F, cudaStream_t st) {
+    ProfScope ps("k_params_finalize", st);
+    k_params_finalize<<<(n + 127) / 128, 128, 0, st>>>(P, n, F);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sat(const uint8_t *img, long long istride, int step, const SatPlanes &S,
+                       unsigned int *alphaMismatch, cudaStream_t st) {
+    const int rowsPerCta = kThreads / 32;
+    {
+    ProfScope ps("k_sat_rows", st);
+    k_sat_rows<<<(S.ih + rowsPerCta - 1) / rowsPerCta, kThreads, 0, st>>>(img, istride, step, S,
+                                                                            alphaMismatch);
+    }
+    count_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 block(32 * kSatChunks);
+    PlanePtrs<unsigned int> sp;
+    for (int k = 0; k < 4; k++) sp.p[k] = S.sum[k];
+    ProfScope ps("k_sat_cols", st);
+    dim3 g1((S.iw + 31) / 32, S.nsum);
+    k_sat_cols<unsigned int><<<g1, block, 0, st>>>(sp, S.pitch, S.iw, S.ih);
+    PlanePtrs<unsigned long long> qp;
+    qp.p[0] = S.sq;
+    qp.p[1] = S.sqA;
+    qp.p[2] = qp.p[3] = nullptr;
+    dim3 g2((S.iw + 31) / 32, S.sqA ? 2 : 1);
+    k_sat_cols<unsigned long long><<<g2, block, 0, st>>>(qp, S.pitch, S.iw, S.ih);
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
+                            const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
+                            int cnS, cudaStream_t st) {
+    // Channels per launch so that one row pair of the group fits 128 KB of
+    // shared memory; row pairs per CTA fill ~32 KB when rows are short.
+    int group = 16384 / fc.n;
+    if (group < 1) group = 1;
+    if (group > chanCount) group = chanCount;
+    int P = 4096 / (fc.n * group);
+    if (P < 1) P = 1;
+    // Largest row count of any tile: blockH + thL - 1, capped by dftH.
+    int maxRows = g.blockH + g.thL - 1;
+    if (maxRows > fc.dftH) maxRows = fc.dftH;
+    const int pairs = (maxRows + 1) / 2;
+    dim3 grid((pairs + P - 1) / P, fc.ntiles);
+    const size_t smem = (size_t)P * group * fc.n * sizeof(float2);
+    set_smem(k_fwd_rows, smem);
+    ProfScope ps("k_fwd_rows", st);
+    for (int c0 = 0; c0 < chanCount; c0 += group) {
+        k_fwd_rows<<<grid, kThreads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
+                                                  spec, cnS, P);
+        count_launches(1);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
+                        const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
+                        const MemberSet &ms, int nmembers, cudaStream_t st) {
+    ColsArgs a;
+    a.mode = mode;
+    a.in = in;
+    a.out = out;
+    a.cnS = cnS;
+    a.g = g;
+    a.fc = fc;
+    a.cls = cls;
+    a.chanCount = chanCount;
+    a.cnDev = cnDev;
+    a.scale = scale;
+    a.ms = ms;
+    int SC = 8192 / fc.dftH;
+    if (SC > 16) SC = 16;
+    if (SC < 1) SC = 1;
+    a.SC = SC;
+    a.logSC = ilog2i(SC);
+    dim3 grid((fc.hw + SC - 1) / SC, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
+    const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
+    set_smem(k_cols, smem);
+    ProfScope ps(mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv"), st);
+    k_cols<<<grid, kThreads, smem, st>>>(a);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta) {
+    int P = 2048 / fc.n;
+    if (P < 1) P = 1;
+    // A tile emits at most dftH rows (a fleet member's last band extends to
+    // its own result edge, still inside the loaded rows <= dftH).
+    const int pairs = (fc.dftH + 1) / 2;
+    *pairsPerCta = P;
+    return (pairs + P - 1) / P;
+}
+
+cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS,
+                            const MemberSet &ms, int nmembers, const SatPlanes &S,
+                            Partial *partials, int partOffset, int ctasPerTile, int pairsPerCta,
+                            cudaStream_t st) {
+    InvArgs a;
+    a.g = g;
+    a.fc = fc;
+    a.cls = cls;
+    a.cnS = cnS;
+    a.ms = ms;
+    a.S = S;
+    a.partials = partials;
+    a.partOffset = partOffset;
+    a.ctasPerTile = ctasPerTile;
+    a.pairsPerCta = pairsPerCta;
+    dim3 grid(ctasPerTile, fc.ntiles, nmembers);
+    const size_t smem = (size_t)pairsPerCta * fc.n * (sizeof(float2) + 2 * sizeof(float));
+    set_smem(k_inv_rows, smem);
+    ProfScope ps("k_inv_rows", st);
+    k_inv_rows<<<grid, kThreads, smem, st>>>(a);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extrema_final(const MemberSet &ms, int nmembers, const Partial *partials,
+                                 int nparts, cvm_result *out, cudaStream_t st) {
+    ProfScope ps("k_extrema_final", st);
+    k_extrema_final<<<nmembers, kThreads, 0, st>>>(ms, partials, nparts, out);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st) {
+    const unsigned char *p = static_cast<const unsigned char *>(src);
+    unsigned char *d = static_cast<unsigned char *>(dst);
+    while (n > 0) {
+        UploadBlob b;
+        const size_t c = n < sizeof(b.bytes) ? n : sizeof(b.bytes);
+        for (size_t i = 0; i < c; i++) b.bytes[i] = p[i];
+        {
+            ProfScope ps("k_upload", st);
+            k_upload<<<1, 256, 0, st>>>(d, b, (int)c);
+        }
+        count_launches(1);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        p += c;
+        d += c;
+        n -= c;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int dh2, int hwp, int cnS,
+                                 cudaStream_t st) {
+    const long long total = (long long)cnS * dh2 * hwp;
+    int blocks = (int)((total + kThreads - 1) / kThreads);
+    if (blocks > 4096) blocks = 4096;
+    ProfScope ps("k_shrink_gather", st);
+    k_shrink_gather<<<blocks, kThreads, 0, st>>>(src, dftH, dst, dh2, hwp, cnS);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+void profile_enable(int on) {
+    std::lock_guard<std::mutex> lk(prof::mu);
+    prof::on = on != 0;
+    if (on) prof::totals.clear();
+}
+
+int profile_read(int i, char *name, size_t len, double *ms, unsigned long long *count) {
+    prof::collect();
+    std::lock_guard<std::mutex> lk(prof::mu);
+    if (i < 0 || i >= (int)prof::totals.size()) return 1;
+    const prof::Total &t = prof::totals[i];
+    if (name && len) {
+        snprintf(name, len, "%s", t.name.c_str());
+    }
+    *ms = t.ms;
+    *count = t.n;
+    return 0;
+}
+
+}  // namespace cvm

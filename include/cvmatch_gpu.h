@@ -1,0 +1,182 @@
+/*
+ * cvmatch_gpu.h -- C ABI of the GB300 (sm_103a) TM_CCOEFF_NORMED engine.
+ *
+ * This is the boundary a cgo shim binds in place of cvmatch's Go core
+ * (L3-L1: impl.go, radix4.go, radix4cols.go, internal/simd).  The Go
+ * package keeps its public API and its image adaptation (toRGBA/toGray,
+ * cvmatch.go:186-217) and passes raw (pointer, stride, width, height)
+ * views across; nothing here takes Go or torch types.
+ *
+ * Conventions
+ *   - Every function returns CVM_OK (0) or a nonzero CVM_ERR_* code; the
+ *     message of the last failure on the calling thread is available from
+ *     cvm_last_error().  Argument errors carry the reference's exact panic
+ *     text, so the Go shim can re-panic with the identical string.
+ *   - Host-buffer entry points copy their inputs to the device inside the
+ *     call and return after the results are back on the host; the caller
+ *     keeps ownership of every buffer and may reuse it after return (cgo's
+ *     pointer rules forbid retaining Go memory, and nothing is retained).
+ *   - RGBA images are interleaved 4 bytes per pixel; gray images 1 byte.
+ *     Strides are in bytes and may exceed width*bytes-per-pixel
+ *     (sub-images).
+ *   - All entry points are safe for concurrent use from several threads.
+ *     Handles serialise their own lazy geometry builds.
+ *   - The computation is the reference's op sequence: scores are
+ *     bit-identical to cvmatch's Go path on the same inputs.
+ */
+#ifndef CVMATCH_GPU_H
+#define CVMATCH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Match's six-tuple; the reference's Fleet Result (fleet.go:13-18). */
+typedef struct cvm_result {
+    float min_v;
+    int32_t min_x, min_y;
+    float max_v;
+    int32_t max_x, max_y;
+} cvm_result;
+
+typedef struct cvm_matcher cvm_matcher;
+typedef struct cvm_fleet cvm_fleet;
+
+enum {
+    CVM_OK = 0,
+    CVM_ERR_ARGS = 1,        /* "cvmatch: bad match arguments (...)"  impl.go:1127-1130, matcher.go:97-99, fleet.go:192-194 */
+    CVM_ERR_STATS_CAP = 2,   /* "cvmatch: template area ... exceeds the exact-statistics bound ..." impl.go:1131-1133, matcher.go:67-69 */
+    CVM_ERR_EMPTY_FLEET = 3, /* "cvmatch: empty fleet"  fleet.go:86-88 */
+    CVM_ERR_MIXED_FLEET = 4, /* "cvmatch: fleet mixes color and gray matchers"  fleet.go:93-97 */
+    CVM_ERR_NIL_IMAGE = 5,   /* "cvmatch: nil image"  cvmatch.go:170-173 */
+    CVM_ERR_EMPTY_IMAGE = 6, /* "cvmatch: empty image"  cvmatch.go:174-177 */
+    CVM_ERR_CUDA = 10,       /* a CUDA runtime call failed (message names it) */
+    CVM_ERR_UNSUPPORTED = 11,/* a transform size beyond this build's limits */
+    CVM_ERR_NO_DEVICE = 12   /* no sm_103 device / the library was not built for it */
+};
+
+/* Copies the calling thread's last error message (NUL-terminated,
+ * truncated to len) and returns its full length. */
+size_t cvm_last_error(char *buf, size_t len);
+
+/* ------------------------------------------------- one-shot entry points */
+
+/* Match (cvmatch.go:75-94): parent and sub are RGBA; the alpha channel is
+ * skipped exactly when both alpha planes are constant (cvmatch.go:82-85). */
+int cvm_match(const uint8_t *parent, int64_t pstride, int pw, int ph,
+              const uint8_t *sub, int64_t sstride, int sw, int sh, cvm_result *out);
+
+/* MatchMap (cvmatch.go:100-117): as cvm_match, and fills map with the
+ * (pw-sw+1) x (ph-sh+1) row-major float32 response. */
+int cvm_match_map(const uint8_t *parent, int64_t pstride, int pw, int ph,
+                  const uint8_t *sub, int64_t sstride, int sw, int sh, float *map);
+
+/* MatchGray (cvmatch.go:128-139) on 8-bit gray planes (the zero-copy
+ * *image.Gray / *image.YCbCr Y-plane case of toGray, cvmatch.go:205-208). */
+int cvm_match_gray(const uint8_t *parent, int64_t pstride, int pw, int ph,
+                   const uint8_t *sub, int64_t sstride, int sw, int sh, cvm_result *out);
+
+/* MatchGray on RGBA/NRGBA inputs: both images are converted on the device
+ * with rgbToGray's fixed-point weights (cvmatch.go:209-212, 222-240). */
+int cvm_match_gray_rgba(const uint8_t *parent, int64_t pstride, int pw, int ph,
+                        const uint8_t *sub, int64_t sstride, int sw, int sh, cvm_result *out);
+
+/* matchU8 (impl.go:1126-1155): the generic core every entry point funnels
+ * into.  cn channels of step-byte pixels; map may be NULL. */
+int cvm_match_u8(const uint8_t *img, int64_t istride, int iw, int ih,
+                 const uint8_t *tpl, int64_t tstride, int tw, int th, int cn, int step,
+                 float *map, cvm_result *out);
+
+/* Device-resident matchU8: img/tpl/map/out are device pointers, the work
+ * is queued on stream (a cudaStream_t, NULL = legacy default stream) and
+ * the call returns without synchronising. */
+int cvm_match_u8_device(const uint8_t *d_img, int64_t istride, int iw, int ih,
+                        const uint8_t *d_tpl, int64_t tstride, int tw, int th, int cn, int step,
+                        float *d_map, cvm_result *d_out, void *stream);
+
+/* Device-resident Match: colour semantics with the alpha decision made on
+ * the device (no host round trip). */
+int cvm_match_device(const uint8_t *d_parent, int64_t pstride, int pw, int ph,
+                     const uint8_t *d_sub, int64_t sstride, int sw, int sh,
+                     float *d_map, cvm_result *d_out, void *stream);
+
+/* ----------------------------------------------------- image primitives */
+
+/* rgbToGray (cvmatch.go:222-240): out is w*h packed gray bytes. */
+int cvm_rgba_to_gray(const uint8_t *pix, int64_t stride, int w, int h, uint8_t *out);
+
+/* alphaConst (cvmatch.go:146-168): *out = 1 when every alpha byte equals
+ * the first pixel's. */
+int cvm_alpha_const(const uint8_t *pix, int64_t stride, int w, int h, int *out);
+
+/* ------------------------------------------------------------- Matcher */
+
+/* newMatcher (matcher.go:45-76): step 4 = NewMatcher (RGBA, Match
+ * semantics), step 1 = NewGrayMatcher (gray plane, MatchGray semantics).
+ * The pixels are copied; the template statistics are computed here. */
+int cvm_matcher_new(const uint8_t *pix, int64_t stride, int w, int h, int step, cvm_matcher **out);
+
+/* Matcher.Find (matcher.go:83-130): bit-identical to Match / MatchGray. */
+int cvm_matcher_find(cvm_matcher *m, const uint8_t *parent, int64_t pstride, int pw, int ph,
+                     cvm_result *out);
+
+/* Device-resident Find: d_parent and d_out are device pointers; queued on
+ * stream without synchronising. */
+int cvm_matcher_find_device(cvm_matcher *m, const uint8_t *d_parent, int64_t pstride, int pw, int ph,
+                            cvm_result *d_out, void *stream);
+
+void cvm_matcher_free(cvm_matcher *m);
+
+/* --------------------------------------------------------------- Fleet */
+
+/* NewFleet (fleet.go:85-101): the member list is copied; the matchers must
+ * outlive the fleet.  All members share one mode. */
+int cvm_fleet_new(cvm_matcher *const *ms, int n, cvm_fleet **out);
+
+/* Fleet.FindAll (fleet.go:176-332): out receives n results in
+ * construction order. */
+int cvm_fleet_find_all(cvm_fleet *f, const uint8_t *parent, int64_t pstride, int pw, int ph,
+                       cvm_result *out);
+
+/* Device-resident FindAll: d_parent/d_out are device pointers (d_out holds
+ * n results); queued on stream without synchronising. */
+int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pstride, int pw, int ph,
+                              cvm_result *d_out, void *stream);
+
+void cvm_fleet_free(cvm_fleet *f);
+
+/* ------------------------------------------------------------- support */
+
+/* The tile geometry the library plans for a tw x th template over a
+ * rw x rh result (newGoPlan, impl.go:246-295, and the shrunk last band of
+ * shrinkDH, impl.go:573-582): out = {dftW, dftH, blockW, blockH, dh2,
+ * tiles}, dh2 = 0 when the last band keeps dftH.  Host-only; no device. */
+int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]);
+
+/* Page-locked host memory for frames the caller wants copied at full
+ * host-to-device bandwidth (plain pageable memory also works). */
+void *cvm_host_alloc(size_t bytes);
+void cvm_host_free(void *p);
+
+/* Number of this library's kernels launched since load (a counter the
+ * benchmark reads to report launches per step). */
+uint64_t cvm_launch_count(void);
+
+/* Per-kernel timing for profiling runs: while enabled, every kernel launch
+ * is bracketed by CUDA events recorded on its own stream (off by default;
+ * enabling clears earlier totals).  cvm_profile_read(i, ...) returns 0 and
+ * the i-th kernel's name, total milliseconds and launch count, or nonzero
+ * past the last kernel; it waits for the recorded events. */
+void cvm_profile_enable(int on);
+int cvm_profile_read(int i, char *name, size_t len, double *ms_total, uint64_t *launches);
+
+/* Library version string. */
+const char *cvm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

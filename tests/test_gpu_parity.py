@@ -1,0 +1,420 @@
+"""Parity of the CUDA path with the oracle, through the C ABI, on a GB300.
+
+The bar is bit identity: the CUDA kernels run the reference's per-element
+op sequence, so every score map and extremum must equal the oracle's (and
+therefore the reference's) bits.  Size-independent properties cover the
+full-size configurations; the reference's semantic tests (cvmatch_test.go,
+matcher_test.go, fleet_test.go) are mirrored on synthetic inputs.
+"""
+import json
+import os
+import sys
+import threading
+
+import numpy as np
+import pytest
+
+import cvmatch_gb300 as cvm
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+from synth import image  # noqa: E402
+
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def same_tuple(a, b):
+    return (np.float32(a[0]).view(np.uint32) == np.float32(b[0]).view(np.uint32) and a[1:3] == b[1:3]
+            and np.float32(a[3]).view(np.uint32) == np.float32(b[3]).view(np.uint32) and a[4:6] == b[4:6])
+
+
+def rgba(seed, h, w, alpha=255):
+    a = image(seed, h, w, 4).copy()
+    if alpha is not None:
+        a[..., 3] = alpha
+    return a
+
+
+# ------------------------------------------------------------ golden pins
+
+
+def test_case110_reference_hash_on_gpu():
+    img, tpl = make_golden.canary110()
+    t, res = cvm.match_u8(img, tpl, 1)
+    assert hex(oracle.fnv_golden_hash(res, t)) == GOLDEN["reference_pins"]["case110_fnv"]
+
+
+@pytest.mark.parametrize("idx", range(len(make_golden.SOLO_CASES)))
+def test_solo_fixture_bit_exact(idx):
+    c = make_golden.SOLO_CASES[idx]
+    img, tpl = make_golden.solo_inputs(c)
+    t, res = cvm.match_u8(img, tpl, c[5])
+    assert make_golden.digest(res, t) == GOLDEN["solo"][idx]["digest"], c[0]
+
+
+@pytest.mark.parametrize("idx", range(len(make_golden.SOLO_CASES)))
+def test_solo_matches_live_oracle(idx):
+    c = make_golden.SOLO_CASES[idx]
+    img, tpl = make_golden.solo_inputs(c)
+    t, res = cvm.match_u8(img, tpl, c[5])
+    to, ro = oracle.match_u8(img, tpl, c[5], threads=4)
+    assert np.array_equal(bits(res), bits(ro))
+    assert same_tuple(t, to)
+
+
+@pytest.mark.parametrize("idx", range(len(make_golden.FLEET_CASES)))
+def test_fleet_fixture_bit_exact(idx):
+    c = make_golden.FLEET_CASES[idx]
+    parent, tpls = make_golden.fleet_inputs(c)
+    ms = [cvm.NewMatcher(t) if c[3] == 4 else cvm.NewGrayMatcher(t) for t in tpls]
+    got = cvm.NewFleet(*ms).FindAll(parent)
+    want = GOLDEN["fleet"][idx]["results"]
+    for g, w in zip(got, want):
+        assert same_tuple(tuple(g), tuple(w)), (g, w)
+
+
+# ------------------------------------------------------ FP64 definition
+
+
+@pytest.mark.parametrize("shape", [
+    (97, 61, 17, 13, 1, 0, 0), (97, 61, 17, 13, 4, 0, 0), (64, 64, 64, 64, 1, 0, 0),
+    (50, 40, 1, 1, 4, 0, 0), (300, 200, 31, 29, 1, 7, 3), (40, 300, 33, 257, 1, 0, 0),
+    (128, 96, 5, 4, 3, 0, 0)])
+def test_against_fp64_definition(shape):
+    iw, ih, tw, th, cn, ipad, tpad = shape
+    img = image(42 + iw, ih, iw, cn, ipad)
+    tpl = image(43 + tw, th, tw, cn, tpad)
+    t, res = cvm.match_u8(img, tpl, cn)
+    ref = oracle.ref_match_f64(img, tpl, cn)
+    assert np.max(np.abs(res.astype(np.float64) - ref)) <= 1e-4
+    flat = res.ravel()
+    assert t[2] * res.shape[1] + t[1] == int(np.argmin(flat))
+    assert t[5] * res.shape[1] + t[4] == int(np.argmax(flat))
+
+
+# ------------------------------------------------ public API semantics
+
+
+def test_planted_template_match_and_gray():
+    parent = rgba(7, 400, 640)
+    sub = parent[77:77 + 48, 123:123 + 64].copy()
+    for fn in (cvm.Match, cvm.MatchGray):
+        _, _, _, v, x, y = fn(parent, sub)
+        assert (x, y) == (123, 77) and v >= 0.999
+
+
+def test_match_equals_oracle_cn3_bitwise():
+    parent = rgba(8, 300, 420)
+    sub = parent[40:72, 100:196].copy()
+    t = cvm.Match(parent, sub)
+    to, _ = oracle.match_u8(parent, sub, 3, want_map=False)
+    assert same_tuple(t, to)
+    m, w, h = cvm.MatchMap(parent, sub)
+    _, mo = oracle.match_u8(parent, sub, 3)
+    assert (w, h) == (420 - 96 + 1, 300 - 32 + 1) and np.array_equal(bits(m), bits(mo))
+
+
+def test_sub_image_input():
+    parent = rgba(9, 240, 320)
+    region = parent[60:140, 50:130]  # a view with the parent's stride
+    _, _, _, v, x, y = cvm.Match(parent, region)
+    assert (x, y) == (50, 60) and v >= 0.999
+
+
+def test_gray_plane_input():
+    y = image(11, 150, 200, 1).copy()
+    sub = y[20:50, 60:100].copy()
+    _, _, _, v, x, yy = cvm.MatchGray(y, sub)
+    assert (x, yy) == (60, 20) and v >= 0.999
+
+
+def test_flat_template():
+    parent = np.zeros((100, 100, 4), np.uint8)
+    sub = np.zeros((10, 10, 4), np.uint8)
+    assert cvm.Match(parent, sub) == (1.0, 0, 0, 1.0, 0, 0)
+    m, w, h = cvm.MatchMap(rgba(3, 100, 100), sub)
+    assert np.all(m == 1.0)
+
+
+def test_bad_input_raises():
+    with pytest.raises(cvm.CvmatchError, match="bad match arguments"):
+        cvm.Match(np.zeros((10, 10, 4), np.uint8), np.zeros((20, 20, 4), np.uint8))
+
+
+def test_constant_alpha_skip_and_varying_alpha():
+    iw, ih, tw, th = 120, 90, 24, 18
+    img = rgba(21, ih, iw, None)
+    tpl = rgba(22, th, tw, None)
+    for a_img, a_tpl in ((200, 55), (0, 255), (128, 128)):
+        img[..., 3] = a_img
+        tpl[..., 3] = a_tpl
+        m, _, _ = cvm.MatchMap(img, tpl)
+        _, m3 = oracle.match_u8(img, tpl, 3)
+        assert np.array_equal(bits(m), bits(m3))
+    img = rgba(23, 80, 100, None)  # varying alpha: full 4 channels
+    sub = img[30:46, 40:60].copy()
+    m, _, _ = cvm.MatchMap(img, sub)
+    _, m4 = oracle.match_u8(img, sub, 4)
+    assert np.array_equal(bits(m), bits(m4))
+    ref = oracle.ref_match_f64(img, sub, 4)
+    assert np.max(np.abs(m - ref)) <= 1e-4
+    _, _, _, v, x, y = cvm.Match(img, sub)
+    assert (x, y) == (40, 30) and v >= 0.999
+
+
+def test_alpha_mixed_constancy():
+    parent = rgba(92, 90, 120, None)  # varying alpha
+    sub = parent[40:58, 60:84].copy()
+    sub[..., 3] = 128  # constant template alpha: still the 4-channel path
+    m, _, _ = cvm.MatchMap(parent, sub)
+    _, m4 = oracle.match_u8(parent, sub, 4)
+    assert np.array_equal(bits(m), bits(m4))
+
+
+def test_find_all_occurrences_via_map():
+    rng = np.random.default_rng(101)
+    parent = np.empty((300, 400, 4), np.uint8)
+    parent[..., :3] = rng.integers(0, 64, (300, 400, 3))
+    parent[..., 3] = 255
+    tpl = rgba(102, 24, 32)
+    spots = [(10, 12), (200, 40), (350, 260), (60, 240), (180, 150)]
+    for x, y in spots:
+        parent[y:y + 24, x:x + 32] = tpl
+    resp, w, h = cvm.MatchMap(parent, tpl)
+    hits = []
+    for y in range(h):
+        for x in np.nonzero(resp[y] >= 0.999)[0]:
+            nb = resp[max(0, y - 12):y + 13, max(0, x - 16):x + 17]
+            if not np.any(nb > resp[y, x]):
+                hits.append((int(x), y))
+    assert sorted(hits) == sorted(spots)
+
+
+def test_gray_conversion_and_alpha_scan():
+    for w, h, pad in ((1, 1, 0), (7, 3, 0), (33, 5, 2), (641, 2, 3)):
+        pix = image(8 + w, h, w, 4, pad)
+        got = cvm.rgba_to_gray(pix)
+        p = pix.astype(np.uint32)
+        want = ((4899 * p[..., 0] + 9617 * p[..., 1] + 1868 * p[..., 2] + 8192) >> 14).astype(np.uint8)
+        assert np.array_equal(got, want)
+    a = rgba(5, 50, 70)
+    assert cvm.alpha_const(a)
+    a[49, 69, 3] = 3
+    assert not cvm.alpha_const(a)
+
+
+# -------------------------------------------------------------- Matcher
+
+
+def test_matcher_find_equals_match():
+    parent = rgba(31, 240, 320)
+    sub = parent[80:104, 100:132].copy()
+    want = cvm.Match(parent, sub)
+    m = cvm.NewMatcher(sub)
+    for _ in range(3):
+        assert same_tuple(m.Find(parent), want)
+    g = cvm.NewGrayMatcher(sub)
+    wantg = cvm.MatchGray(parent, sub)
+    for _ in range(3):
+        assert same_tuple(g.Find(parent), wantg)
+
+
+def test_matcher_geometry_change():
+    full = rgba(33, 400, 560)
+    sub = full[100:196, 200:296].copy()
+    crop = full[:400 - 24, :560 - 40]
+    m = cvm.NewMatcher(sub)
+    for _ in range(2):
+        for parent in (full, crop):
+            assert same_tuple(m.Find(parent), cvm.Match(parent, sub))
+
+
+def test_matcher_concurrent():
+    parent = rgba(35, 300, 400, None)
+    sub = parent[10:50, 20:70].copy()
+    want = cvm.Match(parent, sub)
+    m = cvm.NewMatcher(sub)
+    out = [None] * 8
+
+    def work(i):
+        out[i] = m.Find(parent)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(8)]
+    [t.start() for t in ts]
+    [t.join() for t in ts]
+    assert all(same_tuple(o, want) for o in out)
+
+
+def test_concurrent_match_calls():
+    parent = rgba(31, 240, 320)
+    sub = parent[80:104, 100:132].copy()
+    want, wantg = cvm.Match(parent, sub), cvm.MatchGray(parent, sub)
+    errs = []
+
+    def work():
+        for _ in range(5):
+            if not same_tuple(cvm.Match(parent, sub), want) or not same_tuple(cvm.MatchGray(parent, sub), wantg):
+                errs.append(1)
+
+    ts = [threading.Thread(target=work) for _ in range(8)]
+    [t.start() for t in ts]
+    [t.join() for t in ts]
+    assert not errs
+
+
+# ---------------------------------------------------------------- Fleet
+
+
+def desk(seed=41):
+    rng = np.random.default_rng(seed)
+    img = np.empty((700, 1000, 4), np.uint8)
+    img[..., :3] = rng.integers(0, 256, (700, 1000, 3))
+    img[..., 3] = 255
+    for _ in range(30):
+        w, h = rng.integers(20, 300, 2)
+        x, y = rng.integers(0, 1000 - w), rng.integers(0, 700 - h)
+        img[y:y + h, x:x + w, :3] = rng.integers(0, 256, 3)
+    return img
+
+
+def crops(img, seed=11, n=12):
+    rng = np.random.default_rng(seed)
+    sizes = [(24, 24), (96, 32), (48, 48), (300, 200), (16, 16), (64, 128)]
+    out, at = [], []
+    for i in range(n):
+        w, h = sizes[i % len(sizes)]
+        x, y = int(rng.integers(0, img.shape[1] - w)), int(rng.integers(0, img.shape[0] - h))
+        out.append(img[y:y + h, x:x + w].copy())
+        at.append((x, y))
+    return out, at
+
+
+@pytest.mark.parametrize("gray", [False, True])
+def test_fleet_bit_exact_vs_oracle(gray):
+    img = desk()
+    subs, at = crops(img)
+    ms = [cvm.NewGrayMatcher(s) if gray else cvm.NewMatcher(s) for s in subs]
+    got = cvm.NewFleet(*ms).FindAll(img)
+    if gray:
+        gimg = oracle.rgba_to_gray(img)
+        want = oracle.fleet_find_all([oracle.rgba_to_gray(s) for s in subs], gimg, threads=8)
+    else:
+        want = oracle.fleet_find_all(subs, img, threads=8)
+    for g, w in zip(got, want):
+        assert same_tuple(tuple(g), w)
+    hits = sum((g.MaxX, g.MaxY) == a for g, a in zip(got, at))
+    assert hits >= len(got) * 2 // 3
+
+
+def test_fleet_single_member_equals_find():
+    img = desk(43)
+    sub = img[100:132, 200:296].copy()
+    m = cvm.NewMatcher(sub)
+    (r,) = cvm.NewFleet(m).FindAll(img)
+    assert same_tuple(tuple(r), m.Find(img))
+
+
+def test_fleet_flat_members_and_all_flat():
+    img = desk(45)
+    subs, _ = crops(img, n=3)
+    flat = np.zeros((300, 400, 4), np.uint8)
+    flat[..., :3] = 30
+    flat[..., 3] = 255
+    ms = [cvm.NewMatcher(flat), cvm.NewMatcher(subs[0]), cvm.NewMatcher(subs[1])]
+    got = cvm.NewFleet(*ms).FindAll(img)
+    assert tuple(got[0]) == (1.0, 0, 0, 1.0, 0, 0)
+    for i in (1, 2):
+        assert (got[i].MaxX, got[i].MaxY) == ms[i].Find(img)[4:6]
+    assert tuple(cvm.NewFleet(cvm.NewMatcher(flat)).FindAll(img)[0]) == (1.0, 0, 0, 1.0, 0, 0)
+
+
+def test_fleet_mixed_alpha_and_orthogonal():
+    img = desk(47)
+    subs, at = crops(img, n=3)
+    va = subs[0].copy()
+    va.reshape(-1, 4)[::4, 3] = np.arange(va.reshape(-1, 4)[::4].shape[0]) % 256
+    wide = img[40:48, 52:352].copy()
+    tall = img[150:450, 700:708].copy()
+    tpls = [va, subs[1], subs[2], wide, tall]
+    got = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls]).FindAll(img)
+    want = oracle.fleet_find_all(tpls, img, threads=8)
+    for g, w in zip(got, want):
+        assert same_tuple(tuple(g), w)
+
+
+def test_fleet_determinism_order_repeat_isolation():
+    img = desk(49)
+    subs, _ = crops(img)
+    ms = [cvm.NewGrayMatcher(s) for s in subs]
+    base = cvm.NewFleet(*ms).FindAll(img)
+    rev = cvm.NewFleet(*ms[::-1]).FindAll(img)
+    assert [tuple(r) for r in rev[::-1]] == [tuple(b) for b in base]
+    fl = cvm.NewFleet(ms)
+    assert fl.FindAll(img) == fl.FindAll(img) == base
+    lst = [ms[0], ms[1]]
+    f2 = cvm.NewFleet(lst)
+    want = f2.FindAll(img)
+    lst[0] = ms[3]
+    assert f2.FindAll(img) == want
+
+
+def test_fleet_concurrent():
+    img = desk(51)
+    subs, _ = crops(img, n=6)
+    fl = cvm.NewFleet(*[cvm.NewMatcher(s) for s in subs])
+    out = [None] * 4
+
+    def work(i):
+        out[i] = fl.FindAll(img)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(4)]
+    [t.start() for t in ts]
+    [t.join() for t in ts]
+    assert all(o == out[0] for o in out)
+
+
+def test_fleet_mixed_modes_rejected():
+    a = rgba(1, 20, 20)
+    with pytest.raises(cvm.CvmatchError, match="fleet mixes color and gray matchers"):
+        cvm.NewFleet(cvm.NewMatcher(a), cvm.NewGrayMatcher(a))
+
+
+# ------------------------------------------------- benchmark-sized configs
+
+
+def test_config_c1_gray_bit_exact():
+    import bench
+    frame, tpl, (x, y) = bench.scene_c1()
+    t = cvm.MatchGray(frame, tpl)
+    g, gt = oracle.rgba_to_gray(frame), oracle.rgba_to_gray(tpl)
+    to, _ = oracle.match_u8(g, gt, 1, threads=8, want_map=False)
+    assert same_tuple(t, to) and (t[4], t[5]) == (x, y)
+
+
+def test_config_c2_match_bit_exact():
+    import bench
+    frame, tpl, (x, y) = bench.scene_c2()
+    m, w, h = cvm.MatchMap(frame, tpl)
+    to, mo = oracle.match_u8(frame, tpl, 3, threads=16)
+    assert np.array_equal(bits(m), bits(mo))
+    t = cvm.Match(frame, tpl)
+    assert same_tuple(t, to)
+    assert (t[4], t[5]) == (x, y)
+
+
+def test_config_c3_map_bit_exact():
+    import bench
+    g, tpl, (x, y) = bench.scene_c3()
+    t, m = cvm.match_u8(g, tpl, 1)
+    to, mo = oracle.match_u8(g, tpl, 1, threads=16)
+    assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
+    assert (t[4], t[5]) == (x, y)
+    assert np.all(np.abs(m) <= 1.0)
