@@ -173,9 +173,6 @@ struct Geom {
     TileGeom g;
     int nclass = 1;
     FftClass fc[2];
-    int ctas[2] = {0, 0}, pairs[2] = {0, 0};
-    int partOff[2] = {0, 0};
-    int nparts = 0;
 };
 
 int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G) {
@@ -220,12 +217,6 @@ int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G) {
             f.tileFirst = ntiles - g.ntx;
             f.ntiles = g.ntx;
         }
-        G.ctas[c] = inv_rows_ctas_per_tile(f, &G.pairs[c]);
-    }
-    G.nparts = 0;
-    for (int c = 0; c < G.nclass; c++) {
-        G.partOff[c] = G.nparts;
-        G.nparts += G.fc[c].ntiles * G.ctas[c];
     }
     return CVM_OK;
 }
@@ -260,27 +251,6 @@ int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step
     return CVM_OK;
 }
 
-SatPlanes sat_layout(int iw, int ih, int cnS) {
-    SatPlanes S;
-    S.iw = iw;
-    S.ih = ih;
-    S.nsum = cnS;
-    S.pitch = (long long)align_up((size_t)iw + 1, 32);
-    return S;
-}
-
-size_t sat_bytes(const SatPlanes &S) {
-    const size_t plane = (size_t)S.pitch * (S.ih + 1);
-    return S.nsum * Arena::bytes(plane, 4) + (S.nsum == 4 ? 2 : 1) * Arena::bytes(plane, 8);
-}
-
-void sat_carve(SatPlanes &S, Arena &A) {
-    const size_t plane = (size_t)S.pitch * (S.ih + 1);
-    for (int k = 0; k < S.nsum; k++) S.sum[k] = A.take<unsigned int>(plane);
-    S.sq = A.take<unsigned long long>(plane);
-    S.sqA = S.nsum == 4 ? A.take<unsigned long long>(plane) : nullptr;
-}
-
 // ---------------------------------------------------------- solo pipeline
 
 struct TemplateCache;  // a Matcher's per-geometry state
@@ -310,9 +280,11 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         G = &local;
     }
     const int cnS = J.mode == 1 ? 4 : J.cnFixed;
-    SatPlanes S = sat_layout(J.iw, J.ih, cnS);
+    const NormGrid ng = norm_grid(rw, rh, J.tw, cnS);
+    const int nparts = ng.ncx * ng.nby;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
-                   Arena::bytes(G->nparts, sizeof(Partial)) + sat_bytes(S);
+                   Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(ng.scratchPerCta * nparts, 1);
+    if (!J.map) bytes += Arena::bytes((size_t)rw * rh, sizeof(float));
     for (int c = 0; c < G->nclass; c++) {
         bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
         if (!J.cachedP) bytes += Arena::bytes(tspec_elems(G->fc[c], cnS), sizeof(float2));
@@ -323,8 +295,9 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     A.base = static_cast<char *>(buf.p);
     DevParams *P = A.take<DevParams>(1);
     DevFrame *F = A.take<DevFrame>(1);
-    Partial *parts = A.take<Partial>(G->nparts);
-    sat_carve(S, A);
+    Partial *parts = A.take<Partial>(nparts);
+    unsigned char *normScratch = A.take<unsigned char>(ng.scratchPerCta * nparts);
+    float *corr = J.map ? J.map : A.take<float>((size_t)rw * rh);
     float2 *spec[2] = {nullptr, nullptr};
     const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
     float2 *tsOwn[2] = {nullptr, nullptr};
@@ -336,20 +309,13 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         }
     }
     CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
-    if (J.cachedP) {
+    if (J.cachedP)
         CVM_CUDA(cudaMemcpyAsync(P, J.cachedP, sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
-    } else {
-        DevParams init;
-        memset(&init, 0, sizeof init);
-        init.mode = J.mode;
-        init.cnFixed = J.cnFixed;
-        init.tw = J.tw;
-        init.th = J.th;
-        CVM_CUDA(upload_bytes(P, &init, sizeof init, st));
-        CVM_CUDA(launch_tpl_stats(J.tpl, J.tstride, J.tw, J.th, J.step, cnS, P, st));
-    }
-    CVM_CUDA(launch_sat(J.img, J.istride, J.step, S, J.mode == 1 ? &F->alphaMismatch : nullptr, st));
-    CVM_CUDA(launch_params_finalize(P, 1, F, st));
+    else
+        CVM_CUDA(cudaMemsetAsync(P, 0, sizeof(DevParams), st));
+    CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
+                         J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
+                         J.cnFixed, F, st));
     if (!J.cachedP)
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], st));
     MemberSet ms;
@@ -365,16 +331,18 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.solo.outIdx = 0;
     ms.params = P;
     ms.map = J.map;
+    ms.corr = corr;
+    ms.corrStride = 0;
     for (int c = 0; c < G->nclass; c++) {
         const FftClass &f = G->fc[c];
         CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, f, spec[c], cnS, st));
         ms.scratch[c] = spec[c];
         ms.scratchStride[c] = 0;
         CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
-        CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, S, parts, G->partOff[c], G->ctas[c],
-                                 G->pairs[c], st));
+        CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, st));
     }
-    CVM_CUDA(launch_extrema_final(ms, 1, parts, G->nparts, J.out, st));
+    CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, parts, normScratch, st));
+    CVM_CUDA(launch_extrema_final(ms, 1, parts, nparts, J.out, st));
     return CVM_OK;
 }
 
@@ -586,6 +554,8 @@ int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, 
 
 struct FleetBucketGeom {
     Geom G;
+    NormGrid ng;
+    int rwMax = 0, rhMax = 0;
     int cnS = 1;
     std::vector<float2 *> ts;     // per member: class 0, class 1 (owned)
     DevMember *table = nullptr;   // bucket members in bucket order
@@ -640,6 +610,12 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         bg->cnS = f->step;
         bg->members = b.members;
         const Geom &G = bg->G;
+        for (int mi : b.members) {
+            bg->rwMax = std::max(bg->rwMax, pw - f->ms[mi]->w + 1);
+            bg->rhMax = std::max(bg->rhMax, ph - f->ms[mi]->h + 1);
+        }
+        bg->ng = norm_grid(bg->rwMax, bg->rhMax, b.tw, bg->cnS);
+        const int nparts = bg->ng.ncx * bg->ng.nby;
         std::vector<DevMember> tab(b.members.size());
         for (size_t pos = 0; pos < b.members.size(); pos++) {
             cvm_matcher *m = f->ms[b.members[pos]];
@@ -659,7 +635,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
             d.th = m->h;
             d.rw = pw - m->w + 1;
             d.rh = ph - m->h + 1;
-            d.partBase = (int)pos * G.nparts;
+            d.partBase = (int)pos * nparts;
             d.outIdx = b.members[pos];
         }
         CVM_CUDA(cudaMalloc(&bg->table, tab.size() * sizeof(DevMember)));
@@ -689,7 +665,6 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     std::shared_ptr<FleetGeom> fg;
     CVM_TRY(fleet_geom(f, pw, ph, fg));
     const int cnS = f->step;
-    SatPlanes S = sat_layout(pw, ph, cnS);
     size_t frameBytes = 0, partBytes = 0, waveBytes = 0;
     std::vector<int> wave(fg->bg.size());
     for (size_t b = 0; b < fg->bg.size(); b++) {
@@ -699,24 +674,27 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             fb += Arena::bytes(spec_elems(bg.G.fc[c], cnS), sizeof(float2));
             per += bg.memberScratch[c] * sizeof(float2);
         }
+        const size_t corrPer = (size_t)bg.rwMax * bg.rhMax;
+        const int nparts = bg.ng.ncx * bg.ng.nby;
+        per += corrPer * sizeof(float) + bg.ng.scratchPerCta * nparts;
         frameBytes = std::max(frameBytes, fb);
-        partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * bg.G.nparts, sizeof(Partial)));
+        partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
         w = std::min<int>(w, (int)bg.members.size());
         wave[b] = w;
-        size_t wb = 0;
+        size_t wb = Arena::bytes((size_t)w * corrPer, sizeof(float)) +
+                    Arena::bytes((size_t)w * bg.ng.scratchPerCta * nparts, 1);
         for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));
         waveBytes = std::max(waveBytes, wb);
     }
-    const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) + sat_bytes(S) +
-                         frameBytes + partBytes + waveBytes;
+    const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) + frameBytes +
+                         partBytes + waveBytes;
     PoolBuf buf;
     CVM_TRY(pool_alloc(buf, bytes, st));
     Arena A;
     A.base = static_cast<char *>(buf.p);
     DevParams *P = A.take<DevParams>(n);
     DevFrame *F = A.take<DevFrame>(1);
-    sat_carve(S, A);
     char *frameBase = A.base + A.used;
     A.used += frameBytes;
     Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
@@ -724,13 +702,16 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     char *waveBase = A.base + A.used;
     CVM_CUDA(cudaMemcpyAsync(P, f->dP, n * sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
     CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
-    CVM_CUDA(launch_sat(dParent, pstride, f->step, S, f->step == 4 ? &F->alphaMismatch : nullptr, st));
-    CVM_CUDA(launch_params_finalize(P, n, F, st));
+    CVM_CUDA(launch_prep(nullptr, 0, 0, 0, f->step, 0, f->step == 4 ? dParent : nullptr, pstride, pw, ph, P, n, 0, 0,
+                         0, F, st));
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
+        const int nparts = bg.ng.ncx * bg.ng.nby;
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
+        float *corr = nullptr;
+        unsigned char *normScratch = nullptr;
         {
             Arena fa;
             fa.base = frameBase;
@@ -740,6 +721,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 frame[c] = fa.take<float2>(spec_elems(G.fc[c], cnS));
                 scratch[c] = wa.take<float2>((size_t)wave[b] * bg.memberScratch[c]);
             }
+            corr = wa.take<float>((size_t)wave[b] * bg.rwMax * bg.rhMax);
+            normScratch = wa.take<unsigned char>((size_t)wave[b] * bg.ng.scratchPerCta * nparts);
         }
         // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
         for (int c = 0; c < G.nclass; c++) {
@@ -753,6 +736,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         memset(&ms, 0, sizeof ms);
         ms.table = bg.table;
         ms.params = P;
+        ms.corr = corr;
+        ms.corrStride = (size_t)bg.rwMax * bg.rhMax;
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -763,12 +748,12 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             ms.first = w0;
             for (int c = 0; c < G.nclass; c++) {
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
-                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, S, parts, G.partOff[c], G.ctas[c],
-                                         G.pairs[c], st));
+                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, st));
             }
+            CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, parts, normScratch, st));
         }
         ms.first = 0;
-        CVM_CUDA(launch_extrema_final(ms, nm, parts, G.nparts, dOut, st));
+        CVM_CUDA(launch_extrema_final(ms, nm, parts, nparts, dOut, st));
     }
     return CVM_OK;
 }
@@ -952,15 +937,16 @@ int cvm_matcher_new(const uint8_t *pix, int64_t stride, int w, int h, int step, 
     CVM_CUDA(cudaMalloc(&m->dPix, (size_t)w * h * step));
     CVM_CUDA(cudaMemcpy2DAsync(m->dPix, (size_t)w * step, pix, (size_t)stride, (size_t)w * step, h,
                                cudaMemcpyHostToDevice, st));
+    // Raw template sums (and the template's alpha flag) through the same
+    // statistics kernel one-shot calls use; a scratch frame record serves
+    // the kernel's finalisation, which Find repeats per frame.
     CVM_CUDA(cudaMalloc(&m->dP, sizeof(DevParams)));
-    DevParams init;
-    memset(&init, 0, sizeof init);
-    init.mode = step == 4 ? 1 : 0;
-    init.cnFixed = step == 4 ? 4 : 1;
-    init.tw = w;
-    init.th = h;
-    CVM_CUDA(upload_bytes(m->dP, &init, sizeof init, st));
-    CVM_CUDA(launch_tpl_stats(m->dPix, (long long)w * step, w, h, step, step, m->dP, st));
+    PoolBuf fb;
+    CVM_TRY(pool_alloc(fb, sizeof(DevFrame), st));
+    CVM_CUDA(cudaMemsetAsync(m->dP, 0, sizeof(DevParams), st));
+    CVM_CUDA(cudaMemsetAsync(fb.p, 0, sizeof(DevFrame), st));
+    CVM_CUDA(launch_prep(m->dPix, (long long)w * step, w, h, step, step, nullptr, 0, 0, 0, m->dP, 1, 1,
+                         step == 4 ? 1 : 0, step == 4 ? 4 : 1, static_cast<DevFrame *>(fb.p), st));
     CVM_CUDA(cudaStreamSynchronize(st));
     *out = m.release();
     return CVM_OK;

@@ -71,16 +71,8 @@ struct DevParams {
 struct DevFrame {
     unsigned int alphaMismatch;  // parent alpha plane not constant
     int cnMax;                   // largest effective cn among the members
-    int pad[2];
-};
-
-struct SatPlanes {
-    unsigned int *sum[4] = {nullptr, nullptr, nullptr, nullptr};
-    unsigned long long *sq = nullptr;   // sum over the first min(cnS,3) channels (all when cnS<4)
-    unsigned long long *sqA = nullptr;  // channel-3 squares when cnS == 4
-    long long pitch = 0;                // elements per plane row
-    int nsum = 0;                       // number of sum planes (cnS)
-    int iw = 0, ih = 0;
+    int done;                    // CTAs of k_prep finished (last one finalises)
+    int pad;
 };
 
 // One correlation target of the tail kernels: a solo match or one fleet
@@ -107,6 +99,8 @@ struct MemberSet {
     float2 *scratch[2];        // column-pass output, per wave slot
     size_t scratchStride[2];   // elements between wave slots
     float *map;                // optional score map (solo only)
+    float *corr;               // raw correlation, per wave slot (pitch rw)
+    size_t corrStride;         // elements between wave slots
 };
 
 struct Partial {
@@ -121,11 +115,12 @@ cudaError_t launch_gray(const uint8_t *src, long long sstride, int w, int h, uin
                         long long dstride, cudaStream_t st);
 cudaError_t launch_alpha_scan(const uint8_t *img, long long stride, int w, int h,
                               unsigned int *mismatch, cudaStream_t st);
-cudaError_t launch_tpl_stats(const uint8_t *tpl, long long tstride, int tw, int th, int step,
-                             int cnStats, DevParams *P, cudaStream_t st);
-cudaError_t launch_params_finalize(DevParams *P, int n, DevFrame *F, cudaStream_t st);
-cudaError_t launch_sat(const uint8_t *img, long long istride, int step, const SatPlanes &S,
-                       unsigned int *alphaMismatch, cudaStream_t st);
+// Template statistics (when tpl is set), parent alpha scan (when parent is
+// set) and the finalisation of n params, in one launch.  P (n entries) and
+// F must be zeroed, or hold cached template sums, before the launch.
+cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, int tstep, int cnStats,
+                        const uint8_t *parent, long long pstride, int pw, int ph, DevParams *P, int n,
+                        int setInit, int initMode, int initCnFixed, DevFrame *F, cudaStream_t st);
 // Forward row pass of every tile of `fc` (or of a template: geometry with
 // one 1x1 block whose loads are the template's tw x th).
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
@@ -139,12 +134,19 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
 cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
                         const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
                         const MemberSet &ms, int nmembers, cudaStream_t st);
-// Inverse rows + channel accumulation + normalization + partial extrema.
-cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS,
-                            const MemberSet &ms, int nmembers, const SatPlanes &S,
-                            Partial *partials, int partOffset, int ctasPerTile, int pairsPerCta,
-                            cudaStream_t st);
-int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta);
+// Inverse rows + channel accumulation into each member's raw correlation.
+cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
+                            int nmembers, cudaStream_t st);
+// Normalisation + first-occurrence extrema partials: CW x B results per
+// CTA; `ncx` x `nby` CTAs per member.
+struct NormGrid {
+    int CW, B, ncx, nby, ncCap, cnCap;
+    size_t smemBytes;       // dynamic shared memory per CTA (0 with global scratch)
+    size_t scratchPerCta;   // global scratch per CTA when the arrays exceed shared memory
+};
+NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap);
+cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
+                        const NormGrid &ng, Partial *partials, unsigned char *gscratch, cudaStream_t st);
 cudaError_t launch_extrema_final(const MemberSet &ms, int nmembers, const Partial *partials,
                                  int nparts, cvm_result *out, cudaStream_t st);
 // Stores small host values into device memory through kernel arguments

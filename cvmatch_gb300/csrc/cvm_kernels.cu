@@ -11,19 +11,18 @@
 // intermediate rows) is free; the per-element op sequence is not.  The
 // result is the reference's output bit for bit.
 //
-// Kernels (bytes that bound each are per launch; see the design notes):
+// Kernels:
 //   k_gray            rgbToGray (cvmatch.go:222-240)
 //   k_alpha_scan      alphaConst (cvmatch.go:146-168)
-//   k_tpl_stats       templStats (impl.go:1063-1079), exact u64 atomics
-//   k_params_finalize cn choice (cvmatch.go:82-85, matcher.go:103-112) and the
-//                     templNorm / numScale / varScale constants (impl.go:867-873, 1087)
-//   k_sat_rows/cols   exact summed-area tables replacing colBuildGo/colSlideGo
-//                     (impl.go:708-805)
+//   k_prep            templStats (impl.go:1063-1079) + the parent's alpha scan +
+//                     the cn choice (cvmatch.go:82-85, matcher.go:103-112) and
+//                     tail constants (impl.go:867-873, 1087), one launch
 //   k_fwd_rows        forwardRowPair (impl.go:301-344) for every tile row pair
 //   k_cols            colsR4Go forward / mulConjGo / colsR4Go inverse
 //                     (radix4cols.go:111-125, impl.go:376-388)
 //   k_inv_rows        inverseRowPair (impl.go:394-444) + channel accumulation
-//                     + normOne (impl.go:825-849) + first-occurrence extrema
+//   k_norm            sliding column sums (colBuildGo/colSlideGo, impl.go:708-805),
+//                     normOne (impl.go:825-849), first-occurrence extrema
 //   k_extrema_final   band merge (impl.go:1104-1112) over CTA partials
 //   k_shrink_gather   shrinkInto (impl.go:591-610)
 #include <cfloat>
@@ -278,59 +277,20 @@ __global__ void k_alpha_scan(const uint8_t *__restrict__ img, long long stride, 
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(mismatch, 1u);
 }
 
-// ------------------------------------------------------------ statistics
+// ----------------------------------------------------- statistics + cn
 
-// Exact per-channel template sums and squared sums (templStats,
-// impl.go:1063-1079) plus the template's alpha-constancy flag.
-__global__ void k_tpl_stats(const uint8_t *__restrict__ tpl, long long tstride, int tw, int th,
-                            int step, int cnStats, DevParams *P) {
-    unsigned long long s[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
-    bool bad = false;
-    const uint8_t a0 = step == 4 ? tpl[3] : 0;
-    const long long total = (long long)tw * th;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int y = (int)(i / tw), x = (int)(i - (long long)y * tw);
-        const uint8_t *p = tpl + (long long)y * tstride + (long long)x * step;
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (k < cnStats) {
-                const unsigned v = p[k];
-                s[k] += v;
-                q[k] += v * v;
-            }
-        if (step == 4) bad |= p[3] != a0;
-    }
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
-            q[k] += __shfl_down_sync(0xffffffffu, q[k], o);
-        }
-    const bool anyBad = __any_sync(0xffffffffu, bad);
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < cnStats; k++) {
-            if (s[k]) atomicAdd(&P->tsum[k], s[k]);
-            if (q[k]) atomicAdd(&P->tsq[k], q[k]);
-        }
-        if (anyBad) atomicOr(&P->alphaMismatch, 1u);
-    }
-}
-
-// Chooses the effective channel count and derives the tail constants with
-// the reference's double-precision sequences (impl.go:867-873, 1087).
-__global__ void k_params_finalize(DevParams *P, int n, DevFrame *F) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    DevParams &p = P[i];
+// Derives the effective channel count and the tail constants of one
+// template with the reference's double-precision sequences
+// (impl.go:867-873, 1087; the cn choice of cvmatch.go:82-85 and
+// matcher.go:103-112).  Runs once per call, in the last CTA of k_prep.
+__device__ void finalize_params(DevParams &p, const DevFrame &F, int *cnMax) {
     int cn = p.cnFixed;
-    if (p.mode == 1) cn = (p.alphaMismatch == 0 && F->alphaMismatch == 0) ? 3 : 4;
+    if (p.mode == 1) cn = (p.alphaMismatch == 0 && F.alphaMismatch == 0) ? 3 : 4;
     const long long area = (long long)p.tw * p.th;
     long long vs = 0;
     for (int k = 0; k < cn; k++) {
-        const long long s = (long long)p.tsum[k];
-        vs += area * (long long)p.tsq[k] - s * s;
+        const long long sk = (long long)p.tsum[k];
+        vs += area * (long long)p.tsq[k] - sk * sk;
     }
     p.cn = cn;
     p.varSum = vs;
@@ -338,117 +298,104 @@ __global__ void k_params_finalize(DevParams *P, int n, DevFrame *F) {
     const double ad = __dmul_rn((double)p.tw, (double)p.th);
     p.templNorm = __double2float_rn(__dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad)));
     p.varScale = __double2float_rn(__ddiv_rn(1.0, ad));
-    p.numScale = cn == 1 ? __double2float_rn(__ddiv_rn(__ll2double_rn((long long)p.tsum[0]), ad))
-                         : p.varScale;
-    if (!p.flat) atomicMax(&F->cnMax, cn);
+    p.numScale = cn == 1 ? __double2float_rn(__ddiv_rn(__ll2double_rn((long long)p.tsum[0]), ad)) : p.varScale;
+    if (!p.flat) atomicMax(cnMax, cn);
 }
 
-// ----------------------------------------------------------------- SAT
-
-template <typename T>
-__device__ __forceinline__ T warp_incl_scan(T v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const T u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
-    }
-    return v;
-}
-
-// Row prefix sums: one warp per image row, 32 pixels per step with a
-// carried total.  Writes plane row y+1 (column 0 and plane row 0 are 0).
-// Also flags a non-constant alpha plane (alphaConst).
-__global__ void k_sat_rows(const uint8_t *__restrict__ img, long long istride, int step,
-                           SatPlanes S, unsigned int *alphaMismatch) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = blockIdx.x * (blockDim.x >> 5) + warp;
-    const long long P = S.pitch;
-    if (blockIdx.x == 0 && warp == 0) {
-        for (int x = lane; x <= S.iw; x += 32) {
-            for (int k = 0; k < S.nsum; k++) S.sum[k][x] = 0u;
-            S.sq[x] = 0ull;
-            if (S.sqA) S.sqA[x] = 0ull;
-        }
-    }
-    if (y >= S.ih) return;
-    const uint8_t *row = img + (long long)y * istride;
-    const long long o = (long long)(y + 1) * P;
-    if (lane == 0) {
-        for (int k = 0; k < S.nsum; k++) S.sum[k][o] = 0u;
-        S.sq[o] = 0ull;
-        if (S.sqA) S.sqA[o] = 0ull;
-    }
-    const uint8_t a0 = img[3];
-    const int nsq = S.nsum < 4 ? S.nsum : 3;
-    unsigned int carry[4] = {0u, 0u, 0u, 0u};
-    unsigned long long carrySq = 0ull, carryA = 0ull;
-    bool bad = false;
-    for (int xb = 0; xb < S.iw; xb += 32) {
-        const int x = xb + lane;
-        unsigned int v[4] = {0u, 0u, 0u, 0u};
-        if (x < S.iw) {
-            const uint8_t *p = row + (long long)x * step;
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (k < S.nsum) v[k] = p[k];
-            if (alphaMismatch && step == 4) bad |= p[3] != a0;
-        }
-        unsigned long long sq = 0ull;
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            if (k < nsq) sq += (unsigned long long)(v[k] * v[k]);
-        unsigned long long sa = S.sqA ? (unsigned long long)(v[3] * v[3]) : 0ull;
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (k < S.nsum) {
-                const unsigned int incl = warp_incl_scan(v[k]) + carry[k];
-                if (x < S.iw) S.sum[k][o + x + 1] = incl;
-                carry[k] = __shfl_sync(0xffffffffu, incl, 31);
-            }
-        {
-            const unsigned long long incl = warp_incl_scan(sq) + carrySq;
-            if (x < S.iw) S.sq[o + x + 1] = incl;
-            carrySq = __shfl_sync(0xffffffffu, incl, 31);
-        }
-        if (S.sqA) {
-            const unsigned long long incl = warp_incl_scan(sa) + carryA;
-            if (x < S.iw) S.sqA[o + x + 1] = incl;
-            carryA = __shfl_sync(0xffffffffu, incl, 31);
-        }
-    }
-    if (alphaMismatch && __any_sync(0xffffffffu, bad) && lane == 0) atomicOr(alphaMismatch, 1u);
-}
-
-// Column prefix sums over plane rows 1..ih: a CTA owns 32 columns of one
-// plane and splits the rows into kChunks chunks (two passes).
-constexpr int kSatChunks = 16;
-
-template <typename T>
-struct PlanePtrs {
-    T *p[4];
+struct PrepArgs {
+    const uint8_t *tpl;      // template pixels whose statistics P[0] accumulates (nullptr: cached)
+    long long tstride;
+    int tw, th, tstep, cnStats, tplCtas;
+    const uint8_t *parent;   // parent whose alpha plane is scanned (nullptr: no scan)
+    long long pstride;
+    int pw, ph, parentCtas;
+    DevParams *P;
+    int n;                   // params to finalize
+    int setInit;             // store mode/cnFixed/tw/th of `init` into P[0] first
+    int initMode, initCnFixed;
+    DevFrame *F;
 };
 
-template <typename T>
-__global__ void k_sat_cols(PlanePtrs<T> planes, long long pitch, int iw, int ih) {
-    __shared__ T part[kSatChunks][32];
-    T *plane = planes.p[blockIdx.y];
-    const int c = threadIdx.x & 31, chunk = threadIdx.x >> 5;
-    const int x = blockIdx.x * 32 + c + 1;  // plane column
-    const int R = (ih + kSatChunks - 1) / kSatChunks;
-    const int r0 = 1 + chunk * R, r1 = min(ih, chunk * R + R);  // plane rows r0..r1
-    T acc = 0;
-    if (x <= iw)
-        for (int r = r0; r <= r1; r++) acc += plane[(long long)r * pitch + x];
-    part[chunk][c] = acc;
+// One launch for everything a call needs before its transforms: exact
+// template sums and squared sums (templStats, impl.go:1063-1079) with the
+// template's alpha-constancy flag, the parent's alpha scan (alphaConst,
+// cvmatch.go:146-168), and -- in the CTA that finishes last -- the cn
+// choice and tail constants of every member.  P and F are zeroed first.
+__global__ void k_prep(PrepArgs a) {
+    __shared__ int isLast;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    bool bad = false;
+    if ((int)blockIdx.x < a.tplCtas) {
+        unsigned long long sm[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+        const long long total = (long long)a.tw * a.th;
+        const uint8_t a0 = a.tstep == 4 ? a.tpl[3] : 0;
+        for (long long i = (long long)blockIdx.x * nt + tid; i < total; i += (long long)a.tplCtas * nt) {
+            const int y = (int)(i / a.tw), x = (int)(i - (long long)y * a.tw);
+            const uint8_t *p = a.tpl + (long long)y * a.tstride + (long long)x * a.tstep;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (k < a.cnStats) {
+                    const unsigned v = p[k];
+                    sm[k] += v;
+                    q[k] += v * v;
+                }
+            if (a.tstep == 4) bad |= p[3] != a0;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sm[k] += __shfl_down_sync(0xffffffffu, sm[k], o);
+                q[k] += __shfl_down_sync(0xffffffffu, q[k], o);
+            }
+        const bool anyBad = __any_sync(0xffffffffu, bad);
+        if ((tid & 31) == 0) {
+            for (int k = 0; k < a.cnStats; k++) {
+                if (sm[k]) atomicAdd(&a.P[0].tsum[k], sm[k]);
+                if (q[k]) atomicAdd(&a.P[0].tsq[k], q[k]);
+            }
+            if (anyBad) atomicOr(&a.P[0].alphaMismatch, 1u);
+        }
+    } else if (a.parent) {
+        const int c = blockIdx.x - a.tplCtas;
+        const uint8_t a0 = a.parent[3];
+        for (int y = c; y < a.ph; y += a.parentCtas) {
+            const uint8_t *row = a.parent + (long long)y * a.pstride + 3;
+            for (int x = tid; x < a.pw; x += nt) bad |= row[4LL * x] != a0;
+        }
+        if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(&a.F->alphaMismatch, 1u);
+    }
     __syncthreads();
-    if (x > iw) return;
-    T run = 0;
-    for (int k = 0; k < chunk; k++) run += part[k][c];
-    for (int r = r0; r <= r1; r++) {
-        T *e = plane + (long long)r * pitch + x;
-        run += *e;
-        *e = run;
+    if (tid == 0) {
+        __threadfence();
+        isLast = atomicAdd(&a.F->done, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!isLast) return;
+    __threadfence();
+    if (tid == 0 && a.setInit) {
+        a.P[0].mode = a.initMode;
+        a.P[0].cnFixed = a.initCnFixed;
+        a.P[0].tw = a.tw;
+        a.P[0].th = a.th;
+    }
+    __syncthreads();
+    DevFrame F;
+    F.alphaMismatch = ((volatile DevFrame *)a.F)->alphaMismatch;
+    for (int i = tid; i < a.n; i += nt) {
+        DevParams p;
+        const volatile DevParams *src = a.P + i;
+        for (int k = 0; k < 4; k++) {
+            p.tsum[k] = src->tsum[k];
+            p.tsq[k] = src->tsq[k];
+        }
+        p.alphaMismatch = src->alphaMismatch;
+        p.mode = src->mode;
+        p.cnFixed = src->cnFixed;
+        p.tw = src->tw;
+        p.th = src->th;
+        finalize_params(p, F, &a.F->cnMax);
+        a.P[i] = p;
     }
 }
 
@@ -611,27 +558,19 @@ __global__ void k_cols(ColsArgs a) {
 
 // ------------------------------------------------------- inverse rows
 
-__device__ __forceinline__ long long win_u32(const unsigned int *__restrict__ p, long long P, int X,
-                                             int Y, int tw, int th) {
-    const unsigned int a = __ldg(p + (long long)(Y + th) * P + X + tw);
-    const unsigned int b = __ldg(p + (long long)(Y + th) * P + X);
-    const unsigned int c = __ldg(p + (long long)Y * P + X + tw);
-    const unsigned int d = __ldg(p + (long long)Y * P + X);
-    return (long long)(unsigned int)(a - b - c + d);
-}
-
-__device__ __forceinline__ long long win_u64(const unsigned long long *__restrict__ p, long long P,
-                                             int X, int Y, int tw, int th) {
-    const unsigned long long a = __ldg(p + (long long)(Y + th) * P + X + tw);
-    const unsigned long long b = __ldg(p + (long long)(Y + th) * P + X);
-    const unsigned long long c = __ldg(p + (long long)Y * P + X + tw);
-    const unsigned long long d = __ldg(p + (long long)Y * P + X);
-    return (long long)(a - b - c + d);
-}
-
-// float32(float64(v)) (impl.go:902-1009): two roundings, as pinned.
+// float32(float64(v)) (impl.go:902-1009), two roundings as pinned.  Below
+// 2^53 the first rounding is exact, so one int64->float32 rounding gives
+// the same bits; above it the 53-bit rounding is done in integers.  No
+// FP64 instruction (GB300's FP64 rate is a small fraction of FP32).
 __device__ __forceinline__ float f32_via_f64(long long v) {
-    return __double2float_rn(__ll2double_rn(v));
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    if (a < (1ull << 53)) return __ll2float_rn(v);
+    const int sh = (64 - __clzll((long long)a)) - 53;
+    unsigned long long q = a >> sh;
+    const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1ull))) q++;
+    const float f = __ull2float_rn(q << sh);
+    return v < 0 ? -f : f;
 }
 
 // normOne (impl.go:825-849).
@@ -720,112 +659,262 @@ struct InvArgs {
     FftClass fc;
     int cls, cnS;
     MemberSet ms;
-    SatPlanes S;
-    Partial *partials;
-    int ctasPerTile, pairsPerCta, partOffset;
+    int pairsPerCta;
 };
 
-// inverseRowPair (impl.go:394-444) for P row pairs of one (member, tile),
-// all channels accumulated in channel order, then normOne per element and
-// the CTA's first-occurrence extrema.
+// inverseRowPair (impl.go:394-444) for P row pairs of one (member, tile):
+// combine, inverse row transform, then the channels accumulated in channel
+// order (the add=k>0 emit of impl.go:425-443) and stored as the raw
+// correlation the normalisation consumes.
 __global__ void k_inv_rows(InvArgs a) {
     extern __shared__ float2 smem[];
-    __shared__ Ext shExt[kThreads / 32];
     const FftClass &fc = a.fc;
     const int tileLocal = blockIdx.y;
     const int tile = fc.tileFirst + tileLocal;
     const int slot = blockIdx.z;
     const DevMember &m = member_of(a.ms, slot);
     const DevParams &Pm = a.ms.params[m.pIdx];
+    if (Pm.flat) return;
     const TileBox tb = tile_box(a.g, tile);
     const int tx = tile % a.g.ntx, ty = tile / a.g.ntx;
     const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
     const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
     const int pair0 = blockIdx.x * a.pairsPerCta;
+    if (2 * pair0 >= bh) return;
+    const int P = min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1);
     const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * n);  // [P][2][n]
+    const int cn = Pm.cn;
+    const size_t chanStride = (size_t)fc.dftH * hwp;
+    const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
+    for (int k = 0; k < cn; k++) {
+        const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
+        for (int idx = tid; idx < P * n; idx += nt) {
+            const int p = idx >> log2n, kk = idx & (n - 1);
+            const int r = 2 * (pair0 + p);
+            const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
+            const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
+            float2 z;
+            if (kk < hw) {
+                const float2 u = sa[kk], v = sb[kk];
+                z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+            } else {
+                const int mm = n - kk;
+                const float2 u = sa[mm], v = sb[mm];
+                z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+            }
+            smem[p * n + brev_bits(kk, log2n)] = z;
+        }
+        __syncthreads();
+        fft_lines<true>(smem, n, log2n, P, n, fc.triW);
+        for (int idx = tid; idx < P * bw; idx += nt) {
+            const int p = idx / bw, x = idx - p * bw;
+            const float2 z = smem[p * n + x];
+            float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
+            if (k == 0) {
+                *a0 = z.x;
+                *a1 = z.y;
+            } else {
+                *a0 = __fadd_rn(*a0, z.x);
+                *a1 = __fadd_rn(*a1, z.y);
+            }
+        }
+        __syncthreads();
+    }
+    float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
+    for (int idx = tid; idx < 2 * P * bw; idx += nt) {
+        const int rr = idx / bw, x = idx - rr * bw;
+        const int r = 2 * pair0 + rr;
+        if (r < bh) corr[(size_t)(tb.y0 + r) * m.rw + tb.x0 + x] = acc[(size_t)rr * n + x];
+    }
+}
+
+// ----------------------------------------------------------- normalise
+
+struct NormArgs {
+    const uint8_t *img;
+    long long istride;
+    int step;
+    MemberSet ms;
+    int CW, B, ncx;
+    int cnCap;            // channel capacity of the column arrays
+    int ncCap;            // column capacity of the column arrays
+    Partial *partials;
+    unsigned char *gscratch;  // per-CTA column arrays when they exceed shared memory
+    size_t gscratchPerCta;
+};
+
+// Window statistics by sliding column sums, the reference's own scheme
+// (colBuildGo/colSlideGo, impl.go:708-805, and the per-row window sums of
+// impl.go:884-893) run for a CW x B block of results per CTA: column sums
+// over the th rows under the block's first row, then per row an exclusive
+// prefix over the columns gives every window sum as a difference, the
+// normOne tail scores the raw correlation, and the columns slide one row
+// down.  All statistics are exact integers (u32 sums are modular: every
+// window sum is < 2^32), so any schedule yields the reference's values.
+__global__ void k_norm(NormArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ Ext shExt[kThreads / 32];
+    __shared__ unsigned int wsS[kThreads / 32][4];
+    __shared__ unsigned long long wsQ[kThreads / 32];
+    const int slot = blockIdx.z;
+    const DevMember &m = member_of(a.ms, slot);
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    const int X0 = blockIdx.x * a.CW, Y0 = blockIdx.y * a.B;
     const int tid = threadIdx.x, nt = blockDim.x;
     Ext e;
     ext_init(e);
-    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
-    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * n);  // [P][2][n]
-    if (P > 0) {
-        const int cn = Pm.cn;
-        const bool flat = Pm.flat != 0;
-        const size_t chanStride = (size_t)fc.dftH * hwp;
-        const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
-        if (!flat) {
-            for (int k = 0; k < cn; k++) {
-                const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
-                for (int idx = tid; idx < P * n; idx += nt) {
-                    const int p = idx >> log2n, kk = idx & (n - 1);
-                    const int r = 2 * (pair0 + p);
-                    const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
-                    const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
-                    float2 z;
-                    if (kk < hw) {
-                        const float2 u = sa[kk], v = sb[kk];
-                        z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
-                    } else {
-                        const int mm = n - kk;
-                        const float2 u = sa[mm], v = sb[mm];
-                        z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
-                    }
-                    smem[p * n + brev_bits(kk, log2n)] = z;
-                }
-                __syncthreads();
-                fft_lines<true>(smem, n, log2n, P, n, fc.triW);
-                for (int idx = tid; idx < P * bw; idx += nt) {
-                    const int p = idx / bw, x = idx - p * bw;
-                    const float2 z = smem[p * n + x];
-                    float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
-                    if (k == 0) {
-                        *a0 = z.x;
-                        *a1 = z.y;
-                    } else {
-                        *a0 = __fadd_rn(*a0, z.x);
-                        *a1 = __fadd_rn(*a1, z.y);
-                    }
-                }
-                __syncthreads();
+    float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
+    float *map = a.ms.map;
+    if (X0 < m.rw && Y0 < m.rh) {
+        const int CWv = min(a.CW, m.rw - X0), Bv = min(a.B, m.rh - Y0);
+        if (Pm.flat) {
+            for (int idx = tid; idx < CWv * Bv; idx += nt) {
+                const int yy = idx / CWv, x = idx - yy * CWv;
+                const long long li = (long long)(Y0 + yy) * m.rw + X0 + x;
+                if (map) map[li] = 1.f;
+                ext_add(e, 1.f, li);
             }
-        }
-        // Normalisation + extrema over the P row pairs.
-        const long long area = (long long)m.tw * m.th;
-        const SatPlanes &S = a.S;
-        for (int idx = tid; idx < 2 * P * bw; idx += nt) {
-            const int rr = idx / bw, x = idx - rr * bw;
-            const int r = 2 * pair0 + rr;
-            if (r >= bh) continue;
-            const int X = tb.x0 + x, Y = tb.y0 + r;
-            float score;
-            if (flat) {
-                score = 1.f;
-            } else {
-                const float corr = acc[(size_t)rr * n + x];
-                long long s[4] = {0, 0, 0, 0};
-                long long cross = 0, sq = 0;
+        } else {
+            const int cn = Pm.cn, tw = m.tw, th = m.th, step = a.step;
+            const int NC = CWv + tw - 1;
+            const int cap = a.ncCap;
+            unsigned char *base = a.gscratch
+                                      ? a.gscratch + (size_t)(blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)) *
+                                                         a.gscratchPerCta
+                                      : smraw;
+            unsigned long long *colQ = reinterpret_cast<unsigned long long *>(base);
+            unsigned long long *preQ = colQ + cap;
+            unsigned int *colS = reinterpret_cast<unsigned int *>(preQ + cap + 1);
+            unsigned int *preS = colS + (size_t)a.cnCap * cap;
+            const int capP = cap + 1;
+            const long long area = (long long)tw * th;
+            // Column sums over rows Y0 .. Y0+th-1 (colBuildGo).
+            for (int c = tid; c < NC; c += nt) {
+                const uint8_t *p = a.img + (long long)Y0 * a.istride + (long long)(X0 + c) * step;
+                unsigned int sk[4] = {0u, 0u, 0u, 0u};
+                unsigned long long q = 0;
+                for (int dy = 0; dy < th; dy++, p += a.istride) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (k < cn) {
+                            const unsigned v = p[k];
+                            sk[k] += v;
+                            q += v * v;
+                        }
+                }
 #pragma unroll
                 for (int k = 0; k < 4; k++)
-                    if (k < cn) {
-                        s[k] = win_u32(S.sum[k], S.pitch, X, Y, m.tw, m.th);
-                        cross += s[k] * (long long)Pm.tsum[k];
-                        sq += s[k] * s[k];
-                    }
-                long long s2 = win_u64(S.sq, S.pitch, X, Y, m.tw, m.th);
-                if (cn == 4) s2 += win_u64(S.sqA, S.pitch, X, Y, m.tw, m.th);
-                const long long lane0 = cn == 1 ? s[0] : cross;
-                score = norm_one(corr, f32_via_f64(lane0), f32_via_f64(area * s2 - sq), f32_via_f64(s2),
-                                 Pm.numScale, Pm.varScale, Pm.templNorm);
+                    if (k < cn) colS[(size_t)k * cap + c] = sk[k];
+                colQ[c] = q;
             }
-            const long long li = (long long)Y * m.rw + X;
-            if (a.ms.map) a.ms.map[li] = score;
-            ext_add(e, score, li);
+            __syncthreads();
+            const int seg = (NC + nt - 1) / nt;
+            const int c0 = tid * seg, c1 = min(NC, c0 + seg);
+            const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+            for (int y = Y0; y < Y0 + Bv; y++) {
+                // Exclusive prefix of the column sums: segment totals, a
+                // block scan of the totals, then the segment's running sums.
+                unsigned int ts[4] = {0u, 0u, 0u, 0u};
+                unsigned long long tq = 0;
+                for (int c = c0; c < c1; c++) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (k < cn) ts[k] += colS[(size_t)k * cap + c];
+                    tq += colQ[c];
+                }
+                unsigned int is[4];
+                unsigned long long iq = tq;
+#pragma unroll
+                for (int k = 0; k < 4; k++) is[k] = ts[k];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const unsigned int u = __shfl_up_sync(0xffffffffu, is[k], o);
+                        if (lane >= o) is[k] += u;
+                    }
+                    const unsigned long long u = __shfl_up_sync(0xffffffffu, iq, o);
+                    if (lane >= o) iq += u;
+                }
+                if (lane == 31) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) wsS[warp][k] = is[k];
+                    wsQ[warp] = iq;
+                }
+                __syncthreads();
+                unsigned int rs[4];
+                unsigned long long rq = iq - tq;
+#pragma unroll
+                for (int k = 0; k < 4; k++) rs[k] = is[k] - ts[k];
+                for (int w = 0; w < warp; w++) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) rs[k] += wsS[w][k];
+                    rq += wsQ[w];
+                }
+                (void)nw;
+                for (int c = c0; c < c1; c++) {
+                    if (c == 0) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (k < cn) preS[(size_t)k * capP] = 0u;
+                        preQ[0] = 0ull;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (k < cn) {
+                            rs[k] += colS[(size_t)k * cap + c];
+                            preS[(size_t)k * capP + c + 1] = rs[k];
+                        }
+                    rq += colQ[c];
+                    preQ[c + 1] = rq;
+                }
+                __syncthreads();
+                // Scores of row y (the spill + normOne of impl.go:895-1021).
+                const float *crow = corr + (size_t)y * m.rw + X0;
+                for (int x = tid; x < CWv; x += nt) {
+                    long long cross = 0, sq = 0, s0 = 0;
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (k < cn) {
+                            const unsigned int sk = preS[(size_t)k * capP + x + tw] - preS[(size_t)k * capP + x];
+                            if (k == 0) s0 = sk;
+                            cross += (long long)((unsigned long long)sk * (unsigned long long)(unsigned int)Pm.tsum[k]);
+                            sq += (long long)((unsigned long long)sk * (unsigned long long)sk);
+                        }
+                    const long long s2 = (long long)(preQ[x + tw] - preQ[x]);
+                    const long long lane0 = cn == 1 ? s0 : cross;
+                    const float score = norm_one(crow[x], f32_via_f64(lane0), f32_via_f64(area * s2 - sq),
+                                                 f32_via_f64(s2), Pm.numScale, Pm.varScale, Pm.templNorm);
+                    const long long li = (long long)y * m.rw + X0 + x;
+                    if (map) map[li] = score;
+                    ext_add(e, score, li);
+                }
+                // Slide the columns one row down (colSlideGo).
+                if (y + 1 < Y0 + Bv) {
+                    for (int c = tid; c < NC; c += nt) {
+                        const uint8_t *pa = a.img + (long long)(y + th) * a.istride + (long long)(X0 + c) * step;
+                        const uint8_t *ps = a.img + (long long)y * a.istride + (long long)(X0 + c) * step;
+                        long long dq = 0;
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (k < cn) {
+                                const int va = pa[k], vb = ps[k];
+                                colS[(size_t)k * cap + c] += (unsigned int)(va - vb);
+                                dq += va * va - vb * vb;
+                            }
+                        colQ[c] += (unsigned long long)dq;
+                    }
+                }
+                __syncthreads();
+            }
         }
     }
     __syncthreads();
     ext_block_reduce(e, shExt);
     if (tid == 0) {
-        Partial &o = a.partials[m.partBase + a.partOffset + blockIdx.y * a.ctasPerTile + blockIdx.x];
+        Partial &o = a.partials[m.partBase + blockIdx.y * a.ncx + blockIdx.x];
         o.minV = e.minV;
         o.maxV = e.maxV;
         o.minI = e.minI;
@@ -920,48 +1009,38 @@ cudaError_t launch_alpha_scan(const uint8_t *img, long long stride, int w, int h
     return cudaGetLastError();
 }
 
-cudaError_t launch_tpl_stats(const uint8_t *tpl, long long tstride, int tw, int th, int step,
-                             int cnStats, DevParams *P, cudaStream_t st) {
-    const long long total = (long long)tw * th;
-    int blocks = (int)((total + kThreads - 1) / kThreads);
-    if (blocks > 1024) blocks = 1024;
-    ProfScope ps("k_tpl_stats", st);
-    k_tpl_stats<<<blocks, kThreads, 0, st>>>(tpl, tstride, tw, th, step, cnStats, P);
-    count_launches(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_params_finalize(DevParams *P, int n, DevFrame *F, cudaStream_t st) {
-    ProfScope ps("k_params_finalize", st);
-    k_params_finalize<<<(n + 127) / 128, 128, 0, st>>>(P, n, F);
-    count_launches(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sat(const uint8_t *img, long long istride, int step, const SatPlanes &S,
-                       unsigned int *alphaMismatch, cudaStream_t st) {
-    const int rowsPerCta = kThreads / 32;
-    {
-    ProfScope ps("k_sat_rows", st);
-    k_sat_rows<<<(S.ih + rowsPerCta - 1) / rowsPerCta, kThreads, 0, st>>>(img, istride, step, S,
-                                                                            alphaMismatch);
+cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, int tstep, int cnStats,
+                        const uint8_t *parent, long long pstride, int pw, int ph, DevParams *P, int n,
+                        int setInit, int initMode, int initCnFixed, DevFrame *F, cudaStream_t st) {
+    PrepArgs a;
+    a.tpl = tpl;
+    a.tstride = tstride;
+    a.tw = tw;
+    a.th = th;
+    a.tstep = tstep;
+    a.cnStats = cnStats;
+    a.tplCtas = 0;
+    if (tpl) {
+        const long long total = (long long)tw * th;
+        long long c = (total + 4 * kThreads - 1) / (4 * kThreads);
+        a.tplCtas = (int)(c < 1 ? 1 : (c > 128 ? 128 : c));
     }
+    a.parent = parent;
+    a.pstride = pstride;
+    a.pw = pw;
+    a.ph = ph;
+    a.parentCtas = parent ? (ph < 304 ? ph : 304) : 0;
+    a.P = P;
+    a.n = n;
+    a.setInit = setInit;
+    a.initMode = initMode;
+    a.initCnFixed = initCnFixed;
+    a.F = F;
+    int grid = a.tplCtas + a.parentCtas;
+    if (grid < 1) grid = 1;
+    ProfScope ps("k_prep", st);
+    k_prep<<<grid, kThreads, 0, st>>>(a);
     count_launches(1);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    dim3 block(32 * kSatChunks);
-    PlanePtrs<unsigned int> sp;
-    for (int k = 0; k < 4; k++) sp.p[k] = S.sum[k];
-    ProfScope ps("k_sat_cols", st);
-    dim3 g1((S.iw + 31) / 32, S.nsum);
-    k_sat_cols<unsigned int><<<g1, block, 0, st>>>(sp, S.pitch, S.iw, S.ih);
-    PlanePtrs<unsigned long long> qp;
-    qp.p[0] = S.sq;
-    qp.p[1] = S.sqA;
-    qp.p[2] = qp.p[3] = nullptr;
-    dim3 g2((S.iw + 31) / 32, S.sqA ? 2 : 1);
-    k_sat_cols<unsigned long long><<<g2, block, 0, st>>>(qp, S.pitch, S.iw, S.ih);
-    count_launches(2);
     return cudaGetLastError();
 }
 
@@ -1030,26 +1109,68 @@ int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta) {
     return (pairs + P - 1) / P;
 }
 
-cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS,
-                            const MemberSet &ms, int nmembers, const SatPlanes &S,
-                            Partial *partials, int partOffset, int ctasPerTile, int pairsPerCta,
-                            cudaStream_t st) {
+cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
+                            int nmembers, cudaStream_t st) {
     InvArgs a;
     a.g = g;
     a.fc = fc;
     a.cls = cls;
     a.cnS = cnS;
     a.ms = ms;
-    a.S = S;
-    a.partials = partials;
-    a.partOffset = partOffset;
-    a.ctasPerTile = ctasPerTile;
-    a.pairsPerCta = pairsPerCta;
-    dim3 grid(ctasPerTile, fc.ntiles, nmembers);
-    const size_t smem = (size_t)pairsPerCta * fc.n * (sizeof(float2) + 2 * sizeof(float));
+    int P = 0;
+    const int ctas = inv_rows_ctas_per_tile(fc, &P);
+    a.pairsPerCta = P;
+    dim3 grid(ctas, fc.ntiles, nmembers);
+    const size_t smem = (size_t)P * fc.n * (sizeof(float2) + 2 * sizeof(float));
     set_smem(k_inv_rows, smem);
     ProfScope ps("k_inv_rows", st);
     k_inv_rows<<<grid, kThreads, smem, st>>>(a);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+static size_t norm_arrays_bytes(int cap, int cnCap) {
+    return 8 * (2 * (size_t)cap + 1) + 4 * (size_t)cnCap * cap + 4 * (size_t)cnCap * (cap + 1);
+}
+
+NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap) {
+    NormGrid g;
+    g.CW = kThreads;
+    g.B = 32;
+    g.ncx = (rwMax + g.CW - 1) / g.CW;
+    g.nby = (rhMax + g.B - 1) / g.B;
+    g.cnCap = cnCap;
+    g.ncCap = g.CW + twMax - 1;
+    const size_t bytes = norm_arrays_bytes(g.ncCap, cnCap);
+    if (bytes <= 200 * 1024) {
+        g.smemBytes = bytes;
+        g.scratchPerCta = 0;
+    } else {
+        g.smemBytes = 0;
+        g.scratchPerCta = (bytes + 255) / 256 * 256;
+    }
+    return g;
+}
+
+cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
+                        const NormGrid &ng, Partial *partials, unsigned char *gscratch, cudaStream_t st) {
+    NormArgs a;
+    a.img = img;
+    a.istride = istride;
+    a.step = step;
+    a.ms = ms;
+    a.CW = ng.CW;
+    a.B = ng.B;
+    a.ncx = ng.ncx;
+    a.cnCap = ng.cnCap;
+    a.ncCap = ng.ncCap;
+    a.partials = partials;
+    a.gscratch = ng.scratchPerCta ? gscratch : nullptr;
+    a.gscratchPerCta = ng.scratchPerCta;
+    dim3 grid(ng.ncx, ng.nby, nmembers);
+    set_smem(k_norm, ng.smemBytes);
+    ProfScope ps("k_norm", st);
+    k_norm<<<grid, kThreads, ng.smemBytes, st>>>(a);
     count_launches(1);
     return cudaGetLastError();
 }
