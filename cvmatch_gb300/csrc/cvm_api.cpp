@@ -283,7 +283,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     const NormGrid ng = norm_grid(rw, rh, J.tw, cnS);
     const int nparts = ng.ncx * ng.nby;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
-                   Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(ng.scratchPerCta * nparts, 1);
+                   Arena::bytes(nparts, sizeof(Partial));
     if (!J.map) bytes += Arena::bytes((size_t)rw * rh, sizeof(float));
     for (int c = 0; c < G->nclass; c++) {
         bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
@@ -296,7 +296,6 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     DevParams *P = A.take<DevParams>(1);
     DevFrame *F = A.take<DevFrame>(1);
     Partial *parts = A.take<Partial>(nparts);
-    unsigned char *normScratch = A.take<unsigned char>(ng.scratchPerCta * nparts);
     float *corr = J.map ? J.map : A.take<float>((size_t)rw * rh);
     float2 *spec[2] = {nullptr, nullptr};
     const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
@@ -341,8 +340,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
         CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, st));
     }
-    CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, parts, normScratch, st));
-    CVM_CUDA(launch_extrema_final(ms, 1, parts, nparts, J.out, st));
+    CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, parts, &F->normDone, J.out, st));
     return CVM_OK;
 }
 
@@ -676,25 +674,25 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         }
         const size_t corrPer = (size_t)bg.rwMax * bg.rhMax;
         const int nparts = bg.ng.ncx * bg.ng.nby;
-        per += corrPer * sizeof(float) + bg.ng.scratchPerCta * nparts;
+        per += corrPer * sizeof(float);
         frameBytes = std::max(frameBytes, fb);
         partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
         w = std::min<int>(w, (int)bg.members.size());
         wave[b] = w;
-        size_t wb = Arena::bytes((size_t)w * corrPer, sizeof(float)) +
-                    Arena::bytes((size_t)w * bg.ng.scratchPerCta * nparts, 1);
+        size_t wb = Arena::bytes((size_t)w * corrPer, sizeof(float));
         for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));
         waveBytes = std::max(waveBytes, wb);
     }
-    const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) + frameBytes +
-                         partBytes + waveBytes;
+    const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
+                         Arena::bytes(n, sizeof(int)) + frameBytes + partBytes + waveBytes;
     PoolBuf buf;
     CVM_TRY(pool_alloc(buf, bytes, st));
     Arena A;
     A.base = static_cast<char *>(buf.p);
     DevParams *P = A.take<DevParams>(n);
     DevFrame *F = A.take<DevFrame>(1);
+    int *counters = A.take<int>(n);
     char *frameBase = A.base + A.used;
     A.used += frameBytes;
     Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
@@ -702,6 +700,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     char *waveBase = A.base + A.used;
     CVM_CUDA(cudaMemcpyAsync(P, f->dP, n * sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
     CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
+    CVM_CUDA(cudaMemsetAsync(counters, 0, n * sizeof(int), st));
     CVM_CUDA(launch_prep(nullptr, 0, 0, 0, f->step, 0, f->step == 4 ? dParent : nullptr, pstride, pw, ph, P, n, 0, 0,
                          0, F, st));
     for (size_t b = 0; b < fg->bg.size(); b++) {
@@ -711,7 +710,6 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
         float *corr = nullptr;
-        unsigned char *normScratch = nullptr;
         {
             Arena fa;
             fa.base = frameBase;
@@ -722,7 +720,6 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 scratch[c] = wa.take<float2>((size_t)wave[b] * bg.memberScratch[c]);
             }
             corr = wa.take<float>((size_t)wave[b] * bg.rwMax * bg.rhMax);
-            normScratch = wa.take<unsigned char>((size_t)wave[b] * bg.ng.scratchPerCta * nparts);
         }
         // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
         for (int c = 0; c < G.nclass; c++) {
@@ -750,10 +747,9 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
                 CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, st));
             }
-            CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, parts, normScratch, st));
+            CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, parts, counters, dOut, st));
         }
-        ms.first = 0;
-        CVM_CUDA(launch_extrema_final(ms, nm, parts, nparts, dOut, st));
+        (void)nparts;
     }
     return CVM_OK;
 }

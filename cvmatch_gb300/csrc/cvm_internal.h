@@ -72,7 +72,7 @@ struct DevFrame {
     unsigned int alphaMismatch;  // parent alpha plane not constant
     int cnMax;                   // largest effective cn among the members
     int done;                    // CTAs of k_prep finished (last one finalises)
-    int pad;
+    int normDone;                // CTAs of a solo k_norm finished (last one merges)
 };
 
 // One correlation target of the tail kernels: a solo match or one fleet
@@ -84,7 +84,7 @@ struct DevMember {
     const float2 *tspec[2];    // template spectrum, [ch][dftH][hwp], natural rows
     int pIdx;                  // index into the launch's DevParams array
     int tw, th, rw, rh;
-    int partBase;              // first partial record of this member
+    int partBase;              // first partial record of this member (norm CTAs)
     int outIdx;                // result slot
     int pad;
 };
@@ -137,18 +137,18 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
 // Inverse rows + channel accumulation into each member's raw correlation.
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
                             int nmembers, cudaStream_t st);
-// Normalisation + first-occurrence extrema partials: CW x B results per
-// CTA; `ncx` x `nby` CTAs per member.
+// Normalisation + first-occurrence extrema: CW x B results per CTA, ncx x
+// nby CTAs per member, result rows in groups of G; the member's last CTA
+// writes its result to out[outIdx].  counters (one int per member of the
+// table, or one for a solo match) must be zero before the launch.
 struct NormGrid {
-    int CW, B, ncx, nby, ncCap, cnCap;
-    size_t smemBytes;       // dynamic shared memory per CTA (0 with global scratch)
-    size_t scratchPerCta;   // global scratch per CTA when the arrays exceed shared memory
+    int CW, B, G, ncx, nby, ncCap, cnCap;
+    size_t smemBytes;       // dynamic shared memory per CTA
+    size_t scratchPerCta;   // unused (kept 0): every shape fits shared memory
 };
 NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap);
 cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
-                        const NormGrid &ng, Partial *partials, unsigned char *gscratch, cudaStream_t st);
-cudaError_t launch_extrema_final(const MemberSet &ms, int nmembers, const Partial *partials,
-                                 int nparts, cvm_result *out, cudaStream_t st);
+                        const NormGrid &ng, Partial *partials, int *counters, cvm_result *out, cudaStream_t st);
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).
 cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st);

@@ -22,8 +22,8 @@
 //                     (radix4cols.go:111-125, impl.go:376-388)
 //   k_inv_rows        inverseRowPair (impl.go:394-444) + channel accumulation
 //   k_norm            sliding column sums (colBuildGo/colSlideGo, impl.go:708-805),
-//                     normOne (impl.go:825-849), first-occurrence extrema
-//   k_extrema_final   band merge (impl.go:1104-1112) over CTA partials
+//                     normOne (impl.go:825-849), first-occurrence extrema merged
+//                     in raster order (impl.go:1104-1112) by each member's last CTA
 //   k_shrink_gather   shrinkInto (impl.go:591-610)
 #include <cfloat>
 #include <cstdio>
@@ -150,93 +150,154 @@ __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2
     *pd = make_float2(__fsub_rn(s1x, rr), __fsub_rn(s1y, ri));
 }
 
-// The radix-4 cascade (fftR4Scalar, radix4.go:106-149) over `lines`
-// contiguous rows of n elements (row stride ld) in shared memory, input in
-// bit-reversed order.  Each stage is one barrier-separated sweep; a thread
-// owns whole butterflies.
-template <bool INV>
-__device__ void fft_lines(float2 *s, int n, int log2n, int lines, int ld,
-                          const float2 *__restrict__ tri) {
+// ------------------------------------------------- radix-4 cascade passes
+// The reference cascade (fftR4Scalar, radix4.go:106-149) on bit-reversed
+// input: an optional radix-2 head (odd log2 n), then radix-4 stages with
+// quarter sizes h = h0, 4h0, 16h0, ...  A butterfly of stage h touches
+// elements base+j+{0,h,2h,3h} of a 4h-block, so the 16 elements
+// B+j+h*i (i < 16, B a multiple of 16h, j < h) hold four complete
+// butterflies of stage h and four of stage 4h: a thread runs two stages in
+// registers per pass and the data crosses shared memory once per pass
+// instead of once per stage.  Every butterfly is the same single-rounded
+// op sequence with the same twiddle, so results are bit-identical to the
+// stage-by-stage cascade.  Passes over one line:
+//   odd log2 n:  [R2 + R4(h=2) on 8 contiguous]  then pairs from h=8
+//   even log2 n: pairs from h=1
+//   a trailing single radix-4 stage when one remains.
+
+template <bool INV, typename Addr>
+__device__ __forceinline__ void unit_r16(float2 *s, const Addr &addr, int base, int h, const float2 *__restrict__ tA,
+                                         const float2 *__restrict__ tB) {
+    float2 e[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) e[i] = s[addr(base + h * i)];
+    const int j = base & (h - 1);
+    const float2 a1 = __ldg(tA + j), a2 = __ldg(tA + h + j), a3 = __ldg(tA + 2 * h + j);
+#pragma unroll
+    for (int b = 0; b < 4; b++) bfly4<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int jj = j + h * q;
+        bfly4<INV>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + jj), __ldg(tB + 4 * h + jj),
+                   __ldg(tB + 8 * h + jj));
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[addr(base + h * i)] = e[i];
+}
+
+template <bool INV, typename Addr>
+__device__ __forceinline__ void unit_r4(float2 *s, const Addr &addr, int base, int h, const float2 *__restrict__ t) {
+    float2 e[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) e[i] = s[addr(base + h * i)];
+    const int j = base & (h - 1);
+    bfly4<INV>(&e[0], &e[1], &e[2], &e[3], __ldg(t + j), __ldg(t + h + j), __ldg(t + 2 * h + j));
+#pragma unroll
+    for (int i = 0; i < 4; i++) s[addr(base + h * i)] = e[i];
+}
+
+// The radix-2 head plus the h=2 radix-4 stage on 8 contiguous elements.
+template <bool INV, typename Addr>
+__device__ __forceinline__ void unit_head8(float2 *s, const Addr &addr, int base, const float2 *__restrict__ t) {
+    float2 e[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) e[i] = s[addr(base + i)];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const float2 u = e[i], v = e[i + 1];
+        e[i] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+        e[i + 1] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+        bfly4<INV>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[addr(base + i)] = e[i];
+}
+
+// The radix-2 head alone (n = 2, 4-point odd... only n == 2 needs it).
+template <typename Addr>
+__device__ __forceinline__ void unit_r2(float2 *s, const Addr &addr, int base) {
+    const float2 u = s[addr(base)], v = s[addr(base + 1)];
+    s[addr(base)] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+    s[addr(base + 1)] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+}
+
+// Runs the whole cascade over `lines` independent transforms of length n
+// (log2n), element (line, i) at s[la(line, i)].  LINE_FAST maps consecutive
+// threads to consecutive lines (column strips, lines a power of two);
+// otherwise to consecutive units of one line (row lines).  Ends with a
+// barrier.
+template <bool INV, bool LINE_FAST = false, typename LineAddr>
+__device__ void fft_cascade(float2 *s, int n, int log2n, int lines, const LineAddr &la,
+                            const float2 *__restrict__ tri) {
     const int tid = threadIdx.x, nt = blockDim.x;
     int h = 1;
+    const float2 *t = tri;
     if (log2n & 1) {
-        const int half = n >> 1;
-        const int tot = half * lines;
-        for (int b = tid; b < tot; b += nt) {
-            const int line = b >> (log2n - 1);
-            const int i = (b & (half - 1)) << 1;
-            float2 *a = s + line * ld + i;
-            const float2 u = a[0], v = a[1];
-            a[0] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
-            a[1] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+        if (n == 2) {
+            for (int u = tid; u < lines; u += nt) {
+                auto addr = [&](int i) { return la(u, i); };
+                unit_r2(s, addr, 0);
+            }
+            __syncthreads();
+            return;
+        }
+        const int units = n >> 3;
+        for (int u = tid; u < lines * units; u += nt) {
+            const int line = LINE_FAST ? (u & (lines - 1)) : u / units;
+            const int base = (LINE_FAST ? (u / lines) : (u - line * units)) << 3;
+            auto addr = [&](int i) { return la(line, i); };
+            unit_head8<INV>(s, addr, base, t);
         }
         __syncthreads();
-        h = 2;
+        t += 6;  // the h=2 stage's table
+        h = 8;
     }
-    const float2 *t = tri;
-    for (; 4 * h <= n; h <<= 2) {
-        const int quarter = n >> 2;
-        const int tot = quarter * lines;
-        for (int b = tid; b < tot; b += nt) {
-            const int line = b >> (log2n - 2);
-            const int q = b & (quarter - 1);
-            const int j = q & (h - 1);
-            float2 *a = s + line * ld + ((q - j) << 2) + j;
-            bfly4<INV>(a, a + h, a + 2 * h, a + 3 * h, __ldg(t + j), __ldg(t + h + j),
-                       __ldg(t + 2 * h + j));
+    while (16 * h <= n) {
+        const int units = n >> 4;
+        const float2 *tB = t + 3 * h;
+        for (int u = tid; u < lines * units; u += nt) {
+            const int line = LINE_FAST ? (u & (lines - 1)) : u / units;
+            const int v = LINE_FAST ? u / lines : u - line * units;
+            const int j = v & (h - 1), blk = v >> (31 - __clz(h));
+            const int base = blk * 16 * h + j;
+            auto addr = [&](int i) { return la(line, i); };
+            unit_r16<INV>(s, addr, base, h, t, tB);
         }
-        t += 3 * h;
+        __syncthreads();
+        t = tB + 12 * h;
+        h *= 16;
+    }
+    if (4 * h <= n) {
+        const int units = n >> 2;
+        for (int u = tid; u < lines * units; u += nt) {
+            const int line = LINE_FAST ? (u & (lines - 1)) : u / units;
+            const int v = LINE_FAST ? u / lines : u - line * units;
+            const int j = v & (h - 1), blk = v >> (31 - __clz(h));
+            const int base = blk * 4 * h + j;
+            auto addr = [&](int i) { return la(line, i); };
+            unit_r4<INV>(s, addr, base, h, t);
+        }
         __syncthreads();
     }
 }
 
+// Padded shared-memory line layout: one spare slot every 16 elements keeps
+// the strided pass accesses free of bank conflicts.
+__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int padded_len(int n) { return n + (n >> 4) + 1; }
+
 // The column twin (colsR4Go, radix4cols.go:35-125) on a [n x SC] strip in
-// shared memory, element (row r, column c) at s[r*SC + c].  RMAP conjugates
+// shared memory, element (row r, column c) at s[r*SC + c]; RMAP conjugates
 // every row access by the bit reversal (the inverse path's rmap = brev).
 template <bool INV, bool RMAP>
-__device__ void fft_cols(float2 *s, int n, int log2n, int SC, int logSC,
-                         const float2 *__restrict__ tri) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    int h = 1;
-    if (log2n & 1) {
-        const int tot = (n >> 1) << logSC;
-        for (int b = tid; b < tot; b += nt) {
-            const int c = b & (SC - 1);
-            const int r = (b >> logSC) << 1;
-            int i0 = r, i1 = r + 1;
-            if (RMAP) {
-                i0 = brev_bits(i0, log2n);
-                i1 = brev_bits(i1, log2n);
-            }
-            float2 *p = s + i0 * SC + c, *q = s + i1 * SC + c;
-            const float2 u = *p, v = *q;
-            *p = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
-            *q = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
-        }
-        __syncthreads();
-        h = 2;
-    }
-    const float2 *t = tri;
-    for (; 4 * h <= n; h <<= 2) {
-        const int tot = (n >> 2) << logSC;
-        for (int b = tid; b < tot; b += nt) {
-            const int c = b & (SC - 1);
-            const int q = b >> logSC;
-            const int j = q & (h - 1);
-            const int r = ((q - j) << 2) + j;
-            int i0 = r, i1 = r + h, i2 = r + 2 * h, i3 = r + 3 * h;
-            if (RMAP) {
-                i0 = brev_bits(i0, log2n);
-                i1 = brev_bits(i1, log2n);
-                i2 = brev_bits(i2, log2n);
-                i3 = brev_bits(i3, log2n);
-            }
-            bfly4<INV>(s + i0 * SC + c, s + i1 * SC + c, s + i2 * SC + c, s + i3 * SC + c,
-                       __ldg(t + j), __ldg(t + h + j), __ldg(t + 2 * h + j));
-        }
-        t += 3 * h;
-        __syncthreads();
-    }
+__device__ void fft_cols(float2 *s, int n, int log2n, int SC, int logSC, const float2 *__restrict__ tri) {
+    auto la = [=](int c, int r) {
+        const int rr = RMAP ? brev_bits(r, log2n) : r;
+        return (rr << logSC) + c;
+    };
+    fft_cascade<INV, true>(s, n, log2n, SC, la, tri);
 }
 
 struct TileBox {
@@ -418,7 +479,7 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
     if (cn <= 0) return;
     const int P = min(pairsPerCta, (nrows - 2 * pair0 + 1) >> 1);
     const int lines = P * cn;
-    const int n = fc.n, log2n = fc.log2n;
+    const int n = fc.n, log2n = fc.log2n, ld = padded_len(n);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long rowBase = (long long)b.y0 * istride + (long long)b.x0 * step;
     for (int idx = tid; idx < lines * n; idx += nt) {
@@ -431,10 +492,11 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
             v.x = (float)pa[0];
             if (r + 1 < b.loadH) v.y = (float)pa[istride];
         }
-        smem[line * n + brev_bits(x, log2n)] = v;
+        smem[line * ld + padi(brev_bits(x, log2n))] = v;
     }
     __syncthreads();
-    fft_lines<false>(smem, n, log2n, lines, n, fc.triW);
+    auto la = [=](int line, int i) { return line * ld + padi(i); };
+    fft_cascade<false>(smem, n, log2n, lines, la, fc.triW);
     const int hw = fc.hw, mask = n - 1;
     const size_t chanStride = (size_t)fc.dftH * fc.hwp;
     float2 *tbase = spec + (size_t)(tile - fc.tileFirst) * cnS * chanStride;
@@ -442,7 +504,7 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
         const int line = idx / hw, kk = idx - line * hw;
         const int p = line / cn, k = chanFirst + line - p * cn;
         const int r = 2 * (pair0 + p);
-        const float2 zk = smem[line * n + kk], zn = smem[line * n + ((n - kk) & mask)];
+        const float2 zk = smem[line * ld + padi(kk)], zn = smem[line * ld + padi((n - kk) & mask)];
         float2 *cb = tbase + (size_t)k * chanStride;
         cb[(size_t)brev_bits(r, fc.log2H) * fc.hwp + kk] =
             make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
@@ -558,18 +620,32 @@ __global__ void k_cols(ColsArgs a) {
 
 // ------------------------------------------------------- inverse rows
 
-// float32(float64(v)) (impl.go:902-1009), two roundings as pinned.  Below
-// 2^53 the first rounding is exact, so one int64->float32 rounding gives
-// the same bits; above it the 53-bit rounding is done in integers.  No
-// FP64 instruction (GB300's FP64 rate is a small fraction of FP32).
-__device__ __forceinline__ float f32_via_f64(long long v) {
-    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-    if (a < (1ull << 53)) return __ll2float_rn(v);
-    const int sh = (64 - __clzll((long long)a)) - 53;
+// Round-to-nearest-even of a positive integer to `bits` significant bits.
+__device__ __forceinline__ unsigned long long rn_bits(unsigned long long a, int bits) {
+    const int bl = 64 - __clzll((long long)a);
+    if (bl <= bits) return a;
+    const int sh = bl - bits;
     unsigned long long q = a >> sh;
     const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
     if (rem > half || (rem == half && (q & 1ull))) q++;
-    const float f = __ull2float_rn(q << sh);
+    return q << sh;
+}
+
+// float32(float64(v)) (impl.go:902-1009): the conversion to float64 rounds
+// to 53 bits, the one to float32 to 24 bits, both to nearest even.  Done
+// in integer arithmetic; the final int->float conversion is exact.  (A
+// 64-bit integer conversion instruction would run on the FP64 pipe, which
+// GB300 provisions at a small fraction of FP32.)
+__device__ __forceinline__ float f32_via_f64(long long v) {
+    unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    if (a < (1ull << 24)) {
+        const float f = __uint2float_rn((unsigned int)a);
+        return v < 0 ? -f : f;
+    }
+    if (a >= (1ull << 53)) a = rn_bits(a, 53);
+    a = rn_bits(a, 24);
+    const int e = (64 - __clzll((long long)a)) - 24 > 0 ? (64 - __clzll((long long)a)) - 24 : 0;
+    const float f = __fmul_rn(__uint2float_rn((unsigned int)(a >> e)), __int_as_float((127 + e) << 23));
     return v < 0 ? -f : f;
 }
 
@@ -682,9 +758,9 @@ __global__ void k_inv_rows(InvArgs a) {
     const int pair0 = blockIdx.x * a.pairsPerCta;
     if (2 * pair0 >= bh) return;
     const int P = min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1);
-    const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp;
+    const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp, ld = padded_len(n);
     const int tid = threadIdx.x, nt = blockDim.x;
-    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * n);  // [P][2][n]
+    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * ld);  // [P][2][n]
     const int cn = Pm.cn;
     const size_t chanStride = (size_t)fc.dftH * hwp;
     const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
@@ -704,13 +780,14 @@ __global__ void k_inv_rows(InvArgs a) {
                 const float2 u = sa[mm], v = sb[mm];
                 z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
             }
-            smem[p * n + brev_bits(kk, log2n)] = z;
+            smem[p * ld + padi(brev_bits(kk, log2n))] = z;
         }
         __syncthreads();
-        fft_lines<true>(smem, n, log2n, P, n, fc.triW);
+        auto la = [=](int line, int i) { return line * ld + padi(i); };
+        fft_cascade<true>(smem, n, log2n, P, la, fc.triW);
         for (int idx = tid; idx < P * bw; idx += nt) {
             const int p = idx / bw, x = idx - p * bw;
-            const float2 z = smem[p * n + x];
+            const float2 z = smem[p * ld + padi(x)];
             float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
             if (k == 0) {
                 *a0 = z.x;
@@ -737,38 +814,53 @@ struct NormArgs {
     long long istride;
     int step;
     MemberSet ms;
-    int CW, B, ncx;
+    int CW, BV, G, ncx, nby;
     int cnCap;            // channel capacity of the column arrays
-    int ncCap;            // column capacity of the column arrays
+    int cap;              // column capacity (>= CW + tw - 1 of every member)
     Partial *partials;
-    unsigned char *gscratch;  // per-CTA column arrays when they exceed shared memory
-    size_t gscratchPerCta;
+    int *counters;        // per member slot: CTAs finished (zeroed by the caller)
+    cvm_result *out;
 };
 
-// Window statistics by sliding column sums, the reference's own scheme
+__device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
+    cvm_result r;
+    r.min_v = e.minV;
+    r.max_v = e.maxV;
+    r.min_x = (int32_t)(e.minI % rw);
+    r.min_y = (int32_t)(e.minI / rw);
+    r.max_x = (int32_t)(e.maxI % rw);
+    r.max_y = (int32_t)(e.maxI / rw);
+    *out = r;
+}
+
+// Window statistics by the reference's own sliding scheme
 // (colBuildGo/colSlideGo, impl.go:708-805, and the per-row window sums of
-// impl.go:884-893) run for a CW x B block of results per CTA: column sums
-// over the th rows under the block's first row, then per row an exclusive
-// prefix over the columns gives every window sum as a difference, the
-// normOne tail scores the raw correlation, and the columns slide one row
-// down.  All statistics are exact integers (u32 sums are modular: every
-// window sum is < 2^32), so any schedule yields the reference's values.
-__global__ void k_norm(NormArgs a) {
+// impl.go:884-893), for a CW x BV block of results per CTA:
+//   1. column sums over the th rows under the block (colBuildGo);
+//   2. per group of G result rows, each thread slides its columns down
+//      one row at a time (colSlideGo) and stores the per-row column sums;
+//   3. one warp per row turns that row into an exclusive prefix over the
+//      columns, so every window sum is one difference, and scores the row
+//      with normOne (impl.go:825-849) against the raw correlation.
+// All statistics are exact integers (u32 sums are modular: every window sum
+// is < 2^32), so the schedule cannot change a value.  The CTA that
+// finishes a member last merges the member's partial extrema in raster
+// order (impl.go:1104-1112) and writes its result.
+__global__ void __launch_bounds__(256) k_norm(NormArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ Ext shExt[kThreads / 32];
-    __shared__ unsigned int wsS[kThreads / 32][4];
-    __shared__ unsigned long long wsQ[kThreads / 32];
+    __shared__ int isLast;
     const int slot = blockIdx.z;
     const DevMember &m = member_of(a.ms, slot);
     const DevParams &Pm = a.ms.params[m.pIdx];
-    const int X0 = blockIdx.x * a.CW, Y0 = blockIdx.y * a.B;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int X0 = blockIdx.x * a.CW, Y0 = blockIdx.y * a.BV;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     Ext e;
     ext_init(e);
-    float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
+    const float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
     float *map = a.ms.map;
     if (X0 < m.rw && Y0 < m.rh) {
-        const int CWv = min(a.CW, m.rw - X0), Bv = min(a.B, m.rh - Y0);
+        const int CWv = min(a.CW, m.rw - X0), Bv = min(a.BV, m.rh - Y0);
         if (Pm.flat) {
             for (int idx = tid; idx < CWv * Bv; idx += nt) {
                 const int yy = idx / CWv, x = idx - yy * CWv;
@@ -779,27 +871,28 @@ __global__ void k_norm(NormArgs a) {
         } else {
             const int cn = Pm.cn, tw = m.tw, th = m.th, step = a.step;
             const int NC = CWv + tw - 1;
-            const int cap = a.ncCap;
-            unsigned char *base = a.gscratch
-                                      ? a.gscratch + (size_t)(blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)) *
-                                                         a.gscratchPerCta
-                                      : smraw;
-            unsigned long long *colQ = reinterpret_cast<unsigned long long *>(base);
-            unsigned long long *preQ = colQ + cap;
-            unsigned int *colS = reinterpret_cast<unsigned int *>(preQ + cap + 1);
-            unsigned int *preS = colS + (size_t)a.cnCap * cap;
-            const int capP = cap + 1;
+            const int cap = a.cap, cnCap = a.cnCap, G = a.G;
+            const int rcap = cap + 1;
+            // shared layout: colQ[cap] u64 | rowQ[G][rcap] u64 | colS[cnCap][cap] u32 | rowS[cnCap][G][rcap] u32
+            unsigned long long *colQ = reinterpret_cast<unsigned long long *>(smraw);
+            unsigned long long *rowQ = colQ + cap;
+            unsigned int *colS = reinterpret_cast<unsigned int *>(rowQ + (size_t)G * rcap);
+            unsigned int *rowS = colS + (size_t)cnCap * cap;
             const long long area = (long long)tw * th;
-            // Column sums over rows Y0 .. Y0+th-1 (colBuildGo).
+            const unsigned int t0 = (unsigned int)Pm.tsum[0], t1 = (unsigned int)Pm.tsum[1];
+            const unsigned int t2 = (unsigned int)Pm.tsum[2], t3 = (unsigned int)Pm.tsum[3];
+            // 1. column sums over rows Y0 .. Y0+th-1
             for (int c = tid; c < NC; c += nt) {
                 const uint8_t *p = a.img + (long long)Y0 * a.istride + (long long)(X0 + c) * step;
                 unsigned int sk[4] = {0u, 0u, 0u, 0u};
                 unsigned long long q = 0;
-                for (int dy = 0; dy < th; dy++, p += a.istride) {
+#pragma unroll 4
+                for (int dy = 0; dy < th; dy++) {
+                    const uint8_t *pr = p + (long long)dy * a.istride;
 #pragma unroll
                     for (int k = 0; k < 4; k++)
                         if (k < cn) {
-                            const unsigned v = p[k];
+                            const unsigned v = pr[k];
                             sk[k] += v;
                             q += v * v;
                         }
@@ -810,101 +903,123 @@ __global__ void k_norm(NormArgs a) {
                 colQ[c] = q;
             }
             __syncthreads();
-            const int seg = (NC + nt - 1) / nt;
-            const int c0 = tid * seg, c1 = min(NC, c0 + seg);
-            const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-            for (int y = Y0; y < Y0 + Bv; y++) {
-                // Exclusive prefix of the column sums: segment totals, a
-                // block scan of the totals, then the segment's running sums.
-                unsigned int ts[4] = {0u, 0u, 0u, 0u};
-                unsigned long long tq = 0;
-                for (int c = c0; c < c1; c++) {
+            // lane chunks of the per-row scans; odd so lanes hit distinct banks
+            const int chunk = ((NC + 1 + 31) / 32) | 1;
+            for (int yg = Y0; yg < Y0 + Bv; yg += G) {
+                const int Gv = min(G, Y0 + Bv - yg);
+                // 2. per-row column sums of rows yg .. yg+Gv-1, sliding down
+                for (int c = tid; c < NC; c += nt) {
+                    unsigned int sk[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        if (k < cn) ts[k] += colS[(size_t)k * cap + c];
-                    tq += colQ[c];
-                }
-                unsigned int is[4];
-                unsigned long long iq = tq;
-#pragma unroll
-                for (int k = 0; k < 4; k++) is[k] = ts[k];
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const unsigned int u = __shfl_up_sync(0xffffffffu, is[k], o);
-                        if (lane >= o) is[k] += u;
-                    }
-                    const unsigned long long u = __shfl_up_sync(0xffffffffu, iq, o);
-                    if (lane >= o) iq += u;
-                }
-                if (lane == 31) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) wsS[warp][k] = is[k];
-                    wsQ[warp] = iq;
-                }
-                __syncthreads();
-                unsigned int rs[4];
-                unsigned long long rq = iq - tq;
-#pragma unroll
-                for (int k = 0; k < 4; k++) rs[k] = is[k] - ts[k];
-                for (int w = 0; w < warp; w++) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++) rs[k] += wsS[w][k];
-                    rq += wsQ[w];
-                }
-                (void)nw;
-                for (int c = c0; c < c1; c++) {
-                    if (c == 0) {
+                    for (int k = 0; k < 4; k++) sk[k] = k < cn ? colS[(size_t)k * cap + c] : 0u;
+                    unsigned long long q = colQ[c];
+                    const uint8_t *base = a.img + (long long)(X0 + c) * step;
+                    for (int g = 0; g < Gv; g++) {
 #pragma unroll
                         for (int k = 0; k < 4; k++)
-                            if (k < cn) preS[(size_t)k * capP] = 0u;
-                        preQ[0] = 0ull;
+                            if (k < cn) rowS[((size_t)k * G + g) * rcap + c] = sk[k];
+                        rowQ[(size_t)g * rcap + c] = q;
+                        const int y = yg + g;
+                        if (y + 1 < Y0 + Bv) {
+                            const uint8_t *pa = base + (long long)(y + th) * a.istride;
+                            const uint8_t *ps = base + (long long)y * a.istride;
+                            long long dq = 0;
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+                                if (k < cn) {
+                                    const int va = pa[k], vb = ps[k];
+                                    sk[k] += (unsigned int)(va - vb);
+                                    dq += va * va - vb * vb;
+                                }
+                            q += (unsigned long long)dq;
+                        }
                     }
 #pragma unroll
                     for (int k = 0; k < 4; k++)
-                        if (k < cn) {
-                            rs[k] += colS[(size_t)k * cap + c];
-                            preS[(size_t)k * capP + c + 1] = rs[k];
-                        }
-                    rq += colQ[c];
-                    preQ[c + 1] = rq;
+                        if (k < cn) colS[(size_t)k * cap + c] = sk[k];
+                    colQ[c] = q;
                 }
                 __syncthreads();
-                // Scores of row y (the spill + normOne of impl.go:895-1021).
-                const float *crow = corr + (size_t)y * m.rw + X0;
-                for (int x = tid; x < CWv; x += nt) {
-                    long long cross = 0, sq = 0, s0 = 0;
+                // 3. one warp per row: exclusive prefix, then the row's scores
+                for (int g = warp; g < Gv; g += nw) {
+                    unsigned int *rs[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        if (k < cn) {
-                            const unsigned int sk = preS[(size_t)k * capP + x + tw] - preS[(size_t)k * capP + x];
-                            if (k == 0) s0 = sk;
-                            cross += (long long)((unsigned long long)sk * (unsigned long long)(unsigned int)Pm.tsum[k]);
-                            sq += (long long)((unsigned long long)sk * (unsigned long long)sk);
+                    for (int k = 0; k < 4; k++) rs[k] = rowS + ((size_t)k * G + g) * rcap;
+                    unsigned long long *rq = rowQ + (size_t)g * rcap;
+                    const int c0 = lane * chunk, c1 = min(NC, c0 + chunk);
+                    unsigned int ls[4] = {0u, 0u, 0u, 0u};
+                    unsigned long long lq = 0;
+                    for (int c = c0; c < c1; c++) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (k < cn) ls[k] += rs[k][c];
+                        lq += rq[c];
+                    }
+                    unsigned int xs[4];
+                    unsigned long long xq = lq;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) xs[k] = ls[k];
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const unsigned int u = __shfl_up_sync(0xffffffffu, xs[k], o);
+                            if (lane >= o && k < cn) xs[k] += u;
                         }
-                    const long long s2 = (long long)(preQ[x + tw] - preQ[x]);
-                    const long long lane0 = cn == 1 ? s0 : cross;
-                    const float score = norm_one(crow[x], f32_via_f64(lane0), f32_via_f64(area * s2 - sq),
-                                                 f32_via_f64(s2), Pm.numScale, Pm.varScale, Pm.templNorm);
-                    const long long li = (long long)y * m.rw + X0 + x;
-                    if (map) map[li] = score;
-                    ext_add(e, score, li);
-                }
-                // Slide the columns one row down (colSlideGo).
-                if (y + 1 < Y0 + Bv) {
-                    for (int c = tid; c < NC; c += nt) {
-                        const uint8_t *pa = a.img + (long long)(y + th) * a.istride + (long long)(X0 + c) * step;
-                        const uint8_t *ps = a.img + (long long)y * a.istride + (long long)(X0 + c) * step;
-                        long long dq = 0;
+                        const unsigned long long u = __shfl_up_sync(0xffffffffu, xq, o);
+                        if (lane >= o) xq += u;
+                    }
+                    // exclusive offsets of this lane's chunk
+#pragma unroll
+                    for (int k = 0; k < 4; k++) xs[k] -= ls[k];
+                    xq -= lq;
+                    for (int c = c0; c < c1; c++) {
 #pragma unroll
                         for (int k = 0; k < 4; k++)
                             if (k < cn) {
-                                const int va = pa[k], vb = ps[k];
-                                colS[(size_t)k * cap + c] += (unsigned int)(va - vb);
-                                dq += va * va - vb * vb;
+                                const unsigned int v = rs[k][c];
+                                rs[k][c] = xs[k];
+                                xs[k] += v;
                             }
-                        colQ[c] += (unsigned long long)dq;
+                        const unsigned long long v = rq[c];
+                        rq[c] = xq;
+                        xq += v;
+                    }
+                    if (c0 < NC && c1 == NC) {  // the lane ending the row stores prefix[NC]
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (k < cn) rs[k][NC] = xs[k];
+                        rq[NC] = xq;
+                    }
+                    __syncwarp();
+                    const int y = yg + g;
+                    const float *crow = corr + (size_t)y * m.rw + X0;
+                    for (int x = lane; x < CWv; x += 32) {
+                        const unsigned int s0 = rs[0][x + tw] - rs[0][x];
+                        unsigned long long cross = (unsigned long long)s0 * t0;
+                        unsigned long long sq = (unsigned long long)s0 * s0;
+                        if (cn > 1) {
+                            const unsigned int s1 = rs[1][x + tw] - rs[1][x];
+                            cross += (unsigned long long)s1 * t1;
+                            sq += (unsigned long long)s1 * s1;
+                        }
+                        if (cn > 2) {
+                            const unsigned int s2c = rs[2][x + tw] - rs[2][x];
+                            cross += (unsigned long long)s2c * t2;
+                            sq += (unsigned long long)s2c * s2c;
+                        }
+                        if (cn > 3) {
+                            const unsigned int s3 = rs[3][x + tw] - rs[3][x];
+                            cross += (unsigned long long)s3 * t3;
+                            sq += (unsigned long long)s3 * s3;
+                        }
+                        const long long s2 = (long long)(rq[x + tw] - rq[x]);
+                        const long long lane0 = cn == 1 ? (long long)s0 : (long long)cross;
+                        const float score = norm_one(crow[x], f32_via_f64(lane0), f32_via_f64(area * s2 - (long long)sq),
+                                                     f32_via_f64(s2), Pm.numScale, Pm.varScale, Pm.templNorm);
+                        const long long li = (long long)y * m.rw + X0 + x;
+                        if (map) map[li] = score;
+                        ext_add(e, score, li);
                     }
                 }
                 __syncthreads();
@@ -913,40 +1028,33 @@ __global__ void k_norm(NormArgs a) {
     }
     __syncthreads();
     ext_block_reduce(e, shExt);
+    const int nparts = a.ncx * a.nby;
     if (tid == 0) {
         Partial &o = a.partials[m.partBase + blockIdx.y * a.ncx + blockIdx.x];
         o.minV = e.minV;
         o.maxV = e.maxV;
         o.minI = e.minI;
         o.maxI = e.maxI;
+        __threadfence();
+        isLast = atomicAdd(&a.counters[m.pIdx], 1) == nparts - 1;
     }
-}
-
-__global__ void k_extrema_final(MemberSet ms, const Partial *partials, int nparts, cvm_result *out) {
-    __shared__ Ext shExt[kThreads / 32];
-    const DevMember &m = member_of(ms, blockIdx.x);
-    Ext e;
+    __syncthreads();
+    if (!isLast) return;
+    // The member's last CTA: merge all partials in raster-order semantics.
+    __threadfence();
     ext_init(e);
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
-        const Partial &p = partials[m.partBase + i];
+    for (int i = tid; i < nparts; i += nt) {
+        const volatile Partial *p = a.partials + m.partBase + i;
         Ext o;
-        o.minV = p.minV;
-        o.maxV = p.maxV;
-        o.minI = p.minI;
-        o.maxI = p.maxI;
+        o.minV = p->minV;
+        o.maxV = p->maxV;
+        o.minI = p->minI;
+        o.maxI = p->maxI;
         ext_merge(e, o);
     }
+    __syncthreads();
     ext_block_reduce(e, shExt);
-    if (threadIdx.x == 0) {
-        cvm_result r;
-        r.min_v = e.minV;
-        r.max_v = e.maxV;
-        r.min_x = (int32_t)(e.minI % m.rw);
-        r.min_y = (int32_t)(e.minI / m.rw);
-        r.max_x = (int32_t)(e.maxI % m.rw);
-        r.max_y = (int32_t)(e.maxI / m.rw);
-        out[m.outIdx] = r;
-    }
+    if (tid == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
 }
 
 // Small host values to device memory through kernel arguments.
@@ -1059,7 +1167,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     if (maxRows > fc.dftH) maxRows = fc.dftH;
     const int pairs = (maxRows + 1) / 2;
     dim3 grid((pairs + P - 1) / P, fc.ntiles);
-    const size_t smem = (size_t)P * group * fc.n * sizeof(float2);
+    const size_t smem = (size_t)P * group * padded_len(fc.n) * sizeof(float2);
     set_smem(k_fwd_rows, smem);
     ProfScope ps("k_fwd_rows", st);
     for (int c0 = 0; c0 < chanCount; c0 += group) {
@@ -1121,7 +1229,7 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     const int ctas = inv_rows_ctas_per_tile(fc, &P);
     a.pairsPerCta = P;
     dim3 grid(ctas, fc.ntiles, nmembers);
-    const size_t smem = (size_t)P * fc.n * (sizeof(float2) + 2 * sizeof(float));
+    const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + 2 * fc.n * sizeof(float));
     set_smem(k_inv_rows, smem);
     ProfScope ps("k_inv_rows", st);
     k_inv_rows<<<grid, kThreads, smem, st>>>(a);
@@ -1129,56 +1237,50 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     return cudaGetLastError();
 }
 
-static size_t norm_arrays_bytes(int cap, int cnCap) {
-    return 8 * (2 * (size_t)cap + 1) + 4 * (size_t)cnCap * cap + 4 * (size_t)cnCap * (cap + 1);
+static size_t norm_smem_bytes(int cap, int cnCap, int G) {
+    return (size_t)cap * (8 + 4 * cnCap) + (size_t)G * (cap + 1) * (8 + 4 * cnCap);
 }
 
 NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap) {
     NormGrid g;
     g.CW = kThreads;
     g.B = 32;
-    g.ncx = (rwMax + g.CW - 1) / g.CW;
-    g.nby = (rhMax + g.B - 1) / g.B;
     g.cnCap = cnCap;
     g.ncCap = g.CW + twMax - 1;
-    const size_t bytes = norm_arrays_bytes(g.ncCap, cnCap);
-    if (bytes <= 200 * 1024) {
-        g.smemBytes = bytes;
-        g.scratchPerCta = 0;
-    } else {
-        g.smemBytes = 0;
-        g.scratchPerCta = (bytes + 255) / 256 * 256;
+    g.G = 8;
+    while (g.G > 1 && norm_smem_bytes(g.ncCap, cnCap, g.G) > 96 * 1024) g.G >>= 1;
+    if (norm_smem_bytes(g.ncCap, cnCap, g.G) > 200 * 1024) {
+        g.CW = 128;
+        g.ncCap = g.CW + twMax - 1;
     }
+    g.ncx = (rwMax + g.CW - 1) / g.CW;
+    g.nby = (rhMax + g.B - 1) / g.B;
+    g.smemBytes = norm_smem_bytes(g.ncCap, cnCap, g.G);
+    g.scratchPerCta = 0;
     return g;
 }
 
 cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
-                        const NormGrid &ng, Partial *partials, unsigned char *gscratch, cudaStream_t st) {
+                        const NormGrid &ng, Partial *partials, int *counters, cvm_result *out, cudaStream_t st) {
     NormArgs a;
     a.img = img;
     a.istride = istride;
     a.step = step;
     a.ms = ms;
     a.CW = ng.CW;
-    a.B = ng.B;
+    a.BV = ng.B;
+    a.G = ng.G;
     a.ncx = ng.ncx;
+    a.nby = ng.nby;
     a.cnCap = ng.cnCap;
-    a.ncCap = ng.ncCap;
+    a.cap = ng.ncCap;
     a.partials = partials;
-    a.gscratch = ng.scratchPerCta ? gscratch : nullptr;
-    a.gscratchPerCta = ng.scratchPerCta;
+    a.counters = counters;
+    a.out = out;
     dim3 grid(ng.ncx, ng.nby, nmembers);
     set_smem(k_norm, ng.smemBytes);
     ProfScope ps("k_norm", st);
     k_norm<<<grid, kThreads, ng.smemBytes, st>>>(a);
-    count_launches(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_extrema_final(const MemberSet &ms, int nmembers, const Partial *partials,
-                                 int nparts, cvm_result *out, cudaStream_t st) {
-    ProfScope ps("k_extrema_final", st);
-    k_extrema_final<<<nmembers, kThreads, 0, st>>>(ms, partials, nparts, out);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -418,3 +418,37 @@ def test_config_c3_map_bit_exact():
     assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
     assert (t[4], t[5]) == (x, y)
     assert np.all(np.abs(m) <= 1.0)
+
+
+# ---------------------------------------------------- rare arithmetic paths
+
+
+def test_lanes_above_2_53_gray():
+    """area*s2 exceeds 2^53: float32(float64(v)) rounds twice; the GPU's
+    integer emulation of the first rounding must give the same bits."""
+    img = image(601, 1100, 1100, 1).copy()
+    img[:] = 160 + (img % 96)
+    tpl = img[37:1037, 41:1041].copy()
+    t, m = cvm.match_u8(img, tpl, 1)
+    to, mo = oracle.match_u8(img, tpl, 1, threads=16)
+    assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
+
+
+def test_lanes_above_2_53_colour():
+    img = image(602, 520, 720, 4).copy()
+    img[:] = 200 + (img % 56)
+    tpl = img[10:510, 12:712].copy()
+    t, m = cvm.match_u8(img, tpl, 4)
+    to, mo = oracle.match_u8(img, tpl, 4, threads=16)
+    assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
+
+
+def test_very_wide_colour_template_global_column_arrays():
+    """A 4100-px-wide RGBA template: the normalisation's column arrays no
+    longer fit shared memory and live in global scratch."""
+    img = image(603, 60, 4200, 4).copy()
+    tpl = img[11:51, 50:4150].copy()
+    t, m = cvm.match_u8(img, tpl, 4)
+    to, mo = oracle.match_u8(img, tpl, 4, threads=16)
+    assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
+    assert (t[4], t[5]) == (50, 11)
