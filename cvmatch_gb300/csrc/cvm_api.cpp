@@ -115,6 +115,24 @@ cudaStream_t thread_stream() {
     return s;
 }
 
+// Per-thread side stream and fork/join events: the template side of a call
+// (statistics, alpha scans, template spectrum) runs beside the frame's
+// forward transforms, joined before the first step that needs both.
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+SideStream &side_stream() {
+    thread_local SideStream s;
+    if (!s.st) {
+        cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
+    }
+    return s;
+}
+
 const float2 *dev_tri(int n) {
     DeviceState &d = dev();
     std::lock_guard<std::mutex> lk(d.triMu);
@@ -312,11 +330,6 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         CVM_CUDA(cudaMemcpyAsync(P, J.cachedP, sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
     else
         CVM_CUDA(cudaMemsetAsync(P, 0, sizeof(DevParams), st));
-    CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
-                         J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
-                         J.cnFixed, F, st));
-    if (!J.cachedP)
-        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], st));
     MemberSet ms;
     memset(&ms, 0, sizeof ms);
     ms.solo.tspec[0] = ts[0];
@@ -332,15 +345,33 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.map = J.map;
     ms.corr = corr;
     ms.corrStride = 0;
+    // Fork: statistics, alpha scans and the template spectrum on the side
+    // stream; the frame channels whose presence does not depend on the
+    // alpha decision (all of them for a fixed cn, RGB for colour) on st.
+    SideStream &ss = side_stream();
+    CVM_CUDA(cudaEventRecord(ss.fork, st));
+    CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
+    CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
+                         J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
+                         J.cnFixed, F, ss.st));
+    if (!J.cachedP)
+        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st));
+    CVM_CUDA(cudaEventRecord(ss.join, ss.st));
+    const int cnSure = J.mode == 1 ? 3 : cnS;
+    for (int c = 0; c < G->nclass; c++)
+        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnSure, nullptr, G->g, G->fc[c], spec[c], cnS, st));
+    CVM_CUDA(cudaStreamWaitEvent(st, ss.join, 0));
     for (int c = 0; c < G->nclass; c++) {
         const FftClass &f = G->fc[c];
-        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, f, spec[c], cnS, st));
+        if (cnS > cnSure)  // the alpha channel, present only when the device chose cn = 4
+            CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, f, spec[c], cnS, st, cnSure));
         ms.scratch[c] = spec[c];
         ms.scratchStride[c] = 0;
         CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
         CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, st));
     }
-    CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, parts, &F->normDone, J.out, st));
+    for (int cnL = J.mode == 1 ? 3 : J.cnFixed; cnL <= (J.mode == 1 ? 4 : J.cnFixed); cnL++)
+        CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, cnL, parts, &F->normDone, J.out, st));
     return CVM_OK;
 }
 
@@ -747,7 +778,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
                 CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, st));
             }
-            CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, parts, counters, dOut, st));
+            for (int cnL = f->step == 4 ? 3 : 1; cnL <= (f->step == 4 ? 4 : 1); cnL++)
+                CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, cnL, parts, counters, dOut, st));
         }
         (void)nparts;
     }

@@ -123,9 +123,10 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
                         int setInit, int initMode, int initCnFixed, DevFrame *F, cudaStream_t st);
 // Forward row pass of every tile of `fc` (or of a template: geometry with
 // one 1x1 block whose loads are the template's tw x th).
+// Channels [chanFirst, min(chanCount, *cnDev)) are transformed.
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st);
+                            int cnS, cudaStream_t st, int chanFirst = 0);
 // Column pass.  mode 0: forward only, natural output (template spectra with
 // `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
 // conj-multiply + inverse, in place on the members' scratch (solo match);
@@ -147,8 +148,12 @@ struct NormGrid {
     size_t scratchPerCta;   // unused (kept 0): every shape fits shared memory
 };
 NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap);
+// cnLaunch: the members' effective channel count (kernels are specialised
+// on it); a member whose device-side cn differs is skipped by the launch
+// and must be covered by the launch for its own cn.
 cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
-                        const NormGrid &ng, Partial *partials, int *counters, cvm_result *out, cudaStream_t st);
+                        const NormGrid &ng, int cnLaunch, Partial *partials, int *counters, cvm_result *out,
+                        cudaStream_t st);
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).
 cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st);

@@ -631,32 +631,44 @@ __device__ __forceinline__ unsigned long long rn_bits(unsigned long long a, int 
     return q << sh;
 }
 
+// Correctly rounded float32 of an unsigned 64-bit integer in integer
+// arithmetic (a 64-bit integer conversion instruction would run on the FP64
+// pipe, which GB300 provisions at a small fraction of FP32): the top 24
+// significant bits, rounded to nearest even on the dropped bits, then the
+// exponent added exactly.
+__device__ __forceinline__ float u64_to_f32_rn(unsigned long long a) {
+    if ((a >> 32) == 0) return __uint2float_rn((unsigned int)a);
+    const int sh = 40 - __clzll((long long)a);  // bit length - 24, in 9..40
+    const unsigned int q = (unsigned int)(a >> sh);
+    const unsigned long long rem = a << (64 - sh);  // dropped bits, left-aligned
+    const unsigned int up = (rem > 0x8000000000000000ull) || (rem == 0x8000000000000000ull && (q & 1u));
+    const float f = __uint2float_rn(q + up);  // <= 2^24: exact
+    return __int_as_float(__float_as_int(f) + (sh << 23));
+}
+
 // float32(float64(v)) (impl.go:902-1009): the conversion to float64 rounds
-// to 53 bits, the one to float32 to 24 bits, both to nearest even.  Done
-// in integer arithmetic; the final int->float conversion is exact.  (A
-// 64-bit integer conversion instruction would run on the FP64 pipe, which
-// GB300 provisions at a small fraction of FP32.)
+// to 53 bits, the one to float32 to 24 bits, both to nearest even.  Below
+// 2^53 the first rounding is exact, so a single rounding gives the bits.
 __device__ __forceinline__ float f32_via_f64(long long v) {
     unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-    if (a < (1ull << 24)) {
-        const float f = __uint2float_rn((unsigned int)a);
-        return v < 0 ? -f : f;
-    }
     if (a >= (1ull << 53)) a = rn_bits(a, 53);
-    a = rn_bits(a, 24);
-    const int e = (64 - __clzll((long long)a)) - 24 > 0 ? (64 - __clzll((long long)a)) - 24 : 0;
-    const float f = __fmul_rn(__uint2float_rn((unsigned int)(a >> e)), __int_as_float((127 + e) << 23));
+    const float f = u64_to_f32_rn(a);
     return v < 0 ? -f : f;
 }
 
-// normOne (impl.go:825-849).
-__device__ __forceinline__ float norm_one(float num, float lane0, float idiff, float s2,
+// normOne (impl.go:825-849).  s2 is the exact integer: lim = min(eps *
+// float32(s2), 0.5) is 0.5 for every s2 >= 2^19 (eps * 2^19 = 0.625), so
+// the conversion is only needed below 2^24, where it is exact.
+__device__ __forceinline__ float norm_one(float num, float lane0, float idiff, unsigned long long s2i,
                                           float numScale, float varScale, float templNorm) {
     const float eps = 1.1920928955078125e-06f;  // 10 * 2^-23, exact in float32
     num = __fsub_rn(num, __fmul_rn(lane0, numScale));
     const float diff2 = __fmul_rn(idiff, varScale);
-    float lim = __fmul_rn(eps, s2);
-    if (lim > 0.5f) lim = 0.5f;
+    float lim = 0.5f;
+    if (s2i < (1ull << 24)) {
+        lim = __fmul_rn(eps, __uint2float_rn((unsigned int)s2i));
+        if (lim > 0.5f) lim = 0.5f;
+    }
     float den = 0.f;
     if (diff2 > lim) den = __fmul_rn(__fsqrt_rn(diff2), templNorm);
     const float an = fabsf(num);
@@ -846,6 +858,7 @@ __device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
 // is < 2^32), so the schedule cannot change a value.  The CTA that
 // finishes a member last merges the member's partial extrema in raster
 // order (impl.go:1104-1112) and writes its result.
+template <int CN>
 __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ Ext shExt[kThreads / 32];
@@ -853,6 +866,7 @@ __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
     const int slot = blockIdx.z;
     const DevMember &m = member_of(a.ms, slot);
     const DevParams &Pm = a.ms.params[m.pIdx];
+    if (Pm.cn != CN) return;  // this member belongs to the launch specialised on its cn
     const int X0 = blockIdx.x * a.CW, Y0 = blockIdx.y * a.BV;
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     Ext e;
@@ -869,7 +883,8 @@ __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
                 ext_add(e, 1.f, li);
             }
         } else {
-            const int cn = Pm.cn, tw = m.tw, th = m.th, step = a.step;
+            constexpr int cn = CN;
+            const int tw = m.tw, th = m.th, step = a.step;
             const int NC = CWv + tw - 1;
             const int cap = a.cap, cnCap = a.cnCap, G = a.G;
             const int rcap = cap + 1;
@@ -1013,10 +1028,10 @@ __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
                             cross += (unsigned long long)s3 * t3;
                             sq += (unsigned long long)s3 * s3;
                         }
-                        const long long s2 = (long long)(rq[x + tw] - rq[x]);
-                        const long long lane0 = cn == 1 ? (long long)s0 : (long long)cross;
-                        const float score = norm_one(crow[x], f32_via_f64(lane0), f32_via_f64(area * s2 - (long long)sq),
-                                                     f32_via_f64(s2), Pm.numScale, Pm.varScale, Pm.templNorm);
+                        const unsigned long long s2 = rq[x + tw] - rq[x];
+                        const float l0 = cn == 1 ? __uint2float_rn(s0) : f32_via_f64((long long)cross);
+                        const float id = f32_via_f64((long long)((unsigned long long)area * s2 - sq));
+                        const float score = norm_one(crow[x], l0, id, s2, Pm.numScale, Pm.varScale, Pm.templNorm);
                         const long long li = (long long)y * m.rw + X0 + x;
                         if (map) map[li] = score;
                         ext_add(e, score, li);
@@ -1154,7 +1169,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st) {
+                            int cnS, cudaStream_t st, int chanFirst) {
     // Channels per launch so that one row pair of the group fits 128 KB of
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
@@ -1170,7 +1185,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     const size_t smem = (size_t)P * group * padded_len(fc.n) * sizeof(float2);
     set_smem(k_fwd_rows, smem);
     ProfScope ps("k_fwd_rows", st);
-    for (int c0 = 0; c0 < chanCount; c0 += group) {
+    for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
         k_fwd_rows<<<grid, kThreads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
                                                   spec, cnS, P);
         count_launches(1);
@@ -1261,7 +1276,8 @@ NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap) {
 }
 
 cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
-                        const NormGrid &ng, Partial *partials, int *counters, cvm_result *out, cudaStream_t st) {
+                        const NormGrid &ng, int cnLaunch, Partial *partials, int *counters, cvm_result *out,
+                        cudaStream_t st) {
     NormArgs a;
     a.img = img;
     a.istride = istride;
@@ -1278,9 +1294,25 @@ cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const M
     a.counters = counters;
     a.out = out;
     dim3 grid(ng.ncx, ng.nby, nmembers);
-    set_smem(k_norm, ng.smemBytes);
     ProfScope ps("k_norm", st);
-    k_norm<<<grid, kThreads, ng.smemBytes, st>>>(a);
+    switch (cnLaunch) {
+        case 1:
+            set_smem(k_norm<1>, ng.smemBytes);
+            k_norm<1><<<grid, kThreads, ng.smemBytes, st>>>(a);
+            break;
+        case 2:
+            set_smem(k_norm<2>, ng.smemBytes);
+            k_norm<2><<<grid, kThreads, ng.smemBytes, st>>>(a);
+            break;
+        case 3:
+            set_smem(k_norm<3>, ng.smemBytes);
+            k_norm<3><<<grid, kThreads, ng.smemBytes, st>>>(a);
+            break;
+        default:
+            set_smem(k_norm<4>, ng.smemBytes);
+            k_norm<4><<<grid, kThreads, ng.smemBytes, st>>>(a);
+            break;
+    }
     count_launches(1);
     return cudaGetLastError();
 }
