@@ -25,9 +25,10 @@ namespace cvm {
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
-namespace {
+static thread_local std::string t_err;
+void set_error_message(const char *msg) { t_err = msg; }
 
-thread_local std::string t_err;
+namespace {
 
 int fail(int code, const char *fmt, ...) {
     char buf[512];

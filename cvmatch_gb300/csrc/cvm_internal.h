@@ -163,6 +163,9 @@ cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int d
 // kernel-launch counter (exported by cvm_launch_count)
 void count_launches(unsigned n);
 
+// sets the calling thread's message returned by cvm_last_error
+void set_error_message(const char *msg);
+
 // per-kernel event timing (exported by cvm_profile_enable/cvm_profile_read)
 void profile_enable(int on);
 int profile_read(int i, char *name, size_t len, double *ms, unsigned long long *count);

@@ -103,6 +103,23 @@ int cvm_match_device(const uint8_t *d_parent, int64_t pstride, int pw, int ph,
                      const uint8_t *d_sub, int64_t sstride, int sw, int sh,
                      float *d_map, cvm_result *d_out, void *stream);
 
+/* matchU8 on device buffers without allocating device memory.  This entry
+ * point has no counterpart in the reference.  It is for callers that must
+ * not allocate: code running inside a memory budget another allocator owns
+ * (a framework's caching pool, a runtime that reserves the device at
+ * start-up) or loops where a driver allocation's latency is unacceptable.
+ * The workspace is one fixed 64 MiB device array inside the library, held
+ * by every GPU that loads it until the process exits; a match whose
+ * workspace does not fit (roughly: colour frames above ~2 Mpx, gray frames
+ * above ~6 Mpx) returns CVM_ERR_UNSUPPORTED.  The caller passes inputs and
+ * outputs as for cvm_match_u8_device.  The first call on a device sets the
+ * array up (synchronous copies of the twiddle tables); make that first call
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race, so serialise them. */
+int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride, int iw, int ih,
+                                const uint8_t *d_tpl, int64_t tstride, int tw, int th, int cn, int step,
+                                float *d_map, cvm_result *d_out, void *stream);
+
 /* ----------------------------------------------------- image primitives */
 
 /* rgbToGray (cvmatch.go:222-240): out is w*h packed gray bytes. */
