@@ -121,7 +121,7 @@ cudaStream_t thread_stream() {
 // forward transforms, joined before the first step that needs both.
 struct SideStream {
     cudaStream_t st = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr;
 };
 
 SideStream &side_stream() {
@@ -130,6 +130,7 @@ SideStream &side_stream() {
         cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
         cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
     }
     return s;
 }
@@ -299,11 +300,17 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         G = &local;
     }
     const int cnS = J.mode == 1 ? 4 : J.cnFixed;
-    const NormGrid ng = norm_grid(rw, rh, J.tw, cnS);
-    const int nparts = ng.ncx * ng.nby;
+    const SepGrid sg = sep_grid(rw, rh);
+    int nparts = 0, partOff[2] = {0, 0};
+    for (int c = 0; c < G->nclass; c++) {
+        int P = 0;
+        partOff[c] = nparts;
+        nparts += G->fc[c].ntiles * inv_rows_ctas_per_tile(G->fc[c], &P);
+    }
+    const size_t hElems = (size_t)(cnS + 1) * J.ih * sg.hp;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
-                   Arena::bytes(nparts, sizeof(Partial));
-    if (!J.map) bytes += Arena::bytes((size_t)rw * rh, sizeof(float));
+                   Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
+                   Arena::bytes((size_t)rw * rh, sizeof(float2));
     for (int c = 0; c < G->nclass; c++) {
         bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
         if (!J.cachedP) bytes += Arena::bytes(tspec_elems(G->fc[c], cnS), sizeof(float2));
@@ -315,7 +322,8 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     DevParams *P = A.take<DevParams>(1);
     DevFrame *F = A.take<DevFrame>(1);
     Partial *parts = A.take<Partial>(nparts);
-    float *corr = J.map ? J.map : A.take<float>((size_t)rw * rh);
+    unsigned int *H = A.take<unsigned int>(hElems);
+    float2 *lanes = A.take<float2>((size_t)rw * rh);
     float2 *spec[2] = {nullptr, nullptr};
     const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
     float2 *tsOwn[2] = {nullptr, nullptr};
@@ -344,11 +352,12 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.solo.outIdx = 0;
     ms.params = P;
     ms.map = J.map;
-    ms.corr = corr;
-    ms.corrStride = 0;
-    // Fork: statistics, alpha scans and the template spectrum on the side
-    // stream; the frame channels whose presence does not depend on the
-    // alpha decision (all of them for a fixed cn, RGB for colour) on st.
+    ms.lanes = lanes;
+    ms.lanesStride = 0;
+    // Fork: statistics, alpha scans, the template spectrum and the window
+    // statistics on the side stream; the frame channels whose presence does
+    // not depend on the alpha decision (all of them for a fixed cn, RGB for
+    // colour) on st.
     SideStream &ss = side_stream();
     CVM_CUDA(cudaEventRecord(ss.fork, st));
     CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
@@ -358,6 +367,9 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     if (!J.cachedP)
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st));
     CVM_CUDA(cudaEventRecord(ss.join, ss.st));
+    CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg, J.mode == 1 ? 3 : J.cnFixed,
+                              J.mode == 1 ? 4 : J.cnFixed, H, 0, ss.st));
+    CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st));
     const int cnSure = J.mode == 1 ? 3 : cnS;
     for (int c = 0; c < G->nclass; c++)
         CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnSure, nullptr, G->g, G->fc[c], spec[c], cnS, st));
@@ -369,10 +381,10 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         ms.scratch[c] = spec[c];
         ms.scratchStride[c] = 0;
         CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
-        CVM_CUDA(launch_inv_rows(G->g, f, c, cnS, ms, 1, st));
     }
-    for (int cnL = J.mode == 1 ? 3 : J.cnFixed; cnL <= (J.mode == 1 ? 4 : J.cnFixed); cnL++)
-        CVM_CUDA(launch_norm(J.img, J.istride, J.step, ms, 1, ng, cnL, parts, &F->normDone, J.out, st));
+    CVM_CUDA(cudaStreamWaitEvent(st, ss.joinStats, 0));
+    for (int c = 0; c < G->nclass; c++)
+        CVM_CUDA(launch_inv_rows(G->g, G->fc[c], c, cnS, ms, 1, partOff[c], nparts, parts, &F->normDone, J.out, st));
     return CVM_OK;
 }
 
@@ -584,7 +596,8 @@ int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, 
 
 struct FleetBucketGeom {
     Geom G;
-    NormGrid ng;
+    SepGrid sg;
+    int nparts = 0, partOff[2] = {0, 0};
     int rwMax = 0, rhMax = 0;
     int cnS = 1;
     std::vector<float2 *> ts;     // per member: class 0, class 1 (owned)
@@ -644,8 +657,14 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
             bg->rwMax = std::max(bg->rwMax, pw - f->ms[mi]->w + 1);
             bg->rhMax = std::max(bg->rhMax, ph - f->ms[mi]->h + 1);
         }
-        bg->ng = norm_grid(bg->rwMax, bg->rhMax, b.tw, bg->cnS);
-        const int nparts = bg->ng.ncx * bg->ng.nby;
+        bg->sg = sep_grid(bg->rwMax, bg->rhMax);
+        int nparts = 0;
+        for (int c = 0; c < G.nclass; c++) {
+            int P = 0;
+            bg->partOff[c] = nparts;
+            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], &P);
+        }
+        bg->nparts = nparts;
         std::vector<DevMember> tab(b.members.size());
         for (size_t pos = 0; pos < b.members.size(); pos++) {
             cvm_matcher *m = f->ms[b.members[pos]];
@@ -704,15 +723,16 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             fb += Arena::bytes(spec_elems(bg.G.fc[c], cnS), sizeof(float2));
             per += bg.memberScratch[c] * sizeof(float2);
         }
-        const size_t corrPer = (size_t)bg.rwMax * bg.rhMax;
-        const int nparts = bg.ng.ncx * bg.ng.nby;
-        per += corrPer * sizeof(float);
+        const size_t lanesPer = (size_t)bg.rwMax * bg.rhMax;
+        const size_t hPer = (size_t)(cnS + 1) * ph * bg.sg.hp;
+        const int nparts = bg.nparts;
+        per += lanesPer * sizeof(float2) + hPer * sizeof(unsigned int);
         frameBytes = std::max(frameBytes, fb);
         partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
         w = std::min<int>(w, (int)bg.members.size());
         wave[b] = w;
-        size_t wb = Arena::bytes((size_t)w * corrPer, sizeof(float));
+        size_t wb = Arena::bytes((size_t)w * lanesPer, sizeof(float2)) + Arena::bytes((size_t)w * hPer, sizeof(unsigned int));
         for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));
         waveBytes = std::max(waveBytes, wb);
     }
@@ -738,10 +758,11 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
-        const int nparts = bg.ng.ncx * bg.ng.nby;
+        const size_t hPer = (size_t)(cnS + 1) * ph * bg.sg.hp;
+        unsigned int *H = nullptr;
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
-        float *corr = nullptr;
+        float2 *lanes = nullptr;
         {
             Arena fa;
             fa.base = frameBase;
@@ -751,7 +772,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 frame[c] = fa.take<float2>(spec_elems(G.fc[c], cnS));
                 scratch[c] = wa.take<float2>((size_t)wave[b] * bg.memberScratch[c]);
             }
-            corr = wa.take<float>((size_t)wave[b] * bg.rwMax * bg.rhMax);
+            lanes = wa.take<float2>((size_t)wave[b] * bg.rwMax * bg.rhMax);
+            H = wa.take<unsigned int>((size_t)wave[b] * hPer);
         }
         // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
         for (int c = 0; c < G.nclass; c++) {
@@ -765,8 +787,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         memset(&ms, 0, sizeof ms);
         ms.table = bg.table;
         ms.params = P;
-        ms.corr = corr;
-        ms.corrStride = (size_t)bg.rwMax * bg.rhMax;
+        ms.lanes = lanes;
+        ms.lanesStride = (size_t)bg.rwMax * bg.rhMax;
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -775,14 +797,14 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         for (int w0 = 0; w0 < nm; w0 += wave[b]) {
             const int nw = std::min(wave[b], nm - w0);
             ms.first = w0;
-            for (int c = 0; c < G.nclass; c++) {
+            CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, bg.sg, f->step == 4 ? 3 : 1,
+                                      f->step == 4 ? 4 : 1, H, hPer, st));
+            for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
-                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, st));
-            }
-            for (int cnL = f->step == 4 ? 3 : 1; cnL <= (f->step == 4 ? 4 : 1); cnL++)
-                CVM_CUDA(launch_norm(dParent, pstride, f->step, ms, nw, bg.ng, cnL, parts, counters, dOut, st));
+            for (int c = 0; c < G.nclass; c++)
+                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, bg.partOff[c], bg.nparts, parts, counters, dOut,
+                                         st));
         }
-        (void)nparts;
     }
     return CVM_OK;
 }

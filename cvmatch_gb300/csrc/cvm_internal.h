@@ -99,8 +99,10 @@ struct MemberSet {
     float2 *scratch[2];        // column-pass output, per wave slot
     size_t scratchStride[2];   // elements between wave slots
     float *map;                // optional score map (solo only)
-    float *corr;               // raw correlation, per wave slot (pitch rw)
+    float *corr;               // raw correlation, per wave slot (pitch rw), k_norm only
     size_t corrStride;         // elements between wave slots
+    float2 *lanes;             // per result (t, den) of the statistics kernel, per wave slot
+    size_t lanesStride;        // elements between wave slots
 };
 
 struct Partial {
@@ -135,9 +137,16 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
 cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
                         const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
                         const MemberSet &ms, int nmembers, cudaStream_t st);
-// Inverse rows + channel accumulation into each member's raw correlation.
+// Inverse rows + channel accumulation + the correlation-dependent end of
+// normOne from the members' lanes, first-occurrence extrema, and the
+// member's result written by its last CTA.  Partial records of a member:
+// nparts = sum over its plan classes of ntiles * inv_rows_ctas_per_tile;
+// partOffset = the records of the classes launched before this one;
+// counters[pIdx] must be zero before the first class's launch.
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
-                            int nmembers, cudaStream_t st);
+                            int nmembers, int partOffset, int nparts, Partial *partials, int *counters,
+                            cvm_result *out, cudaStream_t st);
+int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta);
 // Normalisation + first-occurrence extrema: CW x B results per CTA, ncx x
 // nby CTAs per member, result rows in groups of G; the member's last CTA
 // writes its result to out[outIdx].  counters (one int per member of the
@@ -154,6 +163,19 @@ NormGrid norm_grid(int rwMax, int rhMax, int twMax, int cnCap);
 cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const MemberSet &ms, int nmembers,
                         const NormGrid &ng, int cnLaunch, Partial *partials, int *counters, cvm_result *out,
                         cudaStream_t st);
+// Separable window statistics: k_hsum writes horizontal window sums (u32,
+// [q][ih][hp] per wave slot), k_vstats slides them down BV-row bands and
+// stores per result (t, den) into ms.lanes (pitch rw per slot).  The planes
+// of one slot take (cnMax+1) * ih * hp * 4 bytes; [cnMin, cnMax] is the
+// range of device-side channel counts the members may have.
+struct SepGrid {
+    int BV, ncx, nby, hp;
+};
+SepGrid sep_grid(int rwMax, int rhMax);
+cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
+                             int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
+                             unsigned int *H, size_t slotStride, cudaStream_t st);
+
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).
 cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st);

@@ -618,6 +618,253 @@ __global__ void k_cols(ColsArgs a) {
     }
 }
 
+// ------------------------------------------- column pass, even log2 dftH
+// With the reference's storage relabelling (forward rows stored at
+// bit-reversed slots, inverse read through rmap = brev), the forward
+// cascade's last pass and the inverse cascade's first pass act on the same
+// element sets when log2 dftH is even: the 16 rows {B + S*c} (S = dftH/16)
+// hold complete butterflies of the forward's last stage(s), and through the
+// bit reversal the same rows are one contiguous 16-slot block of the
+// inverse's first two stages (slot 16a+r <-> row B + S*brev4(r)).  So the
+// forward's last pass, the conj-multiply and the inverse's first pass run
+// in registers in one sweep; the forward's first pass reads global memory
+// directly and the inverse's last pass writes it.  Every butterfly keeps
+// the reference's op sequence and twiddle.
+
+template <bool INV, typename LD, typename ST>
+__device__ __forceinline__ void unit_r16_io(const LD &ld, const ST &st, int base, int h,
+                                            const float2 *__restrict__ tA, const float2 *__restrict__ tB) {
+    float2 e[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) e[i] = ld(base + h * i);
+    const int j = base & (h - 1);
+    const float2 a1 = __ldg(tA + j), a2 = __ldg(tA + h + j), a3 = __ldg(tA + 2 * h + j);
+#pragma unroll
+    for (int b = 0; b < 4; b++) bfly4<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int jj = j + h * q;
+        bfly4<INV>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + jj), __ldg(tB + 4 * h + jj),
+                   __ldg(tB + 8 * h + jj));
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) st(base + h * i, e[i]);
+}
+
+template <bool INV, typename LD, typename ST>
+__device__ __forceinline__ void unit_r4_io(const LD &ld, const ST &st, int base, int h, const float2 *__restrict__ t) {
+    float2 e[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) e[i] = ld(base + h * i);
+    const int j = base & (h - 1);
+    bfly4<INV>(&e[0], &e[1], &e[2], &e[3], __ldg(t + j), __ldg(t + h + j), __ldg(t + 2 * h + j));
+#pragma unroll
+    for (int i = 0; i < 4; i++) st(base + h * i, e[i]);
+}
+
+__device__ __forceinline__ int brev4c(int r) { return ((r & 1) << 3) | ((r & 2) << 1) | ((r & 4) >> 1) | ((r & 8) >> 3); }
+
+// One even-log2 radix pass (r16 at quarter h, or r4 at h) over all columns
+// of the strip with the given element I/O.  Ends with a barrier.
+template <bool INV, typename LD, typename ST>
+__device__ __forceinline__ void even_pass(int H, int SC, int logSC, bool r16, int h, const float2 *t, const LD &ld,
+                                          const ST &st) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int units = r16 ? H >> 4 : H >> 2;
+    const int lh = 31 - __clz(h);
+    for (int u = tid; u < (units << logSC); u += nt) {
+        const int c = u & (SC - 1), v = u >> logSC;
+        const int j = v & (h - 1), blk = v >> lh;
+        auto l = [&](int i) { return ld(c, i); };
+        auto w = [&](int i, float2 x) { st(c, i, x); };
+        if (r16)
+            unit_r16_io<INV>(l, w, blk * 16 * h + j, h, t, t + 3 * h);
+        else
+            unit_r4_io<INV>(l, w, blk * 4 * h + j, h, t);
+    }
+    __syncthreads();
+}
+
+// The middle sweep over the row sets {B + S*c : c < M} (M = 16, or 4 when
+// dftH = 4): forward's last pass (r16 at quarter hL, or the trailing r4 at
+// hL = 4S), conj-multiply, inverse's first pass; the results go to shared
+// memory (or straight to global memory when the transform has one pass).
+template <int M, int MODE, typename LDX, typename STI, typename STS>
+__device__ __forceinline__ void middle_sweep(int S, int logSC, int SC, int L, bool fwdLastR16, int hL,
+                                             const float2 *__restrict__ tri, const float2 *__restrict__ ts, int hwp,
+                                             int wv, const LDX &ldx, const STI &store_inv, const STS &store_smem,
+                                             bool onlyPass) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float2 zero = make_float2(0.f, 0.f);
+    const float2 *tL = tri + (hL - 1);
+    for (int u = tid; u < (S << logSC); u += nt) {
+        const int c = u & (SC - 1), B = u >> logSC;
+        float2 x[M];
+#pragma unroll
+        for (int ci = 0; ci < M; ci++) x[ci] = ldx(c, B + S * ci);
+        if (MODE == 1) {
+            if (M == 16 && fwdLastR16) {
+                const float2 a1 = __ldg(tL + B), a2 = __ldg(tL + hL + B), a3 = __ldg(tL + 2 * hL + B);
+#pragma unroll
+                for (int q = 0; q < M / 4; q++)
+                    bfly4<false>(&x[4 * q], &x[4 * q + 1], &x[4 * q + 2], &x[4 * q + 3], a1, a2, a3);
+                const float2 *tB = tL + 3 * hL;
+#pragma unroll
+                for (int q = 0; q < M / 4; q++) {
+                    const int jj = B + hL * q;
+                    bfly4<false>(&x[q], &x[q + M / 4], &x[q + M / 2], &x[q + 3 * M / 4], __ldg(tB + jj),
+                                 __ldg(tB + 4 * hL + jj), __ldg(tB + 8 * hL + jj));
+                }
+            } else {
+                // trailing r4 stage hL = 4S (or dftH = 4): butterflies j = B + S*q
+#pragma unroll
+                for (int q = 0; q < M / 4; q++) {
+                    const int j = B + S * q;
+                    bfly4<false>(&x[q], &x[q + M / 4], &x[q + M / 2], &x[q + 3 * M / 4], __ldg(tL + j),
+                                 __ldg(tL + hL + j), __ldg(tL + 2 * hL + j));
+                }
+            }
+        }
+        // spec *= conj(tspec) (mulConjGo, impl.go:376-388)
+#pragma unroll
+        for (int ci = 0; ci < M; ci++) {
+            const float2 av = x[ci], bv = c < wv ? __ldg(ts + (size_t)(B + S * ci) * hwp + c) : zero;
+            x[ci] = make_float2(__fadd_rn(__fmul_rn(av.x, bv.x), __fmul_rn(av.y, bv.y)),
+                                __fsub_rn(__fmul_rn(av.y, bv.x), __fmul_rn(av.x, bv.y)));
+        }
+        // inverse's first pass: logical slot base+r holds row B + S*brev(r)
+        const int abase = brev_bits(B, L);
+        float2 e[M];
+#pragma unroll
+        for (int r = 0; r < M; r++) e[r] = x[M == 16 ? brev4c(r) : ((r & 1) << 1) | ((r & 2) >> 1)];
+        const float2 a1 = __ldg(tri), a2 = __ldg(tri + 1), a3 = __ldg(tri + 2);
+#pragma unroll
+        for (int q = 0; q < M / 4; q++) bfly4<true>(&e[4 * q], &e[4 * q + 1], &e[4 * q + 2], &e[4 * q + 3], a1, a2, a3);
+        if (M == 16) {
+            const float2 *tB = tri + 3;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                bfly4<true>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + q), __ldg(tB + 4 + q), __ldg(tB + 8 + q));
+        }
+#pragma unroll
+        for (int r = 0; r < M; r++) {
+            const int row = B + S * (M == 16 ? brev4c(r) : (((r & 1) << 1) | ((r & 2) >> 1)));
+            if (onlyPass)
+                store_inv(c, abase + r, e[r]);
+            else
+                store_smem(c, row, e[r]);
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
+    extern __shared__ float2 smem[];
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.z % fc.ntiles;
+    const int slot = blockIdx.z / fc.ntiles;
+    const int tile = fc.tileFirst + tileLocal;
+    const int k = blockIdx.y;
+    const DevMember *m = a.mode == 0 ? nullptr : &member_of(a.ms, slot);
+    const DevParams *Pm = m ? a.ms.params + m->pIdx : nullptr;
+    int cn;
+    if (m)
+        cn = Pm->cn;
+    else
+        cn = a.cnDev ? min(*a.cnDev, a.chanCount) : a.chanCount;
+    if (k >= cn) return;
+    if (Pm && Pm->flat) return;
+    const int SC = a.SC, logSC = a.logSC;
+    const int c0 = blockIdx.x * SC;
+    const int H = fc.dftH, L = fc.log2H, hwp = fc.hwp;
+    const int wv = min(SC, fc.hw - c0);
+    const size_t chanStride = (size_t)H * hwp;
+    const TileBox b = tile_box(a.g, tile);
+    const float2 *tri = fc.triH;
+    const float2 zero = make_float2(0.f, 0.f);
+    // even-log2 passes: r16 at h = 16^p for p < L/4, then r4 at h = 16^(L/4)
+    // when L % 4 == 2; stage h's twiddles start at tri + h - 1
+    const int nR16 = L >> 2;
+    const int nPass = nR16 + ((L & 2) ? 1 : 0);
+    auto passH = [](int p) { return 1 << (4 * p); };
+    auto passR16 = [=](int p) { return p < nR16; };
+    const float2 *src = a.in + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+    const int loaded = min(H, (b.loadH + 1) & ~1);
+    auto gload_slots = [=](int c, int s) -> float2 {  // forward-rows output at slot s
+        return (c < wv && brev_bits(s, L) < loaded) ? src[(size_t)s * hwp + c] : zero;
+    };
+    auto sld = [=](int c, int i) { return smem[(i << logSC) + c]; };
+    auto sst = [=](int c, int i, float2 v) { smem[(i << logSC) + c] = v; };
+    auto sld_r = [=](int c, int i) { return smem[(brev_bits(i, L) << logSC) + c]; };
+    auto sst_r = [=](int c, int i, float2 v) { smem[(brev_bits(i, L) << logSC) + c] = v; };
+
+    if (a.mode == 0) {
+        float2 *dst = a.out + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+        const float sc = a.scale;
+        auto gst_nat = [=](int c, int i, float2 v) {
+            if (c < wv) {
+                if (sc != 1.0f) v = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+                dst[(size_t)i * hwp + c] = v;
+            }
+        };
+        for (int p = 0; p < nPass; p++) {
+            const int h = passH(p);
+            const float2 *t = tri + (h - 1);
+            const bool first = p == 0, last = p == nPass - 1;
+            if (first && last)
+                even_pass<false>(H, SC, logSC, passR16(p), h, t, gload_slots, gst_nat);
+            else if (first)
+                even_pass<false>(H, SC, logSC, passR16(p), h, t, gload_slots, sst);
+            else if (last)
+                even_pass<false>(H, SC, logSC, passR16(p), h, t, sld, gst_nat);
+            else
+                even_pass<false>(H, SC, logSC, passR16(p), h, t, sld, sst);
+        }
+        return;
+    }
+    if (a.mode == 1)
+        for (int p = 0; p + 1 < nPass; p++) {
+            const int h = passH(p);
+            if (p == 0)
+                even_pass<false>(H, SC, logSC, passR16(p), h, tri + (h - 1), gload_slots, sst);
+            else
+                even_pass<false>(H, SC, logSC, passR16(p), h, tri + (h - 1), sld, sst);
+        }
+    const int ty = tile / a.g.ntx;
+    const int bh = (ty == a.g.nty - 1) ? m->rh - b.y0 : a.g.blockH;
+    const int rowsOut = min(H, (bh + 1) & ~1);
+    float2 *dst = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] +
+                  ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
+    auto gst_inv = [=](int c, int i, float2 v) {  // logical slot i -> row brev(i)
+        if (c < wv && i < rowsOut) dst[(size_t)brev_bits(i, L) * hwp + c] = v;
+    };
+    const float2 *ts = m->tspec[a.cls] + (size_t)k * chanStride + c0;
+    const bool onlyPass = nPass == 1;
+    const int hL = passH(nPass - 1);
+    const bool fwdLastR16 = passR16(nPass - 1);
+    auto ld_mode2 = [=](int c, int row) { return c < wv ? src[(size_t)row * hwp + c] : zero; };
+    auto ld_mid = [=](int c, int row) { return onlyPass ? gload_slots(c, row) : smem[(row << logSC) + c]; };
+    if (H >= 16) {
+        const int S = H >> 4;
+        if (a.mode == 2)
+            middle_sweep<16, 2>(S, logSC, SC, L, fwdLastR16, hL, tri, ts, hwp, wv, ld_mode2, gst_inv, sst, onlyPass);
+        else
+            middle_sweep<16, 1>(S, logSC, SC, L, fwdLastR16, hL, tri, ts, hwp, wv, ld_mid, gst_inv, sst, onlyPass);
+    } else {
+        if (a.mode == 2)
+            middle_sweep<4, 2>(1, logSC, SC, L, false, 1, tri, ts, hwp, wv, ld_mode2, gst_inv, sst, onlyPass);
+        else
+            middle_sweep<4, 1>(1, logSC, SC, L, false, 1, tri, ts, hwp, wv, ld_mid, gst_inv, sst, onlyPass);
+    }
+    for (int p = 1; p < nPass; p++) {
+        const int h = passH(p);
+        if (p == nPass - 1)
+            even_pass<true>(H, SC, logSC, passR16(p), h, tri + (h - 1), sld_r, gst_inv);
+        else
+            even_pass<true>(H, SC, logSC, passR16(p), h, tri + (h - 1), sld_r, sst_r);
+    }
+}
+
 // ------------------------------------------------------- inverse rows
 
 // Round-to-nearest-even of a positive integer to `bits` significant bits.
@@ -631,18 +878,18 @@ __device__ __forceinline__ unsigned long long rn_bits(unsigned long long a, int 
     return q << sh;
 }
 
-// Correctly rounded float32 of an unsigned 64-bit integer in integer
-// arithmetic (a 64-bit integer conversion instruction would run on the FP64
-// pipe, which GB300 provisions at a small fraction of FP32): the top 24
-// significant bits, rounded to nearest even on the dropped bits, then the
-// exponent added exactly.
+// Correctly rounded float32 of an unsigned 64-bit integer without the 64-bit
+// conversion instruction (it runs on the FP64 pipe, which GB300 provisions
+// at a small fraction of FP32): the top 32 bits with the OR of the dropped
+// bits as a sticky bit round exactly like the full value under one
+// u32->f32 rounding, and the exponent is then adjusted exactly.
 __device__ __forceinline__ float u64_to_f32_rn(unsigned long long a) {
-    if ((a >> 32) == 0) return __uint2float_rn((unsigned int)a);
-    const int sh = 40 - __clzll((long long)a);  // bit length - 24, in 9..40
-    const unsigned int q = (unsigned int)(a >> sh);
-    const unsigned long long rem = a << (64 - sh);  // dropped bits, left-aligned
-    const unsigned int up = (rem > 0x8000000000000000ull) || (rem == 0x8000000000000000ull && (q & 1u));
-    const float f = __uint2float_rn(q + up);  // <= 2^24: exact
+    const unsigned int hi = (unsigned int)(a >> 32), lo = (unsigned int)a;
+    if (hi == 0) return __uint2float_rn(lo);
+    const int sh = 32 - __clz(hi);  // bits above the low word, 1..32
+    const unsigned int t = (unsigned int)(a >> sh);
+    const unsigned int dropped = sh == 32 ? lo : (lo & ((1u << sh) - 1u));
+    const float f = __uint2float_rn(t | (dropped != 0u));
     return __int_as_float(__float_as_int(f) + (sh << 23));
 }
 
@@ -742,81 +989,161 @@ __device__ void ext_block_reduce(Ext &e, Ext *sh) {
     }
 }
 
+__device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
+    cvm_result r;
+    r.min_v = e.minV;
+    r.max_v = e.maxV;
+    r.min_x = (int32_t)(e.minI % rw);
+    r.min_y = (int32_t)(e.minI / rw);
+    r.max_x = (int32_t)(e.maxI % rw);
+    r.max_y = (int32_t)(e.maxI / rw);
+    *out = r;
+}
+
 struct InvArgs {
     TileGeom g;
     FftClass fc;
     int cls, cnS;
     MemberSet ms;
     int pairsPerCta;
+    int partOffset;   // partial records of the classes before this one
+    int nparts;       // partial records per member (all classes)
+    Partial *partials;
+    int *counters;    // per member params index
+    cvm_result *out;
 };
 
 // inverseRowPair (impl.go:394-444) for P row pairs of one (member, tile):
-// combine, inverse row transform, then the channels accumulated in channel
-// order (the add=k>0 emit of impl.go:425-443) and stored as the raw
-// correlation the normalisation consumes.
-__global__ void k_inv_rows(InvArgs a) {
+// combine, inverse row transform, the channels accumulated in channel order
+// (the add=k>0 emit of impl.go:425-443), then the rest of normOne
+// (impl.go:825-849) with the per-result (t, den) the statistics kernel
+// prepared, first-occurrence extrema per CTA, and the member's last CTA
+// merges them in raster-order semantics (impl.go:1104-1112).
+__global__ void __launch_bounds__(256) k_inv_rows(InvArgs a) {
     extern __shared__ float2 smem[];
+    __shared__ Ext shExt[kThreads / 32];
+    __shared__ int isLast;
     const FftClass &fc = a.fc;
     const int tileLocal = blockIdx.y;
     const int tile = fc.tileFirst + tileLocal;
     const int slot = blockIdx.z;
     const DevMember &m = member_of(a.ms, slot);
     const DevParams &Pm = a.ms.params[m.pIdx];
-    if (Pm.flat) return;
     const TileBox tb = tile_box(a.g, tile);
     const int tx = tile % a.g.ntx, ty = tile / a.g.ntx;
     const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
     const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
     const int pair0 = blockIdx.x * a.pairsPerCta;
-    if (2 * pair0 >= bh) return;
-    const int P = min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1);
+    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
     const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp, ld = padded_len(n);
     const int tid = threadIdx.x, nt = blockDim.x;
+    const bool flat = Pm.flat != 0;
     float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * ld);  // [P][2][n]
-    const int cn = Pm.cn;
-    const size_t chanStride = (size_t)fc.dftH * hwp;
-    const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
-    for (int k = 0; k < cn; k++) {
-        const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
-        for (int idx = tid; idx < P * n; idx += nt) {
-            const int p = idx >> log2n, kk = idx & (n - 1);
-            const int r = 2 * (pair0 + p);
-            const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
-            const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
-            float2 z;
-            if (kk < hw) {
-                const float2 u = sa[kk], v = sb[kk];
-                z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
-            } else {
-                const int mm = n - kk;
-                const float2 u = sa[mm], v = sb[mm];
-                z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+    Ext e;
+    ext_init(e);
+    if (P > 0 && !flat) {
+        const int cn = Pm.cn;
+        const size_t chanStride = (size_t)fc.dftH * hwp;
+        const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
+        for (int k = 0; k < cn; k++) {
+            const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
+            for (int idx = tid; idx < P * n; idx += nt) {
+                const int p = idx >> log2n, kk = idx & (n - 1);
+                const int r = 2 * (pair0 + p);
+                const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
+                const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
+                float2 z;
+                if (kk < hw) {
+                    const float2 u = sa[kk], v = sb[kk];
+                    z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+                } else {
+                    const int mm = n - kk;
+                    const float2 u = sa[mm], v = sb[mm];
+                    z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+                }
+                smem[p * ld + padi(brev_bits(kk, log2n))] = z;
             }
-            smem[p * ld + padi(brev_bits(kk, log2n))] = z;
+            __syncthreads();
+            auto la = [=](int line, int i) { return line * ld + padi(i); };
+            fft_cascade<true>(smem, n, log2n, P, la, fc.triW);
+            for (int idx = tid; idx < P * bw; idx += nt) {
+                const int p = idx / bw, x = idx - p * bw;
+                const float2 z = smem[p * ld + padi(x)];
+                float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
+                if (k == 0) {
+                    *a0 = z.x;
+                    *a1 = z.y;
+                } else {
+                    *a0 = __fadd_rn(*a0, z.x);
+                    *a1 = __fadd_rn(*a1, z.y);
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        auto la = [=](int line, int i) { return line * ld + padi(i); };
-        fft_cascade<true>(smem, n, log2n, P, la, fc.triW);
-        for (int idx = tid; idx < P * bw; idx += nt) {
-            const int p = idx / bw, x = idx - p * bw;
-            const float2 z = smem[p * ld + padi(x)];
-            float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
-            if (k == 0) {
-                *a0 = z.x;
-                *a1 = z.y;
-            } else {
-                *a0 = __fadd_rn(*a0, z.x);
-                *a1 = __fadd_rn(*a1, z.y);
+    }
+    if (!a.ms.lanes) {
+        // No statistics lanes: store the raw correlation for k_norm instead.
+        if (P > 0 && !flat) {
+            float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
+            for (int idx = tid; idx < 2 * P * bw; idx += nt) {
+                const int rr = idx / bw, x = idx - rr * bw;
+                const int r = 2 * pair0 + rr;
+                if (r < bh) corr[(size_t)(tb.y0 + r) * m.rw + tb.x0 + x] = acc[(size_t)rr * n + x];
             }
         }
-        __syncthreads();
+        return;
     }
-    float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
-    for (int idx = tid; idx < 2 * P * bw; idx += nt) {
-        const int rr = idx / bw, x = idx - rr * bw;
-        const int r = 2 * pair0 + rr;
-        if (r < bh) corr[(size_t)(tb.y0 + r) * m.rw + tb.x0 + x] = acc[(size_t)rr * n + x];
+    if (P > 0) {
+        const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
+        float *map = a.ms.map;
+        for (int idx = tid; idx < 2 * P * bw; idx += nt) {
+            const int rr = idx / bw, x = idx - rr * bw;
+            const int r = 2 * pair0 + rr;
+            if (r >= bh) continue;
+            const long long li = (long long)(tb.y0 + r) * m.rw + tb.x0 + x;
+            float score = 1.f;
+            if (!flat) {
+                const float2 td = lanes[li];
+                const float num = __fsub_rn(acc[(size_t)rr * n + x], td.x);
+                const float den = td.y, an = fabsf(num);
+                if (an < den)
+                    score = __fdiv_rn(num, den);
+                else if (an < __fmul_rn(den, 1.125f))
+                    score = num > 0.f ? 1.f : -1.f;
+                else
+                    score = 0.f;
+            }
+            if (map) map[li] = score;
+            ext_add(e, score, li);
+        }
     }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (tid == 0) {
+        Partial &o = a.partials[m.partBase + a.partOffset + tileLocal * gridDim.x + blockIdx.x];
+        o.minV = e.minV;
+        o.maxV = e.maxV;
+        o.minI = e.minI;
+        o.maxI = e.maxI;
+        __threadfence();
+        isLast = atomicAdd(&a.counters[m.pIdx], 1) == a.nparts - 1;
+    }
+    __syncthreads();
+    if (!isLast) return;
+    __threadfence();
+    ext_init(e);
+    for (int i = tid; i < a.nparts; i += nt) {
+        const volatile Partial *p = a.partials + m.partBase + i;
+        Ext o;
+        o.minV = p->minV;
+        o.maxV = p->maxV;
+        o.minI = p->minI;
+        o.maxI = p->maxI;
+        ext_merge(e, o);
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (tid == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
 }
 
 // ----------------------------------------------------------- normalise
@@ -834,16 +1161,6 @@ struct NormArgs {
     cvm_result *out;
 };
 
-__device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
-    cvm_result r;
-    r.min_v = e.minV;
-    r.max_v = e.maxV;
-    r.min_x = (int32_t)(e.minI % rw);
-    r.min_y = (int32_t)(e.minI / rw);
-    r.max_x = (int32_t)(e.maxI % rw);
-    r.max_y = (int32_t)(e.maxI / rw);
-    *out = r;
-}
 
 // Window statistics by the reference's own sliding scheme
 // (colBuildGo/colSlideGo, impl.go:708-805, and the per-row window sums of
@@ -1072,6 +1389,234 @@ __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
     if (tid == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
 }
 
+// ------------------------------------------- separable window statistics
+
+// Horizontal window sums of every image row for template width tw:
+// H_q(x, r) = sum_{dx<tw} v_q(x+dx, r) for the CN channels and q = CN the
+// squared pixels summed over the channels (impl.go:708-805 restated as a
+// separable box sum).  One CTA per image row: a block prefix scan of the
+// row in u32 (modular; every window sum is < 2^32 because tw <= 8192 and
+// cn*65025*tw < 2^32), then one difference per output.  Planes are
+// [q][ih][hp] u32 with hp the padded result width.
+struct HsumArgs {
+    const uint8_t *img;
+    long long istride;
+    int step, iw, ih, rw, tw, hp;
+    unsigned int *H;          // plane q of wave slot z at H + z*slotStride + q*planeStride
+    size_t planeStride, slotStride;
+    const DevMember *table;   // fleet: per-slot member (tw, pIdx); nullptr: solo
+    int first;
+    const DevParams *params;
+    int pIdx;                 // solo member params index
+};
+
+template <int CN>
+__device__ __forceinline__ void hsum_row(const HsumArgs &a, int slot, int tw, int rw, unsigned int *sp,
+                                         unsigned int (*wsum)[5]) {
+    const int r = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int iw = a.iw, ld = iw + 1;
+    const uint8_t *row = a.img + (long long)r * a.istride;
+    // 1. coalesced staging of the row's channel values (slot c+1; slot 0 = 0)
+    if (a.step == 4 && ((reinterpret_cast<size_t>(row) & 3) == 0)) {
+        const uchar4 *r4 = reinterpret_cast<const uchar4 *>(row);
+        for (int x = tid; x < iw; x += nt) {
+            const uchar4 v = r4[x];
+            const unsigned int c[4] = {v.x, v.y, v.z, v.w};
+            unsigned int q = 0;
+#pragma unroll
+            for (int k = 0; k < CN; k++) {
+                sp[k * ld + x + 1] = c[k];
+                q += c[k] * c[k];
+            }
+            sp[CN * ld + x + 1] = q;
+        }
+    } else {
+        for (int x = tid; x < iw; x += nt) {
+            const uint8_t *p = row + (long long)x * a.step;
+            unsigned int q = 0;
+#pragma unroll
+            for (int k = 0; k < CN; k++) {
+                const unsigned int v = p[k];
+                sp[k * ld + x + 1] = v;
+                q += v * v;
+            }
+            sp[CN * ld + x + 1] = q;
+        }
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) sp[q * ld] = 0u;
+    }
+    __syncthreads();
+    // 2. in-place inclusive prefix over slots 1..iw: odd-length segments keep
+    //    the lanes on distinct banks
+    const int seg = ((iw + nt - 1) / nt) | 1;
+    const int c0 = 1 + tid * seg, c1 = min(iw + 1, c0 + seg);
+    unsigned int tot[CN + 1];
+#pragma unroll
+    for (int q = 0; q <= CN; q++) tot[q] = 0u;
+    for (int c = c0; c < c1; c++) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) tot[q] += sp[q * ld + c];
+    }
+    unsigned int inc[CN + 1];
+#pragma unroll
+    for (int q = 0; q <= CN; q++) inc[q] = tot[q];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) {
+            const unsigned int u = __shfl_up_sync(0xffffffffu, inc[q], o);
+            if (lane >= o) inc[q] += u;
+        }
+    }
+    if (lane == 31) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) wsum[warp][q] = inc[q];
+    }
+    __syncthreads();
+    unsigned int run[CN + 1];
+#pragma unroll
+    for (int q = 0; q <= CN; q++) {
+        run[q] = inc[q] - tot[q];
+        for (int w = 0; w < warp; w++) run[q] += wsum[w][q];
+    }
+    for (int c = c0; c < c1; c++) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) {
+            run[q] += sp[q * ld + c];
+            sp[q * ld + c] = run[q];
+        }
+    }
+    __syncthreads();
+    // 3. window sums, coalesced out
+    unsigned int *H = a.H + (size_t)slot * a.slotStride + (size_t)r * a.hp;
+    for (int x = tid; x < rw; x += nt) {
+#pragma unroll
+        for (int q = 0; q <= CN; q++) H[(size_t)q * a.planeStride + x] = sp[q * ld + x + tw] - sp[q * ld + x];
+    }
+}
+
+// One launch covers members of either channel count of a mode (colour: 3
+// or 4, chosen on the device; gray: 1).
+template <int CNA, int CNB>
+__global__ void __launch_bounds__(256) k_hsum(HsumArgs a) {
+    extern __shared__ __align__(16) unsigned int sp[];  // [cn+1][iw+1]
+    __shared__ unsigned int wsum[kThreads / 32][5];
+    const int slot = blockIdx.z;
+    int tw = a.tw, rw = a.rw, pIdx = a.pIdx;
+    if (a.table) {
+        const DevMember &m = a.table[a.first + slot];
+        tw = m.tw;
+        rw = m.rw;
+        pIdx = m.pIdx;
+    }
+    const DevParams &Pm = a.params[pIdx];
+    if (Pm.flat) return;
+    if (Pm.cn == CNA)
+        hsum_row<CNA>(a, slot, tw, rw, sp, wsum);
+    else if (CNB != CNA && Pm.cn == CNB)
+        hsum_row<CNB>(a, slot, tw, rw, sp, wsum);
+}
+
+// Vertical sliding of the horizontal window sums, one thread per result
+// column over a band of BV rows: the window statistics of (x, y) are
+// sum_{dy<th} H(x, y+dy), updated by one entering and one leaving row per
+// step.  Everything of normOne (impl.go:825-849) that does not involve the
+// correlation is evaluated here and stored per result as
+//   t   = float32(lane0) * numScale
+//   den = sqrt(idiff * varScale) * templNorm, or 0 under the lim guard
+// so the inverse-rows epilogue only needs num = corr - t and the ladder.
+struct VstatArgs {
+    const unsigned int *H;
+    size_t planeStride, slotStride;
+    int hp;
+    MemberSet ms;
+    int BV;
+};
+
+template <int CN>
+__device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &m, const DevParams &Pm) {
+    const int slot = blockIdx.z;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Y0 = blockIdx.y * a.BV;
+    if (x >= m.rw || Y0 >= m.rh) return;
+    const int Bv = min(a.BV, m.rh - Y0);
+    const int th = m.th;
+    const unsigned int *H = a.H + (size_t)slot * a.slotStride + x;
+    const size_t ps = a.planeStride;
+    const int hp = a.hp;
+    float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride + x;
+    unsigned int s[CN];
+    unsigned long long q = 0;
+#pragma unroll
+    for (int k = 0; k < CN; k++) s[k] = 0u;
+#pragma unroll 4
+    for (int dy = 0; dy < th; dy++) {
+        const unsigned int *h = H + (size_t)(Y0 + dy) * hp;
+#pragma unroll
+        for (int k = 0; k < CN; k++) s[k] += __ldg(h + k * ps);
+        q += __ldg(h + CN * ps);
+    }
+    const unsigned long long area = (unsigned long long)m.tw * th;
+    const unsigned int t0 = (unsigned int)Pm.tsum[0], t1 = (unsigned int)Pm.tsum[1];
+    const unsigned int t2 = (unsigned int)Pm.tsum[2], t3 = (unsigned int)Pm.tsum[3];
+    const float eps = 1.1920928955078125e-06f;  // 10 * 2^-23
+    for (int y = Y0; y < Y0 + Bv; y++) {
+        unsigned int hin[CN + 1], hout[CN + 1];
+        const bool more = y + 1 < Y0 + Bv;
+        if (more) {
+            const unsigned int *hi = H + (size_t)(y + th) * hp, *ho = H + (size_t)y * hp;
+#pragma unroll
+            for (int k = 0; k <= CN; k++) {
+                hin[k] = __ldg(hi + k * ps);
+                hout[k] = __ldg(ho + k * ps);
+            }
+        }
+        unsigned long long cross = (unsigned long long)s[0] * t0, sq = (unsigned long long)s[0] * s[0];
+        if (CN > 1) {
+            cross += (unsigned long long)s[CN > 1 ? 1 : 0] * t1;
+            sq += (unsigned long long)s[CN > 1 ? 1 : 0] * s[CN > 1 ? 1 : 0];
+        }
+        if (CN > 2) {
+            cross += (unsigned long long)s[CN > 2 ? 2 : 0] * t2;
+            sq += (unsigned long long)s[CN > 2 ? 2 : 0] * s[CN > 2 ? 2 : 0];
+        }
+        if (CN > 3) {
+            cross += (unsigned long long)s[CN > 3 ? 3 : 0] * t3;
+            sq += (unsigned long long)s[CN > 3 ? 3 : 0] * s[CN > 3 ? 3 : 0];
+        }
+        // the spill lanes (impl.go:902-1009) and normOne's corr-free part
+        const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);
+        const float id = f32_via_f64((long long)(area * q - sq));
+        const float t = __fmul_rn(l0, Pm.numScale);
+        const float diff2 = __fmul_rn(id, Pm.varScale);
+        float lim = 0.5f;
+        if (q < (1ull << 24)) {
+            lim = __fmul_rn(eps, __uint2float_rn((unsigned int)q));
+            if (lim > 0.5f) lim = 0.5f;
+        }
+        const float den = diff2 > lim ? __fmul_rn(__fsqrt_rn(diff2), Pm.templNorm) : 0.f;
+        lanes[(size_t)y * m.rw] = make_float2(t, den);
+        if (more) {
+#pragma unroll
+            for (int k = 0; k < CN; k++) s[k] += hin[k] - hout[k];
+            q += (unsigned long long)hin[CN] - (unsigned long long)hout[CN];
+        }
+    }
+}
+
+template <int CNA, int CNB>
+__global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
+    const DevMember &m = member_of(a.ms, blockIdx.z);
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    if (Pm.flat) return;
+    if (Pm.cn == CNA)
+        vstat_cols<CNA>(a, m, Pm);
+    else if (CNB != CNA && Pm.cn == CNB)
+        vstat_cols<CNB>(a, m, Pm);
+}
+
 // Small host values to device memory through kernel arguments.
 struct UploadBlob {
     unsigned char bytes[3072];
@@ -1215,9 +1760,14 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     a.logSC = ilog2i(SC);
     dim3 grid((fc.hw + SC - 1) / SC, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
-    set_smem(k_cols, smem);
     ProfScope ps(mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv"), st);
-    k_cols<<<grid, kThreads, smem, st>>>(a);
+    if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
+        set_smem(k_cols_even, smem);
+        k_cols_even<<<grid, kThreads, smem, st>>>(a);
+    } else {
+        set_smem(k_cols, smem);
+        k_cols<<<grid, kThreads, smem, st>>>(a);
+    }
     count_launches(1);
     return cudaGetLastError();
 }
@@ -1233,7 +1783,8 @@ int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta) {
 }
 
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
-                            int nmembers, cudaStream_t st) {
+                            int nmembers, int partOffset, int nparts, Partial *partials, int *counters,
+                            cvm_result *out, cudaStream_t st) {
     InvArgs a;
     a.g = g;
     a.fc = fc;
@@ -1243,6 +1794,11 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     int P = 0;
     const int ctas = inv_rows_ctas_per_tile(fc, &P);
     a.pairsPerCta = P;
+    a.partOffset = partOffset;
+    a.nparts = nparts;
+    a.partials = partials;
+    a.counters = counters;
+    a.out = out;
     dim3 grid(ctas, fc.ntiles, nmembers);
     const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + 2 * fc.n * sizeof(float));
     set_smem(k_inv_rows, smem);
@@ -1314,6 +1870,74 @@ cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const M
             break;
     }
     count_launches(1);
+    return cudaGetLastError();
+}
+
+SepGrid sep_grid(int rwMax, int rhMax) {
+    SepGrid g;
+    g.BV = 16;
+    g.ncx = (rwMax + kThreads - 1) / kThreads;
+    g.nby = (rhMax + g.BV - 1) / g.BV;
+    g.hp = (rwMax + 31) / 32 * 32;
+    return g;
+}
+
+cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
+                             int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
+                             unsigned int *H, size_t slotStride, cudaStream_t st) {
+    HsumArgs h;
+    h.img = img;
+    h.istride = istride;
+    h.step = step;
+    h.iw = iw;
+    h.ih = ih;
+    h.rw = soloRw;
+    h.tw = soloTw;
+    h.hp = sg.hp;
+    h.H = H;
+    h.planeStride = (size_t)ih * sg.hp;
+    h.slotStride = slotStride;
+    h.table = ms.table;
+    h.first = ms.first;
+    h.params = ms.params;
+    h.pIdx = ms.solo.pIdx;
+    VstatArgs v;
+    v.H = H;
+    v.planeStride = h.planeStride;
+    v.slotStride = slotStride;
+    v.hp = sg.hp;
+    v.ms = ms;
+    v.BV = sg.BV;
+    const size_t smem = (size_t)(cnMax + 1) * (iw + 1) * sizeof(unsigned int);
+    dim3 gh(ih, 1, nmembers), gv(sg.ncx, sg.nby, nmembers);
+    {
+        ProfScope ps("k_hsum", st);
+        if (cnMax == 1) {
+            set_smem(k_hsum<1, 1>, smem);
+            k_hsum<1, 1><<<gh, kThreads, smem, st>>>(h);
+        } else if (cnMax == 2) {
+            set_smem(k_hsum<2, 2>, smem);
+            k_hsum<2, 2><<<gh, kThreads, smem, st>>>(h);
+        } else if (cnMin == 3) {
+            set_smem(k_hsum<3, 4>, smem);
+            k_hsum<3, 4><<<gh, kThreads, smem, st>>>(h);
+        } else {
+            set_smem(k_hsum<4, 4>, smem);
+            k_hsum<4, 4><<<gh, kThreads, smem, st>>>(h);
+        }
+    }
+    {
+        ProfScope ps("k_vstats", st);
+        if (cnMax == 1)
+            k_vstats<1, 1><<<gv, kThreads, 0, st>>>(v);
+        else if (cnMax == 2)
+            k_vstats<2, 2><<<gv, kThreads, 0, st>>>(v);
+        else if (cnMin == 3)
+            k_vstats<3, 4><<<gv, kThreads, 0, st>>>(v);
+        else
+            k_vstats<4, 4><<<gv, kThreads, 0, st>>>(v);
+    }
+    count_launches(2);
     return cudaGetLastError();
 }
 
