@@ -482,17 +482,21 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
     const int n = fc.n, log2n = fc.log2n, ld = padded_len(n);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long rowBase = (long long)b.y0 * istride + (long long)b.x0 * step;
-    for (int idx = tid; idx < lines * n; idx += nt) {
-        const int line = idx >> log2n, x = idx & (n - 1);
+    for (int line = 0; line < lines; line++) {
         const int p = line / cn, k = chanFirst + line - p * cn;
         const int r = 2 * (pair0 + p);
-        float2 v = make_float2(0.f, 0.f);
-        if (x < b.loadW) {
-            const uint8_t *pa = img + rowBase + (long long)r * istride + (long long)x * step + k;
-            v.x = (float)pa[0];
-            if (r + 1 < b.loadH) v.y = (float)pa[istride];
+        const bool two = r + 1 < b.loadH;
+        const uint8_t *pa = img + rowBase + (long long)r * istride + k;
+        float2 *dl = smem + line * ld;
+        for (int x = tid; x < n; x += nt) {
+            float2 v = make_float2(0.f, 0.f);
+            if (x < b.loadW) {
+                const uint8_t *q = pa + (long long)x * step;
+                v.x = (float)q[0];
+                if (two) v.y = (float)q[istride];
+            }
+            dl[padi(brev_bits(x, log2n))] = v;
         }
-        smem[line * ld + padi(brev_bits(x, log2n))] = v;
     }
     __syncthreads();
     auto la = [=](int line, int i) { return line * ld + padi(i); };
@@ -500,16 +504,18 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
     const int hw = fc.hw, mask = n - 1;
     const size_t chanStride = (size_t)fc.dftH * fc.hwp;
     float2 *tbase = spec + (size_t)(tile - fc.tileFirst) * cnS * chanStride;
-    for (int idx = tid; idx < lines * hw; idx += nt) {
-        const int line = idx / hw, kk = idx - line * hw;
+    for (int line = 0; line < lines; line++) {
         const int p = line / cn, k = chanFirst + line - p * cn;
         const int r = 2 * (pair0 + p);
-        const float2 zk = smem[line * ld + padi(kk)], zn = smem[line * ld + padi((n - kk) & mask)];
+        const float2 *zl = smem + line * ld;
         float2 *cb = tbase + (size_t)k * chanStride;
-        cb[(size_t)brev_bits(r, fc.log2H) * fc.hwp + kk] =
-            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
-        cb[(size_t)brev_bits(r + 1, fc.log2H) * fc.hwp + kk] =
-            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zn.y)), __fmul_rn(0.5f, __fsub_rn(zn.x, zk.x)));
+        float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * fc.hwp;
+        float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * fc.hwp;
+        for (int kk = tid; kk < hw; kk += nt) {
+            const float2 zk = zl[padi(kk)], zn = zl[padi((n - kk) & mask)];
+            sa[kk] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
+            sb[kk] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zn.y)), __fmul_rn(0.5f, __fsub_rn(zn.x, zk.x)));
+        }
     }
 }
 
@@ -758,6 +764,7 @@ __device__ __forceinline__ void middle_sweep(int S, int logSC, int SC, int L, bo
     __syncthreads();
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
     extern __shared__ float2 smem[];
     const FftClass &fc = a.fc;
@@ -765,7 +772,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
     const int slot = blockIdx.z / fc.ntiles;
     const int tile = fc.tileFirst + tileLocal;
     const int k = blockIdx.y;
-    const DevMember *m = a.mode == 0 ? nullptr : &member_of(a.ms, slot);
+    const DevMember *m = MODE == 0 ? nullptr : &member_of(a.ms, slot);
     const DevParams *Pm = m ? a.ms.params + m->pIdx : nullptr;
     int cn;
     if (m)
@@ -798,7 +805,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
     auto sld_r = [=](int c, int i) { return smem[(brev_bits(i, L) << logSC) + c]; };
     auto sst_r = [=](int c, int i, float2 v) { smem[(brev_bits(i, L) << logSC) + c] = v; };
 
-    if (a.mode == 0) {
+    if (MODE == 0) {
         float2 *dst = a.out + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
         const float sc = a.scale;
         auto gst_nat = [=](int c, int i, float2 v) {
@@ -822,7 +829,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
         }
         return;
     }
-    if (a.mode == 1)
+    if (MODE == 1)
         for (int p = 0; p + 1 < nPass; p++) {
             const int h = passH(p);
             if (p == 0)
@@ -846,12 +853,12 @@ __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
     auto ld_mid = [=](int c, int row) { return onlyPass ? gload_slots(c, row) : smem[(row << logSC) + c]; };
     if (H >= 16) {
         const int S = H >> 4;
-        if (a.mode == 2)
+        if (MODE == 2)
             middle_sweep<16, 2>(S, logSC, SC, L, fwdLastR16, hL, tri, ts, hwp, wv, ld_mode2, gst_inv, sst, onlyPass);
         else
             middle_sweep<16, 1>(S, logSC, SC, L, fwdLastR16, hL, tri, ts, hwp, wv, ld_mid, gst_inv, sst, onlyPass);
     } else {
-        if (a.mode == 2)
+        if (MODE == 2)
             middle_sweep<4, 2>(1, logSC, SC, L, false, 1, tri, ts, hwp, wv, ld_mode2, gst_inv, sst, onlyPass);
         else
             middle_sweep<4, 1>(1, logSC, SC, L, false, 1, tri, ts, hwp, wv, ld_mid, gst_inv, sst, onlyPass);
@@ -1019,7 +1026,7 @@ struct InvArgs {
 // (impl.go:825-849) with the per-result (t, den) the statistics kernel
 // prepared, first-occurrence extrema per CTA, and the member's last CTA
 // merges them in raster-order semantics (impl.go:1104-1112).
-__global__ void __launch_bounds__(256) k_inv_rows(InvArgs a) {
+__global__ void __launch_bounds__(256, 3) k_inv_rows(InvArgs a) {
     extern __shared__ float2 smem[];
     __shared__ Ext shExt[kThreads / 32];
     __shared__ int isLast;
@@ -1047,35 +1054,42 @@ __global__ void __launch_bounds__(256) k_inv_rows(InvArgs a) {
         const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
         for (int k = 0; k < cn; k++) {
             const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
-            for (int idx = tid; idx < P * n; idx += nt) {
-                const int p = idx >> log2n, kk = idx & (n - 1);
+            for (int p = 0; p < P; p++) {
                 const int r = 2 * (pair0 + p);
                 const float2 *sa = cb + (size_t)brev_bits(r, fc.log2H) * hwp;
                 const float2 *sb = cb + (size_t)brev_bits(r + 1, fc.log2H) * hwp;
-                float2 z;
-                if (kk < hw) {
-                    const float2 u = sa[kk], v = sb[kk];
-                    z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
-                } else {
-                    const int mm = n - kk;
-                    const float2 u = sa[mm], v = sb[mm];
-                    z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+                float2 *zl = smem + p * ld;
+                for (int kk = tid; kk < n; kk += nt) {
+                    float2 z;
+                    if (kk < hw) {
+                        const float2 u = sa[kk], v = sb[kk];
+                        z = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+                    } else {
+                        const int mm = n - kk;
+                        const float2 u = sa[mm], v = sb[mm];
+                        z = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+                    }
+                    zl[padi(brev_bits(kk, log2n))] = z;
                 }
-                smem[p * ld + padi(brev_bits(kk, log2n))] = z;
             }
             __syncthreads();
             auto la = [=](int line, int i) { return line * ld + padi(i); };
             fft_cascade<true>(smem, n, log2n, P, la, fc.triW);
-            for (int idx = tid; idx < P * bw; idx += nt) {
-                const int p = idx / bw, x = idx - p * bw;
-                const float2 z = smem[p * ld + padi(x)];
-                float *a0 = acc + (size_t)(2 * p) * n + x, *a1 = a0 + n;
+            for (int p = 0; p < P; p++) {
+                const float2 *zl = smem + p * ld;
+                float *a0 = acc + (size_t)(2 * p) * n, *a1 = a0 + n;
                 if (k == 0) {
-                    *a0 = z.x;
-                    *a1 = z.y;
+                    for (int x = tid; x < bw; x += nt) {
+                        const float2 z = zl[padi(x)];
+                        a0[x] = z.x;
+                        a1[x] = z.y;
+                    }
                 } else {
-                    *a0 = __fadd_rn(*a0, z.x);
-                    *a1 = __fadd_rn(*a1, z.y);
+                    for (int x = tid; x < bw; x += nt) {
+                        const float2 z = zl[padi(x)];
+                        a0[x] = __fadd_rn(a0[x], z.x);
+                        a1[x] = __fadd_rn(a1[x], z.y);
+                    }
                 }
             }
             __syncthreads();
@@ -1085,21 +1099,19 @@ __global__ void __launch_bounds__(256) k_inv_rows(InvArgs a) {
         // No statistics lanes: store the raw correlation for k_norm instead.
         if (P > 0 && !flat) {
             float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
-            for (int idx = tid; idx < 2 * P * bw; idx += nt) {
-                const int rr = idx / bw, x = idx - rr * bw;
-                const int r = 2 * pair0 + rr;
-                if (r < bh) corr[(size_t)(tb.y0 + r) * m.rw + tb.x0 + x] = acc[(size_t)rr * n + x];
-            }
+            for (int rr = 0; rr < 2 * P && 2 * pair0 + rr < bh; rr++)
+                for (int x = tid; x < bw; x += nt)
+                    corr[(size_t)(tb.y0 + 2 * pair0 + rr) * m.rw + tb.x0 + x] = acc[(size_t)rr * n + x];
         }
         return;
     }
     if (P > 0) {
         const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
         float *map = a.ms.map;
-        for (int idx = tid; idx < 2 * P * bw; idx += nt) {
-            const int rr = idx / bw, x = idx - rr * bw;
-            const int r = 2 * pair0 + rr;
-            if (r >= bh) continue;
+        for (int rr = 0; rr < 2 * P; rr++) {
+          const int r = 2 * pair0 + rr;
+          if (r >= bh) break;
+          for (int x = tid; x < bw; x += nt) {
             const long long li = (long long)(tb.y0 + r) * m.rw + tb.x0 + x;
             float score = 1.f;
             if (!flat) {
@@ -1115,6 +1127,7 @@ __global__ void __launch_bounds__(256) k_inv_rows(InvArgs a) {
             }
             if (map) map[li] = score;
             ext_add(e, score, li);
+          }
         }
     }
     __syncthreads();
@@ -1762,8 +1775,16 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
     ProfScope ps(mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv"), st);
     if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
-        set_smem(k_cols_even, smem);
-        k_cols_even<<<grid, kThreads, smem, st>>>(a);
+        if (mode == 0) {
+            set_smem(k_cols_even<0>, smem);
+            k_cols_even<0><<<grid, kThreads, smem, st>>>(a);
+        } else if (mode == 1) {
+            set_smem(k_cols_even<1>, smem);
+            k_cols_even<1><<<grid, kThreads, smem, st>>>(a);
+        } else {
+            set_smem(k_cols_even<2>, smem);
+            k_cols_even<2><<<grid, kThreads, smem, st>>>(a);
+        }
     } else {
         set_smem(k_cols, smem);
         k_cols<<<grid, kThreads, smem, st>>>(a);
