@@ -489,6 +489,159 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind):
             "alg_bytes_per_launch": v["alg_bytes"], "kernels": kernels}
 
 
+def run_gpu_secondary(args):
+    """Secondary workloads (not the default line): 'fleet' = Fleet.FindAll
+    of 256 templates on a 2560x1440 RGBA frame, 'gray' = MatchGray
+    640x480 / 64x48, 'map' = MatchMap gray 3840x2160 / 256x256."""
+    import ctypes as C
+    import torch
+    import cvmatch_gb300 as cvm
+    import oracle
+
+    dev = torch.device("cuda", 0)
+    L = cvm.lib()
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    if args.workload == "fleet":
+        frame, tpls, _ = scene_c4(count=args.templates)
+        ms = [cvm.NewMatcher(t) for t in tpls]
+        fleet = cvm.NewFleet(*ms)
+        n = len(ms)
+        H, W = frame.shape[:2]
+        mpx = n * W * H / 1e6
+        d_frame = torch.from_numpy(frame).to(dev)
+        d_out = torch.zeros(6 * n, dtype=torch.int32, device=dev)
+
+        def step_dev():
+            fleet.find_all_device(d_frame.data_ptr(), frame.strides[0], W, H, d_out.data_ptr(), sh)
+
+        hp = L.cvm_host_alloc(frame.nbytes)
+        hframe = np.ctypeslib.as_array((C.c_uint8 * frame.nbytes).from_address(hp)).reshape(frame.shape)
+        hframe[:] = frame
+        outs = (cvm._CResult * n)()
+
+        def step_e2e():
+            rc = L.cvm_fleet_find_all(fleet._h, hp, frame.strides[0], W, H, outs)
+            assert rc == 0
+
+        h2d, d2h = frame.nbytes, 24 * n
+        cfg = {"workload": f"Fleet.FindAll, {n} RGBA templates 16..192 x 16..128 on a 2560x1440 RGBA frame",
+               "templates": n, "parent": [W, H]}
+
+        def cpu_sample():
+            k = 4
+            t0 = time.perf_counter()
+            oracle.fleet_find_all(tpls[:k], frame, threads=1)
+            dt = time.perf_counter() - t0
+            return {"value": k * W * H / 1e6 / dt, "unit": "template*Mpx/s", "cores": 1, "kind": "port",
+                    "sample": f"the first {k} templates of the fleet, 1 thread"}
+    elif args.workload == "gray":
+        frame, tpl, _ = scene_c1()
+        g, gt = oracle.rgba_to_gray(frame), oracle.rgba_to_gray(tpl)
+        H, W = g.shape
+        th, tw = gt.shape
+        mpx = W * H / 1e6
+        d_img = torch.from_numpy(g).to(dev)
+        d_tpl = torch.from_numpy(gt).to(dev)
+        d_out = torch.zeros(6, dtype=torch.int32, device=dev)
+        L.cvm_match_u8_device.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+
+        def step_dev():
+            assert L.cvm_match_u8_device(d_img.data_ptr(), W, W, H, d_tpl.data_ptr(), tw, tw, th, 1, 1, None,
+                                         d_out.data_ptr(), sh) == 0
+
+        res = cvm._CResult()
+
+        def step_e2e():
+            assert L.cvm_match_gray_rgba(frame.ctypes.data, frame.strides[0], frame.shape[1], frame.shape[0],
+                                         tpl.ctypes.data, tpl.strides[0], tpl.shape[1], tpl.shape[0],
+                                         C.byref(res)) == 0
+
+        h2d, d2h = frame.nbytes + tpl.nbytes, 24
+        cfg = {"workload": "MatchGray 640x480 (from RGBA), template 64x48", "parent": [W, H], "templates": 1}
+
+        def cpu_sample():
+            t0 = time.perf_counter()
+            reps = 0
+            while time.perf_counter() - t0 < 5:
+                oracle.match_u8(g, gt, 1, threads=1, want_map=False)
+                reps += 1
+            return {"value": reps * mpx / (time.perf_counter() - t0), "unit": "template*Mpx/s", "cores": 1,
+                    "kind": "port", "sample": f"{reps} MatchGray calls, 1 thread"}
+    else:  # map
+        g, tpl, _ = scene_c3()
+        H, W = g.shape
+        th, tw = tpl.shape
+        mpx = W * H / 1e6
+        rw, rh = W - tw + 1, H - th + 1
+        d_img = torch.from_numpy(g).to(dev)
+        d_tpl = torch.from_numpy(tpl).to(dev)
+        d_map = torch.empty((rh, rw), dtype=torch.float32, device=dev)
+        d_out = torch.zeros(6, dtype=torch.int32, device=dev)
+        L.cvm_match_u8_device.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+
+        def step_dev():
+            assert L.cvm_match_u8_device(d_img.data_ptr(), W, W, H, d_tpl.data_ptr(), tw, tw, th, 1, 1,
+                                         d_map.data_ptr(), d_out.data_ptr(), sh) == 0
+
+        hmap = np.empty((rh, rw), np.float32)
+        res = cvm._CResult()
+        L.cvm_match_u8.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                   C.c_int, C.c_int, C.c_void_p, C.POINTER(cvm._CResult)]
+
+        def step_e2e():
+            assert L.cvm_match_u8(g.ctypes.data, W, W, H, tpl.ctypes.data, tw, tw, th, 1, 1, hmap.ctypes.data,
+                                  C.byref(res)) == 0
+
+        h2d, d2h = g.nbytes + tpl.nbytes, hmap.nbytes + 24
+        cfg = {"workload": "MatchMap gray 3840x2160, template 256x256, full float32 map returned",
+               "parent": [W, H], "templates": 1}
+
+        def cpu_sample():
+            t0 = time.perf_counter()
+            oracle.match_u8(g, tpl, 1, threads=1, want_map=True)
+            return {"value": mpx / (time.perf_counter() - t0), "unit": "template*Mpx/s", "cores": 1, "kind": "port",
+                    "sample": "one MatchMap call, 1 thread"}
+
+    for _ in range(max(3, args.warmup)):
+        step_dev()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    l0 = L.cvm_launch_count()
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        step_dev()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    launches = (L.cvm_launch_count() - l0) // args.steps
+    ms = float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)]))
+    for _ in range(2):
+        step_e2e()
+    et = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        et.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * float(np.mean(et))
+    line = {"metric": "template*Mpx/s", "value": mpx / (ms / 1e3), "unit": "template*Mpx/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "e2e": {"value": mpx / (e2e_ms / 1e3), "unit": "template*Mpx/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+            "gpu_launches": int(launches), "secondary": True}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,11 +649,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map"],
+                    help="match (default, the reported line) or a secondary configuration")
+    ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "match":
+        return run_gpu_secondary(args)
     return run_gpu(args)
 
 

@@ -631,7 +631,7 @@ struct cvm_fleet {
 namespace {
 
 // Budget for one wave of member tails' column-pass output.
-constexpr size_t kWaveBytes = size_t(512) << 20;
+constexpr size_t kWaveBytes = size_t(4) << 30;
 
 // Per parent size: every bucket's plan and every member's spectrum on its
 // bucket's plan (buildGeom, fleet.go:337-390), plus the device member
@@ -724,20 +724,24 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             per += bg.memberScratch[c] * sizeof(float2);
         }
         const size_t lanesPer = (size_t)bg.rwMax * bg.rhMax;
-        const size_t hPer = (size_t)(cnS + 1) * ph * bg.sg.hp;
         const int nparts = bg.nparts;
-        per += lanesPer * sizeof(float2) + hPer * sizeof(unsigned int);
+        per += lanesPer * sizeof(float2);
         frameBytes = std::max(frameBytes, fb);
         partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
         w = std::min<int>(w, (int)bg.members.size());
         wave[b] = w;
-        size_t wb = Arena::bytes((size_t)w * lanesPer, sizeof(float2)) + Arena::bytes((size_t)w * hPer, sizeof(unsigned int));
+        size_t wb = Arena::bytes((size_t)w * lanesPer, sizeof(float2));
         for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));
         waveBytes = std::max(waveBytes, wb);
     }
+    // one set of row prefixes for every member (each differences it at its own width)
+    const int cnP = f->step == 4 ? 4 : 1;
+    const int hpP = (int)align_up((size_t)pw + 1, 32);
+    const size_t prefixElems = (size_t)(cnP == 4 ? 6 : cnP + 1) * ph * hpP;
     const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
-                         Arena::bytes(n, sizeof(int)) + frameBytes + partBytes + waveBytes;
+                         Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) + frameBytes +
+                         partBytes + waveBytes;
     PoolBuf buf;
     CVM_TRY(pool_alloc(buf, bytes, st));
     Arena A;
@@ -745,6 +749,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     DevParams *P = A.take<DevParams>(n);
     DevFrame *F = A.take<DevFrame>(1);
     int *counters = A.take<int>(n);
+    unsigned int *prefix = A.take<unsigned int>(prefixElems);
     char *frameBase = A.base + A.used;
     A.used += frameBytes;
     Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
@@ -755,11 +760,10 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     CVM_CUDA(cudaMemsetAsync(counters, 0, n * sizeof(int), st));
     CVM_CUDA(launch_prep(nullptr, 0, 0, 0, f->step, 0, f->step == 4 ? dParent : nullptr, pstride, pw, ph, P, n, 0, 0,
                          0, F, st));
+    CVM_CUDA(launch_row_prefix(dParent, pstride, f->step, pw, ph, cnP, prefix, hpP, st));
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
-        const size_t hPer = (size_t)(cnS + 1) * ph * bg.sg.hp;
-        unsigned int *H = nullptr;
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
         float2 *lanes = nullptr;
@@ -773,7 +777,6 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                 scratch[c] = wa.take<float2>((size_t)wave[b] * bg.memberScratch[c]);
             }
             lanes = wa.take<float2>((size_t)wave[b] * bg.rwMax * bg.rhMax);
-            H = wa.take<unsigned int>((size_t)wave[b] * hPer);
         }
         // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
         for (int c = 0; c < G.nclass; c++) {
@@ -797,8 +800,10 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         for (int w0 = 0; w0 < nm; w0 += wave[b]) {
             const int nw = std::min(wave[b], nm - w0);
             ms.first = w0;
-            CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, bg.sg, f->step == 4 ? 3 : 1,
-                                      f->step == 4 ? 4 : 1, H, hPer, st));
+            SepGrid sgP = bg.sg;
+            sgP.hp = hpP;
+            CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
+                                      f->step == 4 ? 4 : 1, prefix, 0, st, 1, &cnP));
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
             for (int c = 0; c < G.nclass; c++)

@@ -172,9 +172,19 @@ struct SepGrid {
     int BV, ncx, nby, hp;
 };
 SepGrid sep_grid(int rwMax, int rhMax);
+// sharedPrefix: H holds launch_row_prefix's shared planes (no per-member
+// k_hsum; each member differences the prefix at its own width).
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
-                             unsigned int *H, size_t slotStride, cudaStream_t st);
+                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix = 0,
+                             const int *prefixCnHost = nullptr);
+// Exclusive row prefixes P_q(x, r) (x = 0..iw), u32 modular, planes
+// [q][ih][hp] with hp >= iw + 1: the first cnP channel sums, the squares of
+// the first min(cnP,3) channels, and for cnP == 4 the alpha squares
+// (cnP + 1 planes, 6 when cnP == 4).  *prefixCnHost of launch_sep_stats
+// must be this cnP.
+cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, int iw, int ih, int cnP,
+                              unsigned int *P, int hp, cudaStream_t st);
 
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).

@@ -27,6 +27,7 @@
 //   k_shrink_gather   shrinkInto (impl.go:591-610)
 #include <cfloat>
 #include <cstdio>
+#include <cstring>
 #include <climits>
 #include <cstdint>
 
@@ -1510,6 +1511,81 @@ __device__ __forceinline__ void hsum_row(const HsumArgs &a, int slot, int tw, in
     }
 }
 
+// Exclusive row prefixes of one image row shared by every fleet member:
+// planes 0..CN-1 the channel sums, plane CN the squares of the first
+// min(CN,3) channels and, for CN == 4, plane 5 the alpha squares (a cn=3
+// member's squared sum excludes alpha, a cn=4 member's includes it).
+// Each member's window sum is then P[x+tw] - P[x] at its own width.
+template <int CN>
+__global__ void __launch_bounds__(256) k_row_prefix(const uint8_t *__restrict__ img, long long istride, int step,
+                                                    int iw, unsigned int *P, size_t planeStride, int hp) {
+    constexpr int NQ = CN == 4 ? 6 : CN + 1;
+    extern __shared__ __align__(16) unsigned int sp[];  // [NQ][iw+1]
+    __shared__ unsigned int wsum[kThreads / 32][NQ];
+    const int r = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int ld = iw + 1;
+    const uint8_t *row = img + (long long)r * istride;
+    for (int x = tid; x < iw; x += nt) {
+        const uint8_t *p = row + (long long)x * step;
+        unsigned int q3 = 0;
+#pragma unroll
+        for (int k = 0; k < CN; k++) {
+            const unsigned int v = p[k];
+            sp[k * ld + x + 1] = v;
+            if (k < 3) q3 += v * v;
+        }
+        sp[CN * ld + x + 1] = q3;
+        if (CN == 4) sp[5 * ld + x + 1] = (unsigned int)p[3] * p[3];
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) sp[q * ld] = 0u;
+    }
+    __syncthreads();
+    const int seg = ((iw + nt - 1) / nt) | 1;
+    const int c0 = 1 + tid * seg, c1 = min(iw + 1, c0 + seg);
+    unsigned int tot[NQ], inc[NQ], run[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) tot[q] = 0u;
+    for (int c = c0; c < c1; c++) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) tot[q] += sp[q * ld + c];
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; q++) inc[q] = tot[q];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const unsigned int u = __shfl_up_sync(0xffffffffu, inc[q], o);
+            if (lane >= o) inc[q] += u;
+        }
+    }
+    if (lane == 31) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) wsum[warp][q] = inc[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        run[q] = inc[q] - tot[q];
+        for (int w = 0; w < warp; w++) run[q] += wsum[w][q];
+    }
+    for (int c = c0; c < c1; c++) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            run[q] += sp[q * ld + c];
+            sp[q * ld + c] = run[q];
+        }
+    }
+    __syncthreads();
+    unsigned int *out = P + (size_t)r * hp;
+    for (int x = tid; x <= iw; x += nt) {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) out[(size_t)q * planeStride + x] = sp[q * ld + x];
+    }
+}
+
 // One launch covers members of either channel count of a mode (colour: 3
 // or 4, chosen on the device; gray: 1).
 template <int CNA, int CNB>
@@ -1546,9 +1622,11 @@ struct VstatArgs {
     int hp;
     MemberSet ms;
     int BV;
+    int fromPrefix;   // H holds the shared row prefix: window sum = P[x+tw] - P[x]
+    int prefixCn;     // channel count the shared prefix was built for
 };
 
-template <int CN>
+template <int CN, bool PRE>
 __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &m, const DevParams &Pm) {
     const int slot = blockIdx.z;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1556,10 +1634,21 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     if (x >= m.rw || Y0 >= m.rh) return;
     const int Bv = min(a.BV, m.rh - Y0);
     const int th = m.th;
-    const unsigned int *H = a.H + (size_t)slot * a.slotStride + x;
+    const unsigned int *H = a.H + (PRE ? 0 : (size_t)slot * a.slotStride) + x;
+    const int tw = PRE ? m.tw : 0;  // second tap of a prefix difference
     const size_t ps = a.planeStride;
     const int hp = a.hp;
     float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride + x;
+    auto tap = [&](const unsigned int *h, int q) { return __ldg(h + q * ps + tw) - __ldg(h + q * ps); };
+    // squares: plane CN of the member's own planes; in the shared colour
+    // prefix, plane 4 (RGB squares) plus plane 5 (alpha squares) for cn = 4
+    const int pcn = a.prefixCn;
+    auto hval = [&](const unsigned int *h, int q) -> unsigned int {
+        if (!PRE) return __ldg(h + q * ps);
+        if (q < CN) return tap(h, q);
+        if (pcn == 4) return CN == 4 ? tap(h, 4) + tap(h, 5) : tap(h, 4);
+        return tap(h, pcn);
+    };
     unsigned int s[CN];
     unsigned long long q = 0;
 #pragma unroll
@@ -1568,8 +1657,8 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     for (int dy = 0; dy < th; dy++) {
         const unsigned int *h = H + (size_t)(Y0 + dy) * hp;
 #pragma unroll
-        for (int k = 0; k < CN; k++) s[k] += __ldg(h + k * ps);
-        q += __ldg(h + CN * ps);
+        for (int k = 0; k < CN; k++) s[k] += hval(h, k);
+        q += hval(h, CN);
     }
     const unsigned long long area = (unsigned long long)m.tw * th;
     const unsigned int t0 = (unsigned int)Pm.tsum[0], t1 = (unsigned int)Pm.tsum[1];
@@ -1582,8 +1671,8 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             const unsigned int *hi = H + (size_t)(y + th) * hp, *ho = H + (size_t)y * hp;
 #pragma unroll
             for (int k = 0; k <= CN; k++) {
-                hin[k] = __ldg(hi + k * ps);
-                hout[k] = __ldg(ho + k * ps);
+                hin[k] = hval(hi, k);
+                hout[k] = hval(ho, k);
             }
         }
         unsigned long long cross = (unsigned long long)s[0] * t0, sq = (unsigned long long)s[0] * s[0];
@@ -1619,15 +1708,15 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     }
 }
 
-template <int CNA, int CNB>
+template <int CNA, int CNB, bool PRE>
 __global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
     const DevMember &m = member_of(a.ms, blockIdx.z);
     const DevParams &Pm = a.ms.params[m.pIdx];
     if (Pm.flat) return;
     if (Pm.cn == CNA)
-        vstat_cols<CNA>(a, m, Pm);
+        vstat_cols<CNA, PRE>(a, m, Pm);
     else if (CNB != CNA && Pm.cn == CNB)
-        vstat_cols<CNB>(a, m, Pm);
+        vstat_cols<CNB, PRE>(a, m, Pm);
 }
 
 // Small host values to device memory through kernel arguments.
@@ -1741,11 +1830,15 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     const int pairs = (maxRows + 1) / 2;
     dim3 grid((pairs + P - 1) / P, fc.ntiles);
     const size_t smem = (size_t)P * group * padded_len(fc.n) * sizeof(float2);
+    // as many threads as a radix-16 pass has units (a multiple of 32 in
+    // 64..256), so no thread idles in those passes
+    int threads = P * group * (fc.n >= 16 ? fc.n / 16 : 1);
+    threads = threads < 64 ? 64 : (threads > kThreads ? kThreads : (threads + 31) / 32 * 32);
     set_smem(k_fwd_rows, smem);
     ProfScope ps("k_fwd_rows", st);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
-        k_fwd_rows<<<grid, kThreads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
-                                                  spec, cnS, P);
+        k_fwd_rows<<<grid, threads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
+                                                 spec, cnS, P);
         count_launches(1);
     }
     return cudaGetLastError();
@@ -1794,7 +1887,9 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
 }
 
 int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta) {
-    int P = 2048 / fc.n;
+    // 4096 elements per CTA: the radix-16 passes (n/16 units per line) keep
+    // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM)
+    int P = 4096 / fc.n;
     if (P < 1) P = 1;
     // A tile emits at most dftH rows (a fleet member's last band extends to
     // its own result edge, still inside the loaded rows <= dftH).
@@ -1905,7 +2000,8 @@ SepGrid sep_grid(int rwMax, int rhMax) {
 
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
-                             unsigned int *H, size_t slotStride, cudaStream_t st) {
+                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix,
+                             const int *prefixCnHost) {
     HsumArgs h;
     h.img = img;
     h.istride = istride;
@@ -1923,6 +2019,8 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     h.params = ms.params;
     h.pIdx = ms.solo.pIdx;
     VstatArgs v;
+    v.fromPrefix = sharedPrefix;
+    v.prefixCn = prefixCnHost ? *prefixCnHost : 0;
     v.H = H;
     v.planeStride = h.planeStride;
     v.slotStride = slotStride;
@@ -1931,7 +2029,7 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     v.BV = sg.BV;
     const size_t smem = (size_t)(cnMax + 1) * (iw + 1) * sizeof(unsigned int);
     dim3 gh(ih, 1, nmembers), gv(sg.ncx, sg.nby, nmembers);
-    {
+    if (!sharedPrefix) {
         ProfScope ps("k_hsum", st);
         if (cnMax == 1) {
             set_smem(k_hsum<1, 1>, smem);
@@ -1949,16 +2047,43 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     }
     {
         ProfScope ps("k_vstats", st);
-        if (cnMax == 1)
-            k_vstats<1, 1><<<gv, kThreads, 0, st>>>(v);
-        else if (cnMax == 2)
-            k_vstats<2, 2><<<gv, kThreads, 0, st>>>(v);
-        else if (cnMin == 3)
-            k_vstats<3, 4><<<gv, kThreads, 0, st>>>(v);
-        else
-            k_vstats<4, 4><<<gv, kThreads, 0, st>>>(v);
+        if (sharedPrefix) {
+            if (cnMax == 1)
+                k_vstats<1, 1, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMax == 2)
+                k_vstats<2, 2, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMin == 3)
+                k_vstats<3, 4, true><<<gv, kThreads, 0, st>>>(v);
+            else
+                k_vstats<4, 4, true><<<gv, kThreads, 0, st>>>(v);
+        } else {
+            if (cnMax == 1)
+                k_vstats<1, 1, false><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMax == 2)
+                k_vstats<2, 2, false><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMin == 3)
+                k_vstats<3, 4, false><<<gv, kThreads, 0, st>>>(v);
+            else
+                k_vstats<4, 4, false><<<gv, kThreads, 0, st>>>(v);
+        }
     }
-    count_launches(2);
+    count_launches(sharedPrefix ? 1 : 2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, int iw, int ih, int cnP,
+                              unsigned int *P, int hp, cudaStream_t st) {
+    const int nq = cnP == 4 ? 6 : cnP + 1;
+    const size_t smem = (size_t)nq * (iw + 1) * sizeof(unsigned int);
+    const size_t planeStride = (size_t)ih * hp;
+    ProfScope ps("k_row_prefix", st);
+    switch (cnP) {
+        case 1: set_smem(k_row_prefix<1>, smem); k_row_prefix<1><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
+        case 2: set_smem(k_row_prefix<2>, smem); k_row_prefix<2><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
+        case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
+        default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
+    }
+    count_launches(1);
     return cudaGetLastError();
 }
 
