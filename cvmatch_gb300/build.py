@@ -34,7 +34,7 @@ def _cuda_home() -> str:
 
 def _sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
-                  if f.endswith((".cu", ".cpp", ".h")))
+                  if f.endswith((".cu", ".cpp", ".h", ".cuh")))
 
 
 def _stale() -> bool:

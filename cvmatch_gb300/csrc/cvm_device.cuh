@@ -1,0 +1,222 @@
+// cvm_device.cuh -- device helpers shared by the kernel translation units
+// (cvm_kernels.cu: the generic-size kernels; cvm_rows.cu: the row
+// transforms specialised on the transform length).
+//
+// The butterfly and complex multiply are the reference's pinned op
+// sequence (radix4.go:17-32, 80-149); every unit built on them keeps it.
+#pragma once
+
+#include <cfloat>
+#include <climits>
+#include <cstdint>
+
+#include "cvm_internal.h"
+
+namespace cvm {
+
+namespace prof {
+int begin(const char *name, cudaStream_t st);
+void end(int idx, cudaStream_t st);
+}  // namespace prof
+
+// Brackets one launch with the optional per-kernel event timing.
+struct ProfScope {
+    int idx;
+    cudaStream_t st;
+    ProfScope(const char *name, cudaStream_t s) : idx(prof::begin(name, s)), st(s) {}
+    ~ProfScope() { prof::end(idx, st); }
+};
+
+struct TileBox {
+    int x0, y0, bw, bh, loadW, loadH;
+};
+
+struct Ext {
+    float minV, maxV;
+    long long minI, maxI;
+};
+
+struct InvArgs {
+    TileGeom g;
+    FftClass fc;
+    int cls, cnS;
+    MemberSet ms;
+    int pairsPerCta;
+    int partOffset;   // partial records of the classes before this one
+    int nparts;       // partial records per member (all classes)
+    Partial *partials;
+    int *counters;    // per member params index
+    cvm_result *out;
+};
+
+// Arguments of the forward-rows kernels (forwardRowPair, impl.go:301-344).
+struct FwdRowsArgs {
+    const uint8_t *img;
+    long long istride;
+    int step, chanCount;
+    const int *cnDev;        // device-side channel count (nullptr: chanCount)
+    int chanFirst, chanGroup;
+    TileGeom g;
+    FftClass fc;
+    float2 *spec;
+    int cnS, pairsPerCta;
+    int pix32;               // 4-byte pixels readable as aligned 32-bit words
+};
+
+// The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).
+bool rows_fixed_length(int log2n);
+void launch_fwd_rows_fixed(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st);
+void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st);
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int brev_bits(int x, int log2n) {
+    return log2n == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - log2n));
+}
+
+// mulPlain (radix4.go:80-85): four single-rounded products, two sums.
+__device__ __forceinline__ float2 cmul_plain(float2 v, float2 w) {
+    float a = __fmul_rn(v.x, w.x), b = __fmul_rn(v.y, w.y);
+    float c = __fmul_rn(v.x, w.y), d = __fmul_rn(v.y, w.x);
+    return make_float2(__fsub_rn(a, b), __fadd_rn(c, d));
+}
+
+// One radix-4 butterfly (radix4.go:126-147); pa/pc/pb/pd are rows r, r+h,
+// r+2h, r+3h.  The inverse conjugates the twiddles and flips the rotation.
+template <bool INV>
+__device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2 *pd, float2 bw,
+                                      float2 cw, float2 dw) {
+    if (INV) {
+        bw.y = -bw.y;
+        cw.y = -cw.y;
+        dw.y = -dw.y;
+    }
+    const float2 av = *pa;
+    const float2 tb = cmul_plain(*pb, bw);
+    const float2 tc = cmul_plain(*pc, cw);
+    const float2 td = cmul_plain(*pd, dw);
+    const float s0x = __fadd_rn(av.x, tc.x), s0y = __fadd_rn(av.y, tc.y);
+    const float s1x = __fsub_rn(av.x, tc.x), s1y = __fsub_rn(av.y, tc.y);
+    const float s2x = __fadd_rn(tb.x, td.x), s2y = __fadd_rn(tb.y, td.y);
+    const float s3x = __fsub_rn(tb.x, td.x), s3y = __fsub_rn(tb.y, td.y);
+    float rr, ri;
+    if (INV) {
+        rr = -s3y;
+        ri = s3x;
+    } else {
+        rr = s3y;
+        ri = -s3x;
+    }
+    *pa = make_float2(__fadd_rn(s0x, s2x), __fadd_rn(s0y, s2y));
+    *pc = make_float2(__fadd_rn(s1x, rr), __fadd_rn(s1y, ri));
+    *pb = make_float2(__fsub_rn(s0x, s2x), __fsub_rn(s0y, s2y));
+    *pd = make_float2(__fsub_rn(s1x, rr), __fsub_rn(s1y, ri));
+}
+
+// Padded shared-memory line layout: one spare slot every 16 elements keeps
+// the strided pass accesses free of bank conflicts.
+__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int padded_len(int n) { return n + (n >> 4) + 1; }
+
+
+__device__ __forceinline__ TileBox tile_box(const TileGeom &g, int tile) {
+    TileBox b;
+    const int tx = tile % g.ntx, ty = tile / g.ntx;
+    b.x0 = tx * g.blockW;
+    b.y0 = ty * g.blockH;
+    b.bw = min(g.blockW, g.rwT - b.x0);
+    b.bh = min(g.blockH, g.rhT - b.y0);
+    b.loadW = b.bw + g.twL - 1;
+    b.loadH = b.bh + g.thL - 1;
+    return b;
+}
+
+__device__ __forceinline__ const DevMember &member_of(const MemberSet &ms, int slot) {
+    return ms.table ? ms.table[ms.first + slot] : ms.solo;
+}
+
+// ------------------------------------------------ first-occurrence extrema
+
+
+__device__ __forceinline__ void ext_init(Ext &e) {
+    e.minV = FLT_MAX;
+    e.maxV = -FLT_MAX;
+    e.minI = LLONG_MAX;
+    e.maxI = LLONG_MAX;
+}
+
+// First occurrence in raster order with strict compares (impl.go:1023-1047,
+// 1104-1112): a smaller value, or an equal value at a smaller index.
+__device__ __forceinline__ void ext_add(Ext &e, float v, long long i) {
+    if (v < e.minV || (v == e.minV && i < e.minI)) {
+        e.minV = v;
+        e.minI = i;
+    }
+    if (v > e.maxV || (v == e.maxV && i < e.maxI)) {
+        e.maxV = v;
+        e.maxI = i;
+    }
+}
+
+__device__ __forceinline__ void ext_merge(Ext &e, const Ext &o) {
+    if (o.minV < e.minV || (o.minV == e.minV && o.minI < e.minI)) {
+        e.minV = o.minV;
+        e.minI = o.minI;
+    }
+    if (o.maxV > e.maxV || (o.maxV == e.maxV && o.maxI < e.maxI)) {
+        e.maxV = o.maxV;
+        e.maxI = o.maxI;
+    }
+}
+
+__device__ void ext_block_reduce(Ext &e, Ext *sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        Ext t;
+        t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
+        t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
+        t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
+        t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
+        ext_merge(e, t);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[warp] = e;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        if (lane < nw)
+            e = sh[lane];
+        else
+            ext_init(e);
+        for (int o = 16; o > 0; o >>= 1) {
+            Ext t;
+            t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
+            t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
+            t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
+            t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
+            ext_merge(e, t);
+        }
+    }
+}
+
+__device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
+    cvm_result r;
+    r.min_v = e.minV;
+    r.max_v = e.maxV;
+    r.min_x = (int32_t)(e.minI % rw);
+    r.min_y = (int32_t)(e.minI / rw);
+    r.max_x = (int32_t)(e.maxI % rw);
+    r.max_y = (int32_t)(e.maxI / rw);
+    *out = r;
+}
+
+
+template <typename K>
+void set_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+}  // namespace cvm

@@ -35,7 +35,7 @@
 #include <string>
 #include <vector>
 
-#include "cvm_internal.h"
+#include "cvm_device.cuh"
 
 namespace cvm {
 
@@ -97,59 +97,9 @@ void collect() {
 }
 }  // namespace prof
 
-struct ProfScope {
-    int idx;
-    cudaStream_t st;
-    ProfScope(const char *name, cudaStream_t s) : idx(prof::begin(name, s)), st(s) {}
-    ~ProfScope() { prof::end(idx, st); }
-};
 
 namespace {
 
-constexpr int kThreads = 256;
-
-__device__ __forceinline__ int brev_bits(int x, int log2n) {
-    return log2n == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - log2n));
-}
-
-// mulPlain (radix4.go:80-85): four single-rounded products, two sums.
-__device__ __forceinline__ float2 cmul_plain(float2 v, float2 w) {
-    float a = __fmul_rn(v.x, w.x), b = __fmul_rn(v.y, w.y);
-    float c = __fmul_rn(v.x, w.y), d = __fmul_rn(v.y, w.x);
-    return make_float2(__fsub_rn(a, b), __fadd_rn(c, d));
-}
-
-// One radix-4 butterfly (radix4.go:126-147); pa/pc/pb/pd are rows r, r+h,
-// r+2h, r+3h.  The inverse conjugates the twiddles and flips the rotation.
-template <bool INV>
-__device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2 *pd, float2 bw,
-                                      float2 cw, float2 dw) {
-    if (INV) {
-        bw.y = -bw.y;
-        cw.y = -cw.y;
-        dw.y = -dw.y;
-    }
-    const float2 av = *pa;
-    const float2 tb = cmul_plain(*pb, bw);
-    const float2 tc = cmul_plain(*pc, cw);
-    const float2 td = cmul_plain(*pd, dw);
-    const float s0x = __fadd_rn(av.x, tc.x), s0y = __fadd_rn(av.y, tc.y);
-    const float s1x = __fsub_rn(av.x, tc.x), s1y = __fsub_rn(av.y, tc.y);
-    const float s2x = __fadd_rn(tb.x, td.x), s2y = __fadd_rn(tb.y, td.y);
-    const float s3x = __fsub_rn(tb.x, td.x), s3y = __fsub_rn(tb.y, td.y);
-    float rr, ri;
-    if (INV) {
-        rr = -s3y;
-        ri = s3x;
-    } else {
-        rr = s3y;
-        ri = -s3x;
-    }
-    *pa = make_float2(__fadd_rn(s0x, s2x), __fadd_rn(s0y, s2y));
-    *pc = make_float2(__fadd_rn(s1x, rr), __fadd_rn(s1y, ri));
-    *pb = make_float2(__fsub_rn(s0x, s2x), __fsub_rn(s0y, s2y));
-    *pd = make_float2(__fsub_rn(s1x, rr), __fsub_rn(s1y, ri));
-}
 
 // ------------------------------------------------- radix-4 cascade passes
 // The reference cascade (fftR4Scalar, radix4.go:106-149) on bit-reversed
@@ -284,10 +234,6 @@ __device__ void fft_cascade(float2 *s, int n, int log2n, int lines, const LineAd
     }
 }
 
-// Padded shared-memory line layout: one spare slot every 16 elements keeps
-// the strided pass accesses free of bank conflicts.
-__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
-__host__ __device__ __forceinline__ int padded_len(int n) { return n + (n >> 4) + 1; }
 
 // The column twin (colsR4Go, radix4cols.go:35-125) on a [n x SC] strip in
 // shared memory, element (row r, column c) at s[r*SC + c]; RMAP conjugates
@@ -301,21 +247,6 @@ __device__ void fft_cols(float2 *s, int n, int log2n, int SC, int logSC, const f
     fft_cascade<INV, true>(s, n, log2n, SC, la, tri);
 }
 
-struct TileBox {
-    int x0, y0, bw, bh, loadW, loadH;
-};
-
-__device__ __forceinline__ TileBox tile_box(const TileGeom &g, int tile) {
-    TileBox b;
-    const int tx = tile % g.ntx, ty = tile / g.ntx;
-    b.x0 = tx * g.blockW;
-    b.y0 = ty * g.blockH;
-    b.bw = min(g.blockW, g.rwT - b.x0);
-    b.bh = min(g.blockH, g.rhT - b.y0);
-    b.loadW = b.bw + g.twL - 1;
-    b.loadH = b.bh + g.thL - 1;
-    return b;
-}
 
 // ------------------------------------------------------------ gray/alpha
 
@@ -537,9 +468,6 @@ struct ColsArgs {
     int SC, logSC;
 };
 
-__device__ __forceinline__ const DevMember &member_of(const MemberSet &ms, int slot) {
-    return ms.table ? ms.table[ms.first + slot] : ms.solo;
-}
 
 // Column pass over one [dftH x SC] strip of one (member, tile, channel).
 __global__ void k_cols(ColsArgs a) {
@@ -932,94 +860,7 @@ __device__ __forceinline__ float norm_one(float num, float lane0, float idiff, u
     return 0.f;
 }
 
-struct Ext {
-    float minV, maxV;
-    long long minI, maxI;
-};
 
-__device__ __forceinline__ void ext_init(Ext &e) {
-    e.minV = FLT_MAX;
-    e.maxV = -FLT_MAX;
-    e.minI = LLONG_MAX;
-    e.maxI = LLONG_MAX;
-}
-
-// First occurrence in raster order with strict compares (impl.go:1023-1047,
-// 1104-1112): a smaller value, or an equal value at a smaller index.
-__device__ __forceinline__ void ext_add(Ext &e, float v, long long i) {
-    if (v < e.minV || (v == e.minV && i < e.minI)) {
-        e.minV = v;
-        e.minI = i;
-    }
-    if (v > e.maxV || (v == e.maxV && i < e.maxI)) {
-        e.maxV = v;
-        e.maxI = i;
-    }
-}
-
-__device__ __forceinline__ void ext_merge(Ext &e, const Ext &o) {
-    if (o.minV < e.minV || (o.minV == e.minV && o.minI < e.minI)) {
-        e.minV = o.minV;
-        e.minI = o.minI;
-    }
-    if (o.maxV > e.maxV || (o.maxV == e.maxV && o.maxI < e.maxI)) {
-        e.maxV = o.maxV;
-        e.maxI = o.maxI;
-    }
-}
-
-__device__ void ext_block_reduce(Ext &e, Ext *sh) {
-    for (int o = 16; o > 0; o >>= 1) {
-        Ext t;
-        t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
-        t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
-        t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
-        t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
-        ext_merge(e, t);
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) sh[warp] = e;
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-        if (lane < nw)
-            e = sh[lane];
-        else
-            ext_init(e);
-        for (int o = 16; o > 0; o >>= 1) {
-            Ext t;
-            t.minV = __shfl_down_sync(0xffffffffu, e.minV, o);
-            t.maxV = __shfl_down_sync(0xffffffffu, e.maxV, o);
-            t.minI = __shfl_down_sync(0xffffffffu, e.minI, o);
-            t.maxI = __shfl_down_sync(0xffffffffu, e.maxI, o);
-            ext_merge(e, t);
-        }
-    }
-}
-
-__device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
-    cvm_result r;
-    r.min_v = e.minV;
-    r.max_v = e.maxV;
-    r.min_x = (int32_t)(e.minI % rw);
-    r.min_y = (int32_t)(e.minI / rw);
-    r.max_x = (int32_t)(e.maxI % rw);
-    r.max_y = (int32_t)(e.maxI / rw);
-    *out = r;
-}
-
-struct InvArgs {
-    TileGeom g;
-    FftClass fc;
-    int cls, cnS;
-    MemberSet ms;
-    int pairsPerCta;
-    int partOffset;   // partial records of the classes before this one
-    int nparts;       // partial records per member (all classes)
-    Partial *partials;
-    int *counters;    // per member params index
-    cvm_result *out;
-};
 
 // inverseRowPair (impl.go:394-444) for P row pairs of one (member, tile):
 // combine, inverse row transform, the channels accumulated in channel order
@@ -1745,11 +1586,6 @@ __global__ void k_shrink_gather(const float2 *__restrict__ src, int dftH, float2
     }
 }
 
-template <typename K>
-void set_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 int ilog2i(int v) {
     int l = 0;
@@ -1834,8 +1670,29 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     // 64..256), so no thread idles in those passes
     int threads = P * group * (fc.n >= 16 ? fc.n / 16 : 1);
     threads = threads < 64 ? 64 : (threads > kThreads ? kThreads : (threads + 31) / 32 * 32);
-    set_smem(k_fwd_rows, smem);
     ProfScope ps("k_fwd_rows", st);
+    if (rows_fixed_length(fc.log2n)) {
+        FwdRowsArgs a;
+        a.img = img;
+        a.istride = istride;
+        a.step = step;
+        a.chanCount = chanCount;
+        a.cnDev = cnDev;
+        a.chanGroup = group;
+        a.g = g;
+        a.fc = fc;
+        a.spec = spec;
+        a.cnS = cnS;
+        a.pairsPerCta = P;
+        a.pix32 = step == 4 && (reinterpret_cast<uintptr_t>(img) & 3) == 0 && (istride & 3) == 0;
+        for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
+            a.chanFirst = c0;
+            launch_fwd_rows_fixed(a, grid, threads, smem, st);
+            count_launches(1);
+        }
+        return cudaGetLastError();
+    }
+    set_smem(k_fwd_rows, smem);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
         k_fwd_rows<<<grid, threads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
                                                  spec, cnS, P);
@@ -1917,9 +1774,13 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.out = out;
     dim3 grid(ctas, fc.ntiles, nmembers);
     const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + 2 * fc.n * sizeof(float));
-    set_smem(k_inv_rows, smem);
     ProfScope ps("k_inv_rows", st);
-    k_inv_rows<<<grid, kThreads, smem, st>>>(a);
+    if (rows_fixed_length(fc.log2n)) {
+        launch_inv_rows_fixed(a, grid, smem, st);
+    } else {
+        set_smem(k_inv_rows, smem);
+        k_inv_rows<<<grid, kThreads, smem, st>>>(a);
+    }
     count_launches(1);
     return cudaGetLastError();
 }

@@ -1,0 +1,418 @@
+// cvm_rows.cu -- the row transforms specialised on the transform length.
+//
+// forwardRowPair (impl.go:301-344) and inverseRowPair (impl.go:394-444)
+// for dftW = 2^5 .. 2^12, one kernel instance per length.  The arithmetic
+// is exactly that of the generic-length kernels in cvm_kernels.cu (same
+// butterflies, same twiddles, same order of every rounded op); what the
+// fixed length buys is addressing: with the length and each pass's
+// quarter size known at compile time, every element of a radix unit sits
+// at a constant offset from the unit's first element in the padded
+// shared-memory line, so a unit costs one address computation instead of
+// one per element.  Other lengths run the generic kernels.
+#include "cvm_device.cuh"
+
+namespace cvm {
+namespace {
+
+// padi() of a compile-time index.
+__host__ __device__ constexpr int padc(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v >> 1); }
+
+template <int LOG2N>
+__device__ __forceinline__ int brevn(int x) {
+    return (int)(__brev((unsigned)x) >> (32 - LOG2N));
+}
+
+// Element i of a unit of quarter size H starting at base = blk*R*H + j
+// (j < H) sits at padi(base) + padc(H*i): for H >= 16 the pad counter is
+// linear in i, and for H < 16 the low bits j + (H*i mod 16) never reach 16.
+template <bool INV, int H>
+__device__ __forceinline__ void unit16(float2 *p, const float2 *__restrict__ tA, const float2 *__restrict__ tB) {
+    float2 e[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) e[i] = p[padc(H * i)];
+    const float2 a1 = __ldg(tA), a2 = __ldg(tA + H), a3 = __ldg(tA + 2 * H);
+#pragma unroll
+    for (int b = 0; b < 4; b++) bfly4<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        bfly4<INV>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
+                   __ldg(tB + 8 * H + H * q));
+#pragma unroll
+    for (int i = 0; i < 16; i++) p[padc(H * i)] = e[i];
+}
+
+template <bool INV, int H>
+__device__ __forceinline__ void unit4(float2 *p, const float2 *__restrict__ t) {
+    float2 e[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) e[i] = p[padc(H * i)];
+    bfly4<INV>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
+#pragma unroll
+    for (int i = 0; i < 4; i++) p[padc(H * i)] = e[i];
+}
+
+// The radix-2 head and the h=2 stage on 8 contiguous elements.
+template <bool INV>
+__device__ __forceinline__ void unit_head(float2 *p, const float2 *__restrict__ t) {
+    float2 e[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) e[i] = p[i];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const float2 u = e[i], v = e[i + 1];
+        e[i] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+        e[i + 1] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+        bfly4<INV>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+#pragma unroll
+    for (int i = 0; i < 8; i++) p[i] = e[i];
+}
+
+template <int LOG2N>
+struct Line {
+    static constexpr int N = 1 << LOG2N;
+    static constexpr int LD = N + (N >> 4) + 1;  // padded_len(N)
+};
+
+template <bool INV, int LOG2N, int H>
+__device__ __forceinline__ void pass16(float2 *s, int lines, const float2 *tA, const float2 *tB) {
+    constexpr int LU = LOG2N - 4, LH = ilog2c(H), LD = Line<LOG2N>::LD;
+    const int total = lines << LU;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int line = u >> LU, v = u & ((1 << LU) - 1);
+        const int j = v & (H - 1), base = ((v >> LH) << (LH + 4)) + j;
+        unit16<INV, H>(s + line * LD + padi(base), tA + j, tB + j);
+    }
+    __syncthreads();
+}
+
+template <bool INV, int LOG2N, int H>
+__device__ __forceinline__ void pass4(float2 *s, int lines, const float2 *t) {
+    constexpr int LU = LOG2N - 2, LH = ilog2c(H), LD = Line<LOG2N>::LD;
+    const int total = lines << LU;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int line = u >> LU, v = u & ((1 << LU) - 1);
+        const int j = v & (H - 1), base = ((v >> LH) << (LH + 2)) + j;
+        unit4<INV, H>(s + line * LD + padi(base), t + j);
+    }
+    __syncthreads();
+}
+
+template <bool INV, int LOG2N>
+__device__ __forceinline__ void pass_head(float2 *s, int lines, const float2 *t) {
+    constexpr int LU = LOG2N - 3, LD = Line<LOG2N>::LD;
+    const int total = lines << LU;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int line = u >> LU, v = u & ((1 << LU) - 1);
+        unit_head<INV>(s + line * LD + padi(v << 3), t);
+    }
+    __syncthreads();
+}
+
+// Stage h's twiddle table starts at h - 1 (even log2) or h - 2 (odd log2,
+// after the head's h=2 table) in the concatenated table of
+// makeTriTwiddles (radix4.go:45-73).
+template <bool INV, int LOG2N, int H>
+__device__ __forceinline__ void passes_from(float2 *s, int lines, const float2 *tri) {
+    constexpr int N = 1 << LOG2N;
+    constexpr int OFF = (LOG2N & 1) ? H - 2 : H - 1;
+    if constexpr (16 * H <= N) {
+        pass16<INV, LOG2N, H>(s, lines, tri + OFF, tri + OFF + 3 * H);
+        passes_from<INV, LOG2N, 16 * H>(s, lines, tri);
+    } else if constexpr (4 * H <= N) {
+        pass4<INV, LOG2N, H>(s, lines, tri + OFF);
+    }
+}
+
+// fftR4Scalar (radix4.go:106-149) over `lines` padded lines of length 2^LOG2N
+// in bit-reversed order; ends with a barrier.
+template <bool INV, int LOG2N>
+__device__ __forceinline__ void line_fft(float2 *s, int lines, const float2 *tri) {
+    if constexpr (LOG2N & 1) {
+        pass_head<INV, LOG2N>(s, lines, tri);
+        passes_from<INV, LOG2N, 8>(s, lines, tri);
+    } else {
+        passes_from<INV, LOG2N, 1>(s, lines, tri);
+    }
+}
+
+// floor(line / cn) for cn in 1..4 and line < 2^15.
+__device__ __forceinline__ int div_cn(int line, int cn) {
+    const int magic = cn == 1 ? 65536 : (cn == 2 ? 32768 : (cn == 3 ? 21846 : 16384));
+    return (line * magic) >> 16;
+}
+
+// ------------------------------------------------------------ forward rows
+
+template <int LOG2N>
+__global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
+    constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
+    extern __shared__ float2 smem[];
+    const FftClass &fc = a.fc;
+    const int tile = fc.tileFirst + blockIdx.y;
+    const TileBox b = tile_box(a.g, tile);
+    const int nrows = min(b.loadH, fc.dftH);
+    const int pair0 = blockIdx.x * a.pairsPerCta;
+    if (2 * pair0 >= nrows) return;
+    const int cnEff = a.cnDev ? min(*a.cnDev, a.chanCount) : a.chanCount;
+    const int cn = min(cnEff - a.chanFirst, a.chanGroup);  // channels of this launch's group
+    if (cn <= 0) return;
+    const int P = min(a.pairsPerCta, (nrows - 2 * pair0 + 1) >> 1);
+    const int lines = P * cn;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long istride = a.istride;
+    const uint8_t *img0 = a.img + (long long)(b.y0 + 2 * pair0) * istride + (long long)b.x0 * a.step;
+    // Pack rows r (real part) and r+1 (imaginary part) of every channel of
+    // the group, each pixel read once for all of them.
+    for (int it = tid; it < (P << LOG2N); it += nt) {
+        const int p = it >> LOG2N, x = it & (N - 1);
+        float va[4] = {0.f, 0.f, 0.f, 0.f}, vb[4] = {0.f, 0.f, 0.f, 0.f};
+        if (x < b.loadW) {
+            const bool two = 2 * (pair0 + p) + 1 < b.loadH;
+            const uint8_t *q = img0 + (long long)(2 * p) * istride + (long long)x * a.step;
+            if (a.pix32) {
+                const unsigned int w0 = *reinterpret_cast<const unsigned int *>(q);
+                const unsigned int w1 = two ? *reinterpret_cast<const unsigned int *>(q + istride) : 0u;
+#pragma unroll
+                for (int g = 0; g < 4; g++) {
+                    const int sh = 8 * (a.chanFirst + g);
+                    va[g] = (float)((w0 >> (sh & 31)) & 255u);
+                    vb[g] = (float)((w1 >> (sh & 31)) & 255u);
+                }
+            } else {
+#pragma unroll
+                for (int g = 0; g < 4; g++)
+                    if (g < cn) {
+                        va[g] = (float)q[a.chanFirst + g];
+                        if (two) vb[g] = (float)q[istride + a.chanFirst + g];
+                    }
+            }
+        }
+        float2 *d = smem + (p * cn) * LD + padi(brevn<LOG2N>(x));
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+            if (g < cn) d[g * LD] = make_float2(va[g], vb[g]);
+    }
+    __syncthreads();
+    line_fft<false, LOG2N>(smem, lines, fc.triW);
+    // Untangle (impl.go:331-341) into the two real-row spectra at their
+    // bit-reversed column-transform slots.
+    const int hwp = fc.hwp, log2H = fc.log2H;
+    const size_t chanStride = (size_t)fc.dftH * hwp;
+    float2 *tbase = a.spec + (size_t)(tile - fc.tileFirst) * a.cnS * chanStride;
+    auto emit = [&](int line, int kk) {
+        const int p = div_cn(line, cn), k = a.chanFirst + line - p * cn;
+        const int r = 2 * (pair0 + p);
+        const float2 *zl = smem + line * LD;
+        const float2 zk = zl[padi(kk)], zn = zl[padi((N - kk) & (N - 1))];
+        float2 *cb = tbase + (size_t)k * chanStride;
+        cb[(size_t)brev_bits(r, log2H) * hwp + kk] =
+            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
+        cb[(size_t)brev_bits(r + 1, log2H) * hwp + kk] =
+            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zn.y)), __fmul_rn(0.5f, __fsub_rn(zn.x, zk.x)));
+    };
+    for (int it = tid; it < (lines << (LOG2N - 1)); it += nt) emit(it >> (LOG2N - 1), it & (HALF - 1));
+    for (int line = tid; line < lines; line += nt) emit(line, HALF);
+}
+
+// ------------------------------------------------------------ inverse rows
+
+// The generic inverse-rows kernel (cvm_kernels.cu) with the length fixed:
+// combine (impl.go:405-413) reads each spectrum pair once and writes both
+// z[kk] and its mirror z[N-kk]; the channels accumulate in channel order;
+// the epilogue scores with the per-result (t, den) lanes and keeps
+// first-occurrence extrema merged by each member's last CTA.
+template <int LOG2N>
+__global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
+    constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
+    constexpr int XIT = (N + kThreads - 1) / kThreads;  // result columns per thread
+    extern __shared__ float2 smem[];
+    __shared__ Ext shExt[kThreads / 32];
+    __shared__ int isLast;
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.y;
+    const int tile = fc.tileFirst + tileLocal;
+    const int slot = blockIdx.z;
+    const DevMember &m = member_of(a.ms, slot);
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    const TileBox tb = tile_box(a.g, tile);
+    const int tx = tile % a.g.ntx, ty = tile / a.g.ntx;
+    const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
+    const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
+    const int pair0 = blockIdx.x * a.pairsPerCta;
+    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    const int hwp = fc.hwp, log2H = fc.log2H;
+    const int tid = threadIdx.x;
+    const bool flat = Pm.flat != 0;
+    float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * LD);  // [P][2][N]
+    Ext e;
+    ext_init(e);
+    if (P > 0 && !flat) {
+        const int cn = Pm.cn;
+        const size_t chanStride = (size_t)fc.dftH * hwp;
+        const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
+        for (int k = 0; k < cn; k++) {
+            const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
+            const int total = P << (LOG2N - 1);
+#pragma unroll 4
+            for (int it = tid; it < total; it += kThreads) {
+                const int p = it >> (LOG2N - 1), kk = it & (HALF - 1);
+                const int r = 2 * (pair0 + p);
+                const float2 u = __ldg(cb + (size_t)brev_bits(r, log2H) * hwp + kk);
+                const float2 v = __ldg(cb + (size_t)brev_bits(r + 1, log2H) * hwp + kk);
+                float2 *zl = smem + p * LD;
+                zl[padi(brevn<LOG2N>(kk))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+                if (kk > 0)
+                    zl[padi(brevn<LOG2N>(N - kk))] = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+            }
+            if (tid < P) {
+                const int r = 2 * (pair0 + tid);
+                const float2 u = __ldg(cb + (size_t)brev_bits(r, log2H) * hwp + HALF);
+                const float2 v = __ldg(cb + (size_t)brev_bits(r + 1, log2H) * hwp + HALF);
+                smem[tid * LD + padi(brevn<LOG2N>(HALF))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+            }
+            __syncthreads();
+            line_fft<true, LOG2N>(smem, P, fc.triW);
+            for (int p = 0; p < P; p++) {
+                const float2 *zl = smem + p * LD;
+                float *a0 = acc + (size_t)(2 * p) * N, *a1 = a0 + N;
+#pragma unroll
+                for (int q = 0; q < XIT; q++) {
+                    const int x = tid + q * kThreads;
+                    if (x < bw) {
+                        const float2 z = zl[padi(x)];
+                        if (k == 0) {
+                            a0[x] = z.x;
+                            a1[x] = z.y;
+                        } else {
+                            a0[x] = __fadd_rn(a0[x], z.x);
+                            a1[x] = __fadd_rn(a1[x], z.y);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (!a.ms.lanes) {
+        // No statistics lanes: store the raw correlation for k_norm instead.
+        if (P > 0 && !flat) {
+            float *corr = a.ms.corr + (size_t)slot * a.ms.corrStride;
+            for (int rr = 0; rr < 2 * P && 2 * pair0 + rr < bh; rr++)
+#pragma unroll
+                for (int q = 0; q < XIT; q++) {
+                    const int x = tid + q * kThreads;
+                    if (x < bw) corr[(size_t)(tb.y0 + 2 * pair0 + rr) * m.rw + tb.x0 + x] = acc[(size_t)rr * N + x];
+                }
+        }
+        return;
+    }
+    if (P > 0) {
+        const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
+        float *map = a.ms.map;
+        for (int rr = 0; rr < 2 * P; rr++) {
+            const int r = 2 * pair0 + rr;
+            if (r >= bh) break;
+            const long long rowBase = (long long)(tb.y0 + r) * m.rw + tb.x0;
+            float2 td[XIT];
+#pragma unroll
+            for (int q = 0; q < XIT; q++) {
+                const int x = tid + q * kThreads;
+                td[q] = (!flat && x < bw) ? __ldg(lanes + rowBase + x) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int q = 0; q < XIT; q++) {
+                const int x = tid + q * kThreads;
+                if (x < bw) {
+                    float score = 1.f;
+                    if (!flat) {
+                        const float num = __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
+                        const float den = td[q].y, an = fabsf(num);
+                        if (an < den)
+                            score = __fdiv_rn(num, den);
+                        else if (an < __fmul_rn(den, 1.125f))
+                            score = num > 0.f ? 1.f : -1.f;
+                        else
+                            score = 0.f;
+                    }
+                    if (map) map[rowBase + x] = score;
+                    ext_add(e, score, rowBase + x);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (tid == 0) {
+        Partial &o = a.partials[m.partBase + a.partOffset + tileLocal * gridDim.x + blockIdx.x];
+        o.minV = e.minV;
+        o.maxV = e.maxV;
+        o.minI = e.minI;
+        o.maxI = e.maxI;
+        __threadfence();
+        isLast = atomicAdd(&a.counters[m.pIdx], 1) == a.nparts - 1;
+    }
+    __syncthreads();
+    if (!isLast) return;
+    __threadfence();
+    ext_init(e);
+    for (int i = tid; i < a.nparts; i += kThreads) {
+        const volatile Partial *p = a.partials + m.partBase + i;
+        Ext o;
+        o.minV = p->minV;
+        o.maxV = p->maxV;
+        o.minI = p->minI;
+        o.maxI = p->maxI;
+        ext_merge(e, o);
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (tid == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
+}
+
+template <int L>
+void fwd_one(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
+    set_smem(k_fwd_rows_t<L>, smem);
+    k_fwd_rows_t<L><<<grid, threads, smem, st>>>(a);
+}
+
+template <int L>
+void inv_one(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
+    set_smem(k_inv_rows_t<L>, smem);
+    k_inv_rows_t<L><<<grid, kThreads, smem, st>>>(a);
+}
+
+}  // namespace
+
+bool rows_fixed_length(int log2n) { return log2n >= 5 && log2n <= 12; }
+
+void launch_fwd_rows_fixed(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
+    switch (a.fc.log2n) {
+        case 5: fwd_one<5>(a, grid, threads, smem, st); break;
+        case 6: fwd_one<6>(a, grid, threads, smem, st); break;
+        case 7: fwd_one<7>(a, grid, threads, smem, st); break;
+        case 8: fwd_one<8>(a, grid, threads, smem, st); break;
+        case 9: fwd_one<9>(a, grid, threads, smem, st); break;
+        case 10: fwd_one<10>(a, grid, threads, smem, st); break;
+        case 11: fwd_one<11>(a, grid, threads, smem, st); break;
+        default: fwd_one<12>(a, grid, threads, smem, st); break;
+    }
+}
+
+void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
+    switch (a.fc.log2n) {
+        case 5: inv_one<5>(a, grid, smem, st); break;
+        case 6: inv_one<6>(a, grid, smem, st); break;
+        case 7: inv_one<7>(a, grid, smem, st); break;
+        case 8: inv_one<8>(a, grid, smem, st); break;
+        case 9: inv_one<9>(a, grid, smem, st); break;
+        case 10: inv_one<10>(a, grid, smem, st); break;
+        case 11: inv_one<11>(a, grid, smem, st); break;
+        default: inv_one<12>(a, grid, smem, st); break;
+    }
+}
+
+}  // namespace cvm
