@@ -453,16 +453,16 @@ def c2_models(L):
     return m
 
 
-def roofline(L, step_dev, torch, stream, peak, peak_kind):
-    """The dominant kernel's algorithmic bytes over its duration, timed live
-    by the library's event instrumentation (events recorded on the stream
-    each kernel is launched on)."""
+def profile_kernels(L, step_dev, torch, reps=20):
+    """Per-kernel totals over `reps` steps from the library's event
+    instrumentation (events recorded on the stream each kernel is launched
+    on): [(name, total ms, launches)]."""
     import ctypes as C
     L.cvm_profile_enable.argtypes = [C.c_int]
     L.cvm_profile_enable.restype = None
     L.cvm_profile_read.argtypes = [C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
     L.cvm_profile_enable(1)
-    for _ in range(20):
+    for _ in range(reps):
         step_dev()
     torch.cuda.synchronize()
     L.cvm_profile_enable(0)
@@ -473,6 +473,13 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind):
     while L.cvm_profile_read(i, name, 64, C.byref(ms_), C.byref(cnt)) == 0:
         rows.append((name.value.decode(), ms_.value, int(cnt.value)))
         i += 1
+    return rows
+
+
+def roofline(L, step_dev, torch, stream, peak, peak_kind):
+    """The dominant kernel's algorithmic bytes over its duration, timed live
+    by the library's event instrumentation."""
+    rows = profile_kernels(L, step_dev, torch)
     models = c2_models(L)
     total = sum(r[1] for r in rows)
     kernels = {}
@@ -636,6 +643,9 @@ def run_gpu_secondary(args):
             "e2e": {"value": mpx / (e2e_ms / 1e3), "unit": "template*Mpx/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
             "gpu_launches": int(launches), "secondary": True}
+    rows = profile_kernels(L, step_dev, torch, reps=3)
+    tot = sum(r[1] for r in rows) or 1.0
+    line["kernels"] = {nm: {"ms_per_launch": t / max(n, 1), "launches": n, "share": t / tot} for nm, t, n in rows}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
     print(json.dumps(line))

@@ -49,6 +49,24 @@ struct InvArgs {
     cvm_result *out;
 };
 
+// Arguments of the column kernels (colsR4Go, mulConjGo; mode 0: forward
+// spectrum, 1: forward + conj-multiply + inverse, 2: conj-multiply + inverse
+// of a stored natural-order spectrum).
+struct ColsArgs {
+    int mode;
+    const float2 *in;
+    float2 *out;
+    int cnS;
+    TileGeom g;
+    FftClass fc;
+    int cls;
+    int chanCount;
+    const int *cnDev;
+    float scale;
+    MemberSet ms;
+    int SC, logSC;
+};
+
 // Arguments of the forward-rows kernels (forwardRowPair, impl.go:301-344).
 struct FwdRowsArgs {
     const uint8_t *img;
@@ -67,6 +85,9 @@ struct FwdRowsArgs {
 bool rows_fixed_length(int log2n);
 void launch_fwd_rows_fixed(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st);
 void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st);
+// The column kernels specialised on dftH = 2^5 .. 2^12 (cvm_cols.cu).
+bool cols_fixed_length(int log2H);
+void launch_cols_fixed(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st);
 
 namespace {
 

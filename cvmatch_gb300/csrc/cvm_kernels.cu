@@ -453,20 +453,6 @@ __global__ void k_fwd_rows(const uint8_t *__restrict__ img, long long istride, i
 
 // --------------------------------------------------------------- columns
 
-struct ColsArgs {
-    int mode;
-    const float2 *in;
-    float2 *out;
-    int cnS;
-    TileGeom g;
-    FftClass fc;
-    int cls;
-    int chanCount;
-    const int *cnDev;
-    float scale;
-    MemberSet ms;
-    int SC, logSC;
-};
 
 
 // Column pass over one [dftH x SC] strip of one (member, tile, channel).
@@ -1724,7 +1710,9 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     dim3 grid((fc.hw + SC - 1) / SC, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
     ProfScope ps(mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv"), st);
-    if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
+    if (cols_fixed_length(fc.log2H)) {
+        launch_cols_fixed(a, grid, smem, st);
+    } else if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
         if (mode == 0) {
             set_smem(k_cols_even<0>, smem);
             k_cols_even<0><<<grid, kThreads, smem, st>>>(a);
