@@ -307,7 +307,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         partOff[c] = nparts;
         nparts += G->fc[c].ntiles * inv_rows_ctas_per_tile(G->fc[c], &P);
     }
-    const size_t hElems = (size_t)(cnS + 1) * J.ih * sg.hp;
+    const size_t hElems = (size_t)stat_pitch(cnS) * J.ih * sg.hp;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                    Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
                    Arena::bytes((size_t)rw * rh, sizeof(float2));
@@ -738,7 +738,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     // one set of row prefixes for every member (each differences it at its own width)
     const int cnP = f->step == 4 ? 4 : 1;
     const int hpP = (int)align_up((size_t)pw + 1, 32);
-    const size_t prefixElems = (size_t)(cnP == 4 ? 6 : cnP + 1) * ph * hpP;
+    const size_t prefixElems = (size_t)stat_pitch(cnP) * ph * hpP;
     const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                          Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) + frameBytes +
                          partBytes + waveBytes;
@@ -803,7 +803,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             SepGrid sgP = bg.sg;
             sgP.hp = hpP;
             CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
-                                      f->step == 4 ? 4 : 1, prefix, 0, st, 1, &cnP));
+                                      cnP, prefix, 0, st, 1));
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
             for (int c = 0; c < G.nclass; c++)

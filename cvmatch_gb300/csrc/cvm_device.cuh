@@ -233,6 +233,38 @@ __device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
 }
 
 
+__host__ __device__ constexpr int stat_pitch_c(int cn) { return stat_pitch(cn); }
+
+// NP consecutive u32 (NP = 2, 4 or 8; 8- or 16-byte aligned) in one or two
+// vector accesses.
+template <int NP>
+__device__ __forceinline__ void ldv(unsigned int *o, const unsigned int *p) {
+    if constexpr (NP == 2) {
+        const uint2 t = __ldg(reinterpret_cast<const uint2 *>(p));
+        o[0] = t.x;
+        o[1] = t.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < NP; i += 4) {
+            const uint4 t = __ldg(reinterpret_cast<const uint4 *>(p + i));
+            o[i] = t.x;
+            o[i + 1] = t.y;
+            o[i + 2] = t.z;
+            o[i + 3] = t.w;
+        }
+    }
+}
+
+template <int NP>
+__device__ __forceinline__ void stv(unsigned int *p, const unsigned int *v) {
+    if constexpr (NP == 2) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < NP; i += 4) *reinterpret_cast<uint4 *>(p + i) = make_uint4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    }
+}
+
 template <typename K>
 void set_smem(K kernel, size_t bytes) {
     if (bytes > 48 * 1024)

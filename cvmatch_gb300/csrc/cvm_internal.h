@@ -3,9 +3,11 @@
 //
 // Data layout in HBM (one frame, one bucket/plan class):
 //   frame        u8, device copy of the caller's image, pitch = stride
-//   SAT planes   (ih+1) x pitch32 summed-area tables of every channel
-//                (u32, modular: every window sum is < 2^32) and of the
-//                squared pixels (u64); row/column 0 are zero
+//   window sums  per image row, the horizontal window sums of every
+//                channel and of the squared pixels (u32, modular: every
+//                window sum is < 2^32), interleaved per x; a fleet keeps
+//                one set of exclusive row prefixes instead
+//   lanes        per result (t, den): the correlation-free part of normOne
 //   spectra      per tile t and channel k a dftH x hwp complex64 slab
 //                (hwp = dftW/2+1 rounded up to 16): the forward rows
 //                kernel writes logical spectrum row L at slot brev(L),
@@ -164,25 +166,29 @@ cudaError_t launch_norm(const uint8_t *img, long long istride, int step, const M
                         const NormGrid &ng, int cnLaunch, Partial *partials, int *counters, cvm_result *out,
                         cudaStream_t st);
 // Separable window statistics: k_hsum writes horizontal window sums (u32,
-// [q][ih][hp] per wave slot), k_vstats slides them down BV-row bands and
-// stores per result (t, den) into ms.lanes (pitch rw per slot).  The planes
-// of one slot take (cnMax+1) * ih * hp * 4 bytes; [cnMin, cnMax] is the
-// range of device-side channel counts the members may have.
+// interleaved per (row, x): [ih][hp][stat_pitch(cn)] per wave slot),
+// k_vstats slides them down BV-row bands and stores per result (t, den)
+// into ms.lanes (pitch rw per slot).  One slot takes
+// stat_pitch(cnMax) * ih * hp * 4 bytes; [cnMin, cnMax] is the range of
+// device-side channel counts the members may have.
 struct SepGrid {
     int BV, ncx, nby, hp;
+    int rhMax;
 };
+// u32 slots per (row, x) of the interleaved window-sum / row-prefix
+// layouts for cn channels (cn+1 values; 6 for a 4-channel prefix).
+constexpr int stat_pitch(int cn) { return cn == 1 ? 2 : (cn <= 3 ? 4 : 8); }
 SepGrid sep_grid(int rwMax, int rhMax);
 // sharedPrefix: H holds launch_row_prefix's shared planes (no per-member
 // k_hsum; each member differences the prefix at its own width).
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
-                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix = 0,
-                             const int *prefixCnHost = nullptr);
-// Exclusive row prefixes P_q(x, r) (x = 0..iw), u32 modular, planes
-// [q][ih][hp] with hp >= iw + 1: the first cnP channel sums, the squares of
-// the first min(cnP,3) channels, and for cnP == 4 the alpha squares
-// (cnP + 1 planes, 6 when cnP == 4).  *prefixCnHost of launch_sep_stats
-// must be this cnP.
+                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix = 0);
+// Exclusive row prefixes P_q(x, r) (x = 0..iw), u32 modular, interleaved
+// [ih][hp][stat_pitch(cnP)] with hp >= iw + 1: the first cnP channel sums,
+// the squares of the first min(cnP,3) channels and, for cnP == 4, the
+// alpha squares (cnP + 1 values, 6 when cnP == 4).  launch_sep_stats with
+// sharedPrefix reads it with cnMax == cnP.
 cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, int iw, int ih, int cnP,
                               unsigned int *P, int hp, cudaStream_t st);
 

@@ -1237,14 +1237,15 @@ __global__ void __launch_bounds__(256) k_norm(NormArgs a) {
 // squared pixels summed over the channels (impl.go:708-805 restated as a
 // separable box sum).  One CTA per image row: a block prefix scan of the
 // row in u32 (modular; every window sum is < 2^32 because tw <= 8192 and
-// cn*65025*tw < 2^32), then one difference per output.  Planes are
-// [q][ih][hp] u32 with hp the padded result width.
+// cn*65025*tw < 2^32), then one difference per output.  The cn+1 values
+// of one (row, x) are interleaved, stat_pitch(cn) u32 apart per x, so a
+// reader fetches them with one vector load: H[(r*hp + x)*pitch + q].
 struct HsumArgs {
     const uint8_t *img;
     long long istride;
     int step, iw, ih, rw, tw, hp;
-    unsigned int *H;          // plane q of wave slot z at H + z*slotStride + q*planeStride
-    size_t planeStride, slotStride;
+    unsigned int *H;          // wave slot z at H + z*slotStride
+    size_t slotStride;
     const DevMember *table;   // fleet: per-slot member (tw, pIdx); nullptr: solo
     int first;
     const DevParams *params;
@@ -1330,11 +1331,14 @@ __device__ __forceinline__ void hsum_row(const HsumArgs &a, int slot, int tw, in
         }
     }
     __syncthreads();
-    // 3. window sums, coalesced out
-    unsigned int *H = a.H + (size_t)slot * a.slotStride + (size_t)r * a.hp;
+    // 3. window sums, interleaved per x, one vector store each
+    constexpr int NP = stat_pitch_c(CN);
+    unsigned int *H = a.H + (size_t)slot * a.slotStride + (size_t)r * a.hp * NP;
     for (int x = tid; x < rw; x += nt) {
+        unsigned int v[NP];
 #pragma unroll
-        for (int q = 0; q <= CN; q++) H[(size_t)q * a.planeStride + x] = sp[q * ld + x + tw] - sp[q * ld + x];
+        for (int q = 0; q < NP; q++) v[q] = q <= CN ? sp[q * ld + x + tw] - sp[q * ld + x] : 0u;
+        stv<NP>(H + (size_t)x * NP, v);
     }
 }
 
@@ -1345,7 +1349,7 @@ __device__ __forceinline__ void hsum_row(const HsumArgs &a, int slot, int tw, in
 // Each member's window sum is then P[x+tw] - P[x] at its own width.
 template <int CN>
 __global__ void __launch_bounds__(256) k_row_prefix(const uint8_t *__restrict__ img, long long istride, int step,
-                                                    int iw, unsigned int *P, size_t planeStride, int hp) {
+                                                    int iw, unsigned int *P, int hp) {
     constexpr int NQ = CN == 4 ? 6 : CN + 1;
     extern __shared__ __align__(16) unsigned int sp[];  // [NQ][iw+1]
     __shared__ unsigned int wsum[kThreads / 32][NQ];
@@ -1406,10 +1410,13 @@ __global__ void __launch_bounds__(256) k_row_prefix(const uint8_t *__restrict__ 
         }
     }
     __syncthreads();
-    unsigned int *out = P + (size_t)r * hp;
+    constexpr int NP = stat_pitch_c(CN);
+    unsigned int *out = P + (size_t)r * hp * NP;
     for (int x = tid; x <= iw; x += nt) {
+        unsigned int v[NP];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) out[(size_t)q * planeStride + x] = sp[q * ld + x];
+        for (int q = 0; q < NP; q++) v[q] = q < NQ ? sp[q * ld + x] : 0u;
+        stv<NP>(out + (size_t)x * NP, v);
     }
 }
 
@@ -1444,37 +1451,46 @@ __global__ void __launch_bounds__(256) k_hsum(HsumArgs a) {
 //   den = sqrt(idiff * varScale) * templNorm, or 0 under the lim guard
 // so the inverse-rows epilogue only needs num = corr - t and the ladder.
 struct VstatArgs {
-    const unsigned int *H;
-    size_t planeStride, slotStride;
+    const unsigned int *H;    // per-slot window sums, or (PRE) the shared row prefix
+    size_t slotStride;
     int hp;
     MemberSet ms;
     int BV;
-    int fromPrefix;   // H holds the shared row prefix: window sum = P[x+tw] - P[x]
-    int prefixCn;     // channel count the shared prefix was built for
 };
 
-template <int CN, bool PRE>
+// PRE: H is the shared row prefix built for PCN channels (window sum =
+// P[x+tw] - P[x]); its squares are plane PCN (PCN < 4) or planes 4 (RGB)
+// and 5 (alpha) when PCN == 4 (a cn = 3 member leaves alpha out).
+template <int CN, bool PRE, int PCN>
 __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &m, const DevParams &Pm) {
+    constexpr int NP = PRE ? stat_pitch_c(PCN) : stat_pitch_c(CN);
     const int slot = blockIdx.z;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int Y0 = blockIdx.y * a.BV;
     if (x >= m.rw || Y0 >= m.rh) return;
     const int Bv = min(a.BV, m.rh - Y0);
     const int th = m.th;
-    const unsigned int *H = a.H + (PRE ? 0 : (size_t)slot * a.slotStride) + x;
-    const int tw = PRE ? m.tw : 0;  // second tap of a prefix difference
-    const size_t ps = a.planeStride;
-    const int hp = a.hp;
+    const size_t rp = (size_t)a.hp * NP;  // row pitch
+    const unsigned int *H = a.H + (PRE ? 0 : (size_t)slot * a.slotStride) + (size_t)x * NP;
+    const int twoff = PRE ? m.tw * NP : 0;
     float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride + x;
-    auto tap = [&](const unsigned int *h, int q) { return __ldg(h + q * ps + tw) - __ldg(h + q * ps); };
-    // squares: plane CN of the member's own planes; in the shared colour
-    // prefix, plane 4 (RGB squares) plus plane 5 (alpha squares) for cn = 4
-    const int pcn = a.prefixCn;
-    auto hval = [&](const unsigned int *h, int q) -> unsigned int {
-        if (!PRE) return __ldg(h + q * ps);
-        if (q < CN) return tap(h, q);
-        if (pcn == 4) return CN == 4 ? tap(h, 4) + tap(h, 5) : tap(h, 4);
-        return tap(h, pcn);
+    // the CN sums and the squared sum of row h's window
+    auto rowvals = [&](const unsigned int *h, unsigned int *hv) {
+        unsigned int A[NP];
+        ldv<NP>(A, h + twoff);
+        if (!PRE) {
+#pragma unroll
+            for (int q = 0; q <= CN; q++) hv[q] = A[q];
+        } else {
+            unsigned int Bq[NP];
+            ldv<NP>(Bq, h);
+#pragma unroll
+            for (int q = 0; q < CN; q++) hv[q] = A[q] - Bq[q];
+            if (PCN == 4)
+                hv[CN] = CN == 4 ? (A[4] - Bq[4]) + (A[5] - Bq[5]) : A[4] - Bq[4];
+            else
+                hv[CN] = A[PCN] - Bq[PCN];
+        }
     };
     unsigned int s[CN];
     unsigned long long q = 0;
@@ -1482,10 +1498,11 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     for (int k = 0; k < CN; k++) s[k] = 0u;
 #pragma unroll 4
     for (int dy = 0; dy < th; dy++) {
-        const unsigned int *h = H + (size_t)(Y0 + dy) * hp;
+        unsigned int hv[CN + 1];
+        rowvals(H + (size_t)(Y0 + dy) * rp, hv);
 #pragma unroll
-        for (int k = 0; k < CN; k++) s[k] += hval(h, k);
-        q += hval(h, CN);
+        for (int k = 0; k < CN; k++) s[k] += hv[k];
+        q += hv[CN];
     }
     const unsigned long long area = (unsigned long long)m.tw * th;
     const unsigned int t0 = (unsigned int)Pm.tsum[0], t1 = (unsigned int)Pm.tsum[1];
@@ -1495,12 +1512,8 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
         unsigned int hin[CN + 1], hout[CN + 1];
         const bool more = y + 1 < Y0 + Bv;
         if (more) {
-            const unsigned int *hi = H + (size_t)(y + th) * hp, *ho = H + (size_t)y * hp;
-#pragma unroll
-            for (int k = 0; k <= CN; k++) {
-                hin[k] = hval(hi, k);
-                hout[k] = hval(ho, k);
-            }
+            rowvals(H + (size_t)(y + th) * rp, hin);
+            rowvals(H + (size_t)y * rp, hout);
         }
         unsigned long long cross = (unsigned long long)s[0] * t0, sq = (unsigned long long)s[0] * s[0];
         if (CN > 1) {
@@ -1541,9 +1554,9 @@ __global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
     const DevParams &Pm = a.ms.params[m.pIdx];
     if (Pm.flat) return;
     if (Pm.cn == CNA)
-        vstat_cols<CNA, PRE>(a, m, Pm);
+        vstat_cols<CNA, PRE, CNB>(a, m, Pm);
     else if (CNB != CNA && Pm.cn == CNB)
-        vstat_cols<CNB, PRE>(a, m, Pm);
+        vstat_cols<CNB, PRE, CNB>(a, m, Pm);
 }
 
 // Small host values to device memory through kernel arguments.
@@ -1844,13 +1857,22 @@ SepGrid sep_grid(int rwMax, int rhMax) {
     g.ncx = (rwMax + kThreads - 1) / kThreads;
     g.nby = (rhMax + g.BV - 1) / g.BV;
     g.hp = (rwMax + 31) / 32 * 32;
+    g.rhMax = rhMax;
     return g;
+}
+
+// Band height of the vertical slide: every band first sums th rows, so
+// taller bands amortise that start over more results; the band stays at 16
+// rows unless the launch has CTAs to spare (~6 per SM at the taller band).
+static int vstat_band(const SepGrid &sg, int nmembers) {
+    int BV = 16;
+    while (BV < 128 && (long long)sg.ncx * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) * nmembers >= 6 * 152) BV *= 2;
+    return BV;
 }
 
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
-                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix,
-                             const int *prefixCnHost) {
+                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix) {
     HsumArgs h;
     h.img = img;
     h.istride = istride;
@@ -1861,23 +1883,19 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     h.tw = soloTw;
     h.hp = sg.hp;
     h.H = H;
-    h.planeStride = (size_t)ih * sg.hp;
     h.slotStride = slotStride;
     h.table = ms.table;
     h.first = ms.first;
     h.params = ms.params;
     h.pIdx = ms.solo.pIdx;
     VstatArgs v;
-    v.fromPrefix = sharedPrefix;
-    v.prefixCn = prefixCnHost ? *prefixCnHost : 0;
     v.H = H;
-    v.planeStride = h.planeStride;
     v.slotStride = slotStride;
     v.hp = sg.hp;
     v.ms = ms;
-    v.BV = sg.BV;
+    v.BV = vstat_band(sg, nmembers);
     const size_t smem = (size_t)(cnMax + 1) * (iw + 1) * sizeof(unsigned int);
-    dim3 gh(ih, 1, nmembers), gv(sg.ncx, sg.nby, nmembers);
+    dim3 gh(ih, 1, nmembers), gv(sg.ncx, (sg.rhMax + v.BV - 1) / v.BV, nmembers);
     if (!sharedPrefix) {
         ProfScope ps("k_hsum", st);
         if (cnMax == 1) {
@@ -1924,13 +1942,12 @@ cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, i
                               unsigned int *P, int hp, cudaStream_t st) {
     const int nq = cnP == 4 ? 6 : cnP + 1;
     const size_t smem = (size_t)nq * (iw + 1) * sizeof(unsigned int);
-    const size_t planeStride = (size_t)ih * hp;
     ProfScope ps("k_row_prefix", st);
     switch (cnP) {
-        case 1: set_smem(k_row_prefix<1>, smem); k_row_prefix<1><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
-        case 2: set_smem(k_row_prefix<2>, smem); k_row_prefix<2><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
-        case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
-        default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, planeStride, hp); break;
+        case 1: set_smem(k_row_prefix<1>, smem); k_row_prefix<1><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
+        case 2: set_smem(k_row_prefix<2>, smem); k_row_prefix<2><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
+        case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
+        default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
     }
     count_launches(1);
     return cudaGetLastError();
