@@ -387,6 +387,9 @@ def run_gpu(args):
         assert got == res.tuple(), (got, res.tuple())
         peak, peak_kind = measured_peaks()
         roof = roofline(L, step_dev, torch, stream, peak, peak_kind)
+        if args.timeline:
+            for nm, a, b in timeline(L, step_dev, torch):
+                sys.stderr.write(f"timeline {nm:24s} {a:8.1f} {b:8.1f} us\n")
         line = {"metric": "template*Mpx/s", "value": value, "unit": "template*Mpx/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -474,6 +477,28 @@ def profile_kernels(L, step_dev, torch, reps=20):
         rows.append((name.value.decode(), ms_.value, int(cnt.value)))
         i += 1
     return rows
+
+
+def timeline(L, step_dev, torch, steps=3):
+    """Per-launch spans (kernel, start, end; ms after the first launch) of
+    the last of `steps` profiled steps, across the library's streams."""
+    import ctypes as C
+    L.cvm_profile_span.argtypes = [C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.cvm_profile_enable(1)
+    for _ in range(steps):
+        step_dev()
+    torch.cuda.synchronize()
+    L.cvm_profile_enable(0)
+    spans, i = [], 0
+    name = C.create_string_buffer(64)
+    t0, t1 = C.c_double(), C.c_double()
+    while L.cvm_profile_span(i, name, 64, C.byref(t0), C.byref(t1)) == 0:
+        spans.append((name.value.decode(), t0.value, t1.value))
+        i += 1
+    per = len(spans) // steps
+    last = spans[-per:] if per else []
+    base = min((a for _, a, _ in last), default=0.0)
+    return [(nm, round(1e3 * (a - base), 1), round(1e3 * (b - base), 1)) for nm, a, b in last]
 
 
 def roofline(L, step_dev, torch, stream, peak, peak_kind):
@@ -662,6 +687,7 @@ def main():
     ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map"],
                     help="match (default, the reported line) or a secondary configuration")
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
+    ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -119,15 +119,24 @@ cudaStream_t thread_stream() {
 // Per-thread side stream and fork/join events: the template side of a call
 // (statistics, alpha scans, template spectrum) runs beside the frame's
 // forward transforms, joined before the first step that needs both.
+// Two per-thread side streams: st carries the template spectrum (and the
+// frame channel whose presence the alpha decision selects), st2 the window
+// statistics; fork is recorded on the caller's stream once the statistics
+// and the channel count exist, join/joinStats when each chain is done.
 struct SideStream {
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, st2 = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr;
 };
 
 SideStream &side_stream() {
     thread_local SideStream s;
     if (!s.st) {
-        cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
+        // The side chains are short launches that gate the caller's stream:
+        // above its priority, their CTAs are placed first as SMs free up.
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        cudaStreamCreateWithPriority(&s.st, cudaStreamNonBlocking, greatest);
+        cudaStreamCreateWithPriority(&s.st2, cudaStreamNonBlocking, greatest < least ? greatest + 1 : greatest);
         cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
@@ -354,30 +363,29 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.map = J.map;
     ms.lanes = lanes;
     ms.lanesStride = 0;
-    // Fork: statistics, alpha scans, the template spectrum and the window
-    // statistics on the side stream; the frame channels whose presence does
-    // not depend on the alpha decision (all of them for a fixed cn, RGB for
-    // colour) on st.
+    // The template statistics, the parent's alpha scan and the channel
+    // count first (one short launch), then three chains: the frame's row
+    // transforms (every channel the device chose) on st; the template
+    // spectrum on the first side stream; the window statistics on the
+    // second.
     SideStream &ss = side_stream();
-    CVM_CUDA(cudaEventRecord(ss.fork, st));
-    CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
-                         J.cnFixed, F, ss.st));
+                         J.cnFixed, F, st));
+    CVM_CUDA(cudaEventRecord(ss.fork, st));
+    CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
+    CVM_CUDA(cudaStreamWaitEvent(ss.st2, ss.fork, 0));
+    CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg, J.mode == 1 ? 3 : J.cnFixed,
+                              J.mode == 1 ? 4 : J.cnFixed, H, 0, ss.st2));
+    CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
     if (!J.cachedP)
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st));
     CVM_CUDA(cudaEventRecord(ss.join, ss.st));
-    CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg, J.mode == 1 ? 3 : J.cnFixed,
-                              J.mode == 1 ? 4 : J.cnFixed, H, 0, ss.st));
-    CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st));
-    const int cnSure = J.mode == 1 ? 3 : cnS;
     for (int c = 0; c < G->nclass; c++)
-        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnSure, nullptr, G->g, G->fc[c], spec[c], cnS, st));
+        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st));
     CVM_CUDA(cudaStreamWaitEvent(st, ss.join, 0));
     for (int c = 0; c < G->nclass; c++) {
         const FftClass &f = G->fc[c];
-        if (cnS > cnSure)  // the alpha channel, present only when the device chose cn = 4
-            CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, f, spec[c], cnS, st, cnSure));
         ms.scratch[c] = spec[c];
         ms.scratchStride[c] = 0;
         CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
@@ -1118,6 +1126,16 @@ int cvm_profile_read(int i, char *name, size_t len, double *ms_total, uint64_t *
     unsigned long long n = 0;
     const int rc = profile_read(i, name, len, ms_total, &n);
     if (rc == 0 && launches) *launches = n;
+    return rc;
+}
+
+int cvm_profile_span(int i, char *name, size_t len, double *t0_ms, double *t1_ms) {
+    double a = 0, b = 0;
+    const int rc = profile_span(i, name, len, &a, &b);
+    if (rc == 0) {
+        if (t0_ms) *t0_ms = a;
+        if (t1_ms) *t1_ms = b;
+    }
     return rc;
 }
 

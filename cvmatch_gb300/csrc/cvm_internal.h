@@ -207,5 +207,6 @@ void set_error_message(const char *msg);
 // per-kernel event timing (exported by cvm_profile_enable/cvm_profile_read)
 void profile_enable(int on);
 int profile_read(int i, char *name, size_t len, double *ms, unsigned long long *count);
+int profile_span(int i, char *name, size_t len, double *t0, double *t1);
 
 }  // namespace cvm

@@ -57,6 +57,13 @@ struct Total {
     unsigned long long n = 0;
 };
 std::vector<Total> totals;
+// every launch since enabling: start and end relative to the first launch
+struct Span {
+    std::string name;
+    double t0, t1;
+};
+std::vector<Span> spans;
+cudaEvent_t origin = nullptr;
 
 int begin(const char *name, cudaStream_t st) {
     if (!on) return -1;
@@ -81,7 +88,13 @@ void collect() {
         cudaEventSynchronize(r.b);
         float ms = 0;
         cudaEventElapsedTime(&ms, r.a, r.b);
-        cudaEventDestroy(r.a);
+        if (!origin) {
+            origin = r.a;  // kept as the timeline's zero
+        }
+        float t0 = 0;
+        cudaEventElapsedTime(&t0, origin, r.a);
+        spans.push_back(Span{r.name, t0, (double)t0 + ms});
+        if (r.a != origin) cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
         Total *t = nullptr;
         for (Total &x : totals)
@@ -302,6 +315,7 @@ struct PrepArgs {
     const uint8_t *parent;   // parent whose alpha plane is scanned (nullptr: no scan)
     long long pstride;
     int pw, ph, parentCtas;
+    int pvec16;              // parent rows 16-byte aligned: scan with vector loads
     DevParams *P;
     int n;                   // params to finalize
     int setInit;             // store mode/cnFixed/tw/th of `init` into P[0] first
@@ -320,10 +334,10 @@ __global__ void k_prep(PrepArgs a) {
     bool bad = false;
     if ((int)blockIdx.x < a.tplCtas) {
         unsigned long long sm[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
-        const long long total = (long long)a.tw * a.th;
+        const int total = a.tw * a.th;  // below the statistics cap, < 2^31
         const uint8_t a0 = a.tstep == 4 ? a.tpl[3] : 0;
-        for (long long i = (long long)blockIdx.x * nt + tid; i < total; i += (long long)a.tplCtas * nt) {
-            const int y = (int)(i / a.tw), x = (int)(i - (long long)y * a.tw);
+        for (int i = blockIdx.x * nt + tid; i < total; i += a.tplCtas * nt) {
+            const int y = i / a.tw, x = i - y * a.tw;
             const uint8_t *p = a.tpl + (long long)y * a.tstride + (long long)x * a.tstep;
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -341,20 +355,62 @@ __global__ void k_prep(PrepArgs a) {
                 sm[k] += __shfl_down_sync(0xffffffffu, sm[k], o);
                 q[k] += __shfl_down_sync(0xffffffffu, q[k], o);
             }
+        // warp totals -> one set of atomics per CTA
+        __shared__ unsigned long long red[kThreads / 32][8];
+        __shared__ int redBad;
+        if (tid == 0) redBad = 0;
+        __syncthreads();
         const bool anyBad = __any_sync(0xffffffffu, bad);
         if ((tid & 31) == 0) {
-            for (int k = 0; k < a.cnStats; k++) {
-                if (sm[k]) atomicAdd(&a.P[0].tsum[k], sm[k]);
-                if (q[k]) atomicAdd(&a.P[0].tsq[k], q[k]);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                red[tid >> 5][k] = sm[k];
+                red[tid >> 5][4 + k] = q[k];
             }
-            if (anyBad) atomicOr(&a.P[0].alphaMismatch, 1u);
+            if (anyBad) redBad = 1;
         }
+        __syncthreads();
+        if (tid < 8) {
+            unsigned long long t = 0;
+            for (int w = 0; w < (nt >> 5); w++) t += red[w][tid];
+            const int k = tid & 3;
+            if (k < a.cnStats && t) atomicAdd(tid < 4 ? &a.P[0].tsum[k] : &a.P[0].tsq[k], t);
+        }
+        if (tid == 0 && redBad) atomicOr(&a.P[0].alphaMismatch, 1u);
     } else if (a.parent) {
         const int c = blockIdx.x - a.tplCtas;
         const uint8_t a0 = a.parent[3];
-        for (int y = c; y < a.ph; y += a.parentCtas) {
-            const uint8_t *row = a.parent + (long long)y * a.pstride + 3;
-            for (int x = tid; x < a.pw; x += nt) bad |= row[4LL * x] != a0;
+        if (a.pvec16) {
+            // four pixels per 16-byte load, the loads of several items in flight
+            const unsigned int want = (unsigned int)a0 << 24;
+            const int nv = a.pw >> 2, items = a.ph * nv, stride = a.parentCtas * nt;
+            unsigned int acc = 0u;
+            for (int it0 = c * nt + tid; it0 < items; it0 += 8 * stride) {
+                uint4 w[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {  // eight loads in flight
+                    const int it = it0 + k * stride;
+                    w[k] = make_uint4(want, want, want, want);
+                    if (it < items) {
+                        const int y = it / nv, v = it - y * nv;
+                        w[k] = __ldg(reinterpret_cast<const uint4 *>(a.parent + (long long)y * a.pstride) + v);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    acc |= ((w[k].x ^ want) | (w[k].y ^ want) | (w[k].z ^ want) | (w[k].w ^ want)) & 0xff000000u;
+            }
+            bad = acc != 0u;
+            // the last pw % 4 pixels of every row
+            for (int y = c * nt + tid; y < a.ph * (a.pw & 3); y += a.parentCtas * nt) {
+                const int r = y / (a.pw & 3), x = 4 * nv + (y - r * (a.pw & 3));
+                bad |= a.parent[(long long)r * a.pstride + 4LL * x + 3] != a0;
+            }
+        } else {
+            for (int y = c; y < a.ph; y += a.parentCtas) {
+                const uint8_t *row = a.parent + (long long)y * a.pstride + 3;
+                for (int x = tid; x < a.pw; x += nt) bad |= row[4LL * x] != a0;
+            }
         }
         if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(&a.F->alphaMismatch, 1u);
     }
@@ -1635,6 +1691,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
     a.pw = pw;
     a.ph = ph;
     a.parentCtas = parent ? (ph < 304 ? ph : 304) : 0;
+    a.pvec16 = parent && (reinterpret_cast<uintptr_t>(parent) & 15) == 0 && (pstride & 15) == 0;
     a.P = P;
     a.n = n;
     a.setInit = setInit;
@@ -1666,8 +1723,10 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     dim3 grid((pairs + P - 1) / P, fc.ntiles);
     const size_t smem = (size_t)P * group * padded_len(fc.n) * sizeof(float2);
     // as many threads as a radix-16 pass has units (a multiple of 32 in
-    // 64..256), so no thread idles in those passes
-    int threads = P * group * (fc.n >= 16 ? fc.n / 16 : 1);
+    // 64..256), so no thread idles in those passes; a device-chosen colour
+    // count is 3 unless an alpha plane varies, so size for that
+    const int groupLikely = (cnDev && chanCount == 4 && group == 4) ? 3 : group;
+    int threads = P * groupLikely * (fc.n >= 16 ? fc.n / 16 : 1);
     threads = threads < 64 ? 64 : (threads > kThreads ? kThreads : (threads + 31) / 32 * 32);
     ProfScope ps("k_fwd_rows", st);
     if (rows_fixed_length(fc.log2n)) {
@@ -1986,9 +2045,26 @@ cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int d
 }
 
 void profile_enable(int on) {
+    if (on) prof::collect();  // retire the records of an earlier window
     std::lock_guard<std::mutex> lk(prof::mu);
     prof::on = on != 0;
-    if (on) prof::totals.clear();
+    if (on) {
+        prof::totals.clear();
+        prof::spans.clear();
+        if (prof::origin) cudaEventDestroy(prof::origin);
+        prof::origin = nullptr;
+    }
+}
+
+int profile_span(int i, char *name, size_t len, double *t0, double *t1) {
+    prof::collect();
+    std::lock_guard<std::mutex> lk(prof::mu);
+    if (i < 0 || i >= (int)prof::spans.size()) return 1;
+    const prof::Span &sp = prof::spans[i];
+    if (name && len) snprintf(name, len, "%s", sp.name.c_str());
+    *t0 = sp.t0;
+    *t1 = sp.t1;
+    return 0;
 }
 
 int profile_read(int i, char *name, size_t len, double *ms, unsigned long long *count) {

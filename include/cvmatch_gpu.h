@@ -189,6 +189,11 @@ uint64_t cvm_launch_count(void);
  * past the last kernel; it waits for the recorded events. */
 void cvm_profile_enable(int on);
 int cvm_profile_read(int i, char *name, size_t len, double *ms_total, uint64_t *launches);
+/* The i-th profiled launch in completion-collection order: its kernel name
+ * and its start and end in milliseconds after the first profiled launch's
+ * start (a timeline across streams); nonzero past the last launch.
+ * Profiling aid with no reference counterpart. */
+int cvm_profile_span(int i, char *name, size_t len, double *t0_ms, double *t1_ms);
 
 /* Library version string. */
 const char *cvm_version(void);

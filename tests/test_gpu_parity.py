@@ -179,6 +179,36 @@ def test_alpha_mixed_constancy():
     assert np.array_equal(bits(m), bits(m4))
 
 
+@pytest.mark.parametrize("W,pw", [(48, 43), (48, 48), (44, 41), (42, 42)])
+def test_parent_alpha_scan_one_pixel(W, pw):
+    """alphaConst (cvmatch.go:146-168) of a device-resident parent: one
+    alpha byte different anywhere (first row, middle, a row's last pixels
+    past the last whole group of four, the very last pixel) switches the
+    match to four channels.  Pitches W*4 that are multiples of 16 take the
+    vector scan, the others the byte scan."""
+    torch = pytest.importorskip("torch")
+    L = cvm.lib()
+    ph = 37
+    base = rgba(77, ph, W, 200)
+    tpl = base[9:25, 11:31].copy()
+    for where in (None, (0, 1), (ph // 2, pw // 2), (3, pw - 1), (ph - 1, pw - 1)):
+        img = base.copy()
+        if where is not None:
+            img[where[0], where[1], 3] = 201
+        view = img[:, :pw]
+        d_img = torch.from_numpy(img).cuda()
+        d_tpl = torch.from_numpy(tpl).cuda()
+        rw, rh = pw - 20 + 1, ph - 16 + 1
+        d_map = torch.empty((rh, rw), dtype=torch.float32, device="cuda")
+        d_out = torch.zeros(6, dtype=torch.int32, device="cuda")
+        rc = L.cvm_match_device(d_img.data_ptr(), W * 4, pw, ph, d_tpl.data_ptr(), tpl.strides[0], 20, 16,
+                                d_map.data_ptr(), d_out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        _, want = oracle.match_u8(view, tpl, 3 if where is None else 4)
+        assert np.array_equal(bits(d_map.cpu().numpy()), bits(want)), where
+
+
 def test_find_all_occurrences_via_map():
     rng = np.random.default_rng(101)
     parent = np.empty((300, 400, 4), np.uint8)
