@@ -119,10 +119,9 @@ cudaStream_t thread_stream() {
 // Per-thread side stream and fork/join events: the template side of a call
 // (statistics, alpha scans, template spectrum) runs beside the frame's
 // forward transforms, joined before the first step that needs both.
-// Two per-thread side streams: st carries the template spectrum (and the
-// frame channel whose presence the alpha decision selects), st2 the window
-// statistics; fork is recorded on the caller's stream once the statistics
-// and the channel count exist, join/joinStats when each chain is done.
+// Two per-thread side streams: st carries the template spectrum, st2 the
+// window statistics; fork is recorded on the caller's stream once the
+// channel count exists, join/joinStats when each chain is done.
 struct SideStream {
     cudaStream_t st = nullptr, st2 = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr;
@@ -131,8 +130,10 @@ struct SideStream {
 SideStream &side_stream() {
     thread_local SideStream s;
     if (!s.st) {
-        // The side chains are short launches that gate the caller's stream:
-        // above its priority, their CTAs are placed first as SMs free up.
+        // The side chains gate the caller's stream: above its priority,
+        // their CTAs are placed first as SMs free up (at the caller's
+        // priority a one-CTA launch there waits tens of microseconds behind
+        // the transforms).
         int least = 0, greatest = 0;
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
         cudaStreamCreateWithPriority(&s.st, cudaStreamNonBlocking, greatest);
@@ -364,10 +365,12 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.lanes = lanes;
     ms.lanesStride = 0;
     // The template statistics, the parent's alpha scan and the channel
-    // count first (one short launch), then three chains: the frame's row
-    // transforms (every channel the device chose) on st; the template
-    // spectrum on the first side stream; the window statistics on the
-    // second.
+    // count first (one short launch on st), then three chains: the frame's
+    // row transforms (every channel the device chose, one launch) on st;
+    // the template spectrum on the first side stream; the window
+    // statistics on the second.  A launch that does not start first does
+    // not get SMs back from one that did (priority orders only the CTAs
+    // waiting for a slot), so the gating statistics launch goes first.
     SideStream &ss = side_stream();
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,

@@ -285,10 +285,10 @@ __global__ void k_alpha_scan(const uint8_t *__restrict__ img, long long stride, 
 
 // ----------------------------------------------------- statistics + cn
 
-// Derives the effective channel count and the tail constants of one
-// template with the reference's double-precision sequences
-// (impl.go:867-873, 1087; the cn choice of cvmatch.go:82-85 and
-// matcher.go:103-112).  Runs once per call, in the last CTA of k_prep.
+// Derives the effective channel count (cvmatch.go:82-85, matcher.go:103-112)
+// and the tail constants of one template with the reference's
+// double-precision sequences (impl.go:867-873, 1087).  Runs once per call,
+// in the last CTA of k_prep.
 __device__ void finalize_params(DevParams &p, const DevFrame &F, int *cnMax) {
     int cn = p.cnFixed;
     if (p.mode == 1) cn = (p.alphaMismatch == 0 && F.alphaMismatch == 0) ? 3 : 4;
