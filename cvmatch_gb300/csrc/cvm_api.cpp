@@ -116,9 +116,6 @@ cudaStream_t thread_stream() {
     return s;
 }
 
-// Per-thread side stream and fork/join events: the template side of a call
-// (statistics, alpha scans, template spectrum) runs beside the frame's
-// forward transforms, joined before the first step that needs both.
 // Two per-thread side streams: st carries the template spectrum, st2 the
 // window statistics; fork is recorded on the caller's stream once the
 // channel count exists, join/joinStats when each chain is done.
@@ -448,11 +445,69 @@ int check_image(const void *p, int w, int h) {
 }
 
 // Copies a host image to a device buffer with a 128-byte aligned pitch.
+// Per-thread page-locked staging for small pageable inputs (templates,
+// small frames): the copy out of it is asynchronous, so a call's launches
+// are queued while its frame is still in flight -- a pageable copy holds
+// the host until the stream reaches it.  Each slot's last copy is fenced
+// by an event that the next use waits for (normally long complete: the
+// host-buffer entry points synchronise before returning).
+struct Staging {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    ~Staging() {
+        if (p) cudaFreeHost(p);
+        if (done) cudaEventDestroy(done);
+    }
+};
+
+Staging *staging(size_t n, int slot) {
+    thread_local Staging b[2];
+    Staging &s = b[slot & 1];
+    if (!s.done && cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    cudaEventSynchronize(s.done);
+    if (s.cap < n) {
+        if (s.p) cudaFreeHost(s.p);
+        s.p = nullptr;
+        s.cap = 0;
+        const size_t cap = align_up(n, size_t(1) << 16);
+        if (cudaHostAlloc(&s.p, cap, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        s.cap = cap;
+    }
+    return &s;
+}
+
 int upload_image(PoolBuf &b, const uint8_t *src, long long stride, int w, int h, int bpp,
-                 long long *pitch, cudaStream_t st) {
+                 long long *pitch, cudaStream_t st, int stageSlot = 0) {
     const size_t row = (size_t)w * bpp;
     *pitch = (long long)align_up(row, 128);
     CVM_TRY(pool_alloc(b, (size_t)*pitch * h, st));
+    // Page-locked caller memory that the device can address is read by a
+    // kernel over the host link (several times the copy engine's rate for
+    // a frame); anything else goes through the copy engine.
+    cudaPointerAttributes at;
+    if ((size_t)row * h >= (size_t(1) << 20) && cudaPointerGetAttributes(&at, src) == cudaSuccess &&
+        at.type == cudaMemoryTypeHost && at.devicePointer) {
+        CVM_CUDA(launch_ingest(b.p, (size_t)*pitch, at.devicePointer, (size_t)stride, row, h, st));
+        return CVM_OK;
+    }
+    cudaGetLastError();  // an unregistered pointer's query leaves no error behind
+    if (row * h <= (size_t(4) << 20)) {
+        Staging *sg = staging(row * h, stageSlot);
+        if (sg) {
+            unsigned char *stg = static_cast<unsigned char *>(sg->p);
+            for (int y = 0; y < h; y++) memcpy(stg + (size_t)y * row, src + (size_t)y * stride, row);
+            CVM_CUDA(cudaMemcpy2DAsync(b.p, (size_t)*pitch, stg, row, row, h, cudaMemcpyHostToDevice, st));
+            CVM_CUDA(cudaEventRecord(sg->done, st));
+            return CVM_OK;
+        }
+    }
     CVM_CUDA(cudaMemcpy2DAsync(b.p, (size_t)*pitch, src, (size_t)stride, row, h, cudaMemcpyHostToDevice, st));
     return CVM_OK;
 }
@@ -466,8 +521,8 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     PoolBuf bi, bt, gi, gt, bm, bo;
     long long ip, tp;
     const int bpp = grayFromRgba ? 4 : step;
-    CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, st));
-    CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st));
+    CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st, 1));
+    CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, st, 0));
     const uint8_t *dImg = static_cast<const uint8_t *>(bi.p), *dTpl = static_cast<const uint8_t *>(bt.p);
     if (grayFromRgba) {
         long long gp = (long long)align_up((size_t)iw, 128), gtp = (long long)align_up((size_t)tw, 128);

@@ -195,6 +195,10 @@ cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, i
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).
 cudaError_t upload_bytes(void *dst, const void *src, size_t n, cudaStream_t st);
+// rows x rowBytes from device-accessible (page-locked, mapped) host memory
+// at src into device memory, by a kernel reading over the host link.
+cudaError_t launch_ingest(void *dst, size_t dpitch, const void *src, size_t spitch, size_t rowBytes, int rows,
+                          cudaStream_t st);
 cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int dh2, int hwp, int cnS,
                                  cudaStream_t st);
 

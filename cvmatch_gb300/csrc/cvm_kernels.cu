@@ -1615,6 +1615,35 @@ __global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
         vstat_cols<CNB, PRE, CNB>(a, m, Pm);
 }
 
+// Frame ingest from page-locked host memory: the GPU reads the caller's
+// rows over the host link directly (many 16-byte loads in flight per
+// thread), instead of the copy engine's single stream of transfers.
+template <typename V>
+__global__ void k_ingest(unsigned char *__restrict__ dst, size_t dpitch, const unsigned char *__restrict__ src,
+                         size_t spitch, int perRow, int rows) {
+    const long long items = (long long)perRow * rows;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < items; i0 += 4 * stride) {
+        V v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const long long i = i0 + k * stride;
+            if (i < items) {
+                const long long y = i / perRow, x = i - y * perRow;
+                v[k] = reinterpret_cast<const V *>(src + y * spitch)[x];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const long long i = i0 + k * stride;
+            if (i < items) {
+                const long long y = i / perRow, x = i - y * perRow;
+                reinterpret_cast<V *>(dst + y * dpitch)[x] = v[k];
+            }
+        }
+    }
+}
+
 // Small host values to device memory through kernel arguments.
 struct UploadBlob {
     unsigned char bytes[3072];
@@ -2008,6 +2037,24 @@ cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, i
         case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
         default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
     }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ingest(void *dst, size_t dpitch, const void *src, size_t spitch, size_t rowBytes, int rows,
+                          cudaStream_t st) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | dpitch | spitch |
+                        rowBytes;
+    const int grid = 4 * 152;
+    unsigned char *d = static_cast<unsigned char *>(dst);
+    const unsigned char *s = static_cast<const unsigned char *>(src);
+    ProfScope ps("k_ingest", st);
+    if ((a & 15) == 0)
+        k_ingest<uint4><<<grid, kThreads, 0, st>>>(d, dpitch, s, spitch, (int)(rowBytes / 16), rows);
+    else if ((a & 3) == 0)
+        k_ingest<unsigned int><<<grid, kThreads, 0, st>>>(d, dpitch, s, spitch, (int)(rowBytes / 4), rows);
+    else
+        k_ingest<unsigned char><<<grid, kThreads, 0, st>>>(d, dpitch, s, spitch, (int)rowBytes, rows);
     count_launches(1);
     return cudaGetLastError();
 }

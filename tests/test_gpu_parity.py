@@ -209,6 +209,42 @@ def test_parent_alpha_scan_one_pixel(W, pw):
         assert np.array_equal(bits(d_map.cpu().numpy()), bits(want)), where
 
 
+@pytest.mark.parametrize("pw,ph,pad,gray", [(1024, 600, 0, False), (1001, 530, 3, False), (1501, 700, 0, True),
+                                            (1500, 700, 4, True)])
+def test_pinned_host_frame_ingest(pw, ph, pad, gray):
+    """Frames in page-locked host memory (cvm_host_alloc) are read by a
+    kernel over the host link; 16-byte, 4-byte and 1-byte row alignments
+    must all give the oracle's map bit for bit."""
+    import ctypes as C
+    L = cvm.lib()
+    bpp = 1 if gray else 4
+    stride = pw * bpp + pad
+    nbytes = stride * ph
+    hp = L.cvm_host_alloc(nbytes)
+    assert hp
+    try:
+        buf = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(hp)).reshape(ph, stride)
+        src = image(31 + pw, ph, pw, bpp)
+        if not gray:
+            src[..., 3] = 255
+        buf[:, :pw * bpp] = src.reshape(ph, pw * bpp)
+        view = buf[:, :pw * bpp].reshape((ph, pw) if gray else (ph, pw, bpp))
+        tpl = np.ascontiguousarray(view[100:140, 200:260])
+        rw, rh = pw - 60 + 1, ph - 40 + 1
+        got = np.empty((rh, rw), np.float32)
+        if gray:
+            r = cvm._CResult()
+            rc = L.cvm_match_u8(hp, stride, pw, ph, tpl.ctypes.data, tpl.strides[0], 60, 40, 1, 1,
+                                got.ctypes.data, C.byref(r))
+        else:
+            rc = L.cvm_match_map(hp, stride, pw, ph, tpl.ctypes.data, tpl.strides[0], 60, 40, got.ctypes.data)
+        assert rc == 0
+        _, want = oracle.match_u8(view, tpl, 1 if gray else 3)
+        assert np.array_equal(bits(got), bits(want))
+    finally:
+        L.cvm_host_free(hp)
+
+
 def test_find_all_occurrences_via_map():
     rng = np.random.default_rng(101)
     parent = np.empty((300, 400, 4), np.uint8)
