@@ -804,7 +804,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     // one set of row prefixes for every member (each differences it at its own width)
     const int cnP = f->step == 4 ? 4 : 1;
     const int hpP = (int)align_up((size_t)pw + 1, 32);
-    const size_t prefixElems = (size_t)stat_pitch(cnP) * ph * hpP;
+    const size_t prefixElems = (size_t)(cnP == 4 ? 6 : stat_pitch(cnP)) * ph * hpP;
     const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                          Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) + frameBytes +
                          partBytes + waveBytes;

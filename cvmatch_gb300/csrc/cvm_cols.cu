@@ -306,8 +306,10 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
     constexpr int SC = N >= 1024 ? 8192 / N : 16, LSC = ilog2k(SC);
     extern __shared__ float2 smem[];
     const FftClass &fc = a.fc;
-    const int tileLocal = blockIdx.z % fc.ntiles;
-    const int slot = blockIdx.z / fc.ntiles;
+    // mode 2 (a fleet wave): members vary fastest, so the CTAs resident
+    // together read the same frame tile spectrum and share it in L2
+    const int tileLocal = MODE == 2 ? blockIdx.z / a.nmem : blockIdx.z % fc.ntiles;
+    const int slot = MODE == 2 ? blockIdx.z - tileLocal * a.nmem : blockIdx.z / fc.ntiles;
     const int tile = fc.tileFirst + tileLocal;
     const int k = blockIdx.y;
     const DevMember *m = MODE == 0 ? nullptr : &member_of(a.ms, slot);

@@ -65,6 +65,7 @@ struct ColsArgs {
     float scale;
     MemberSet ms;
     int SC, logSC;
+    int nmem;   // members of the launch (grid z = ntiles * nmem)
 };
 
 // Arguments of the forward-rows kernels (forwardRowPair, impl.go:301-344).

@@ -185,10 +185,11 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
                              unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix = 0);
 // Exclusive row prefixes P_q(x, r) (x = 0..iw), u32 modular, interleaved
-// [ih][hp][stat_pitch(cnP)] with hp >= iw + 1: the first cnP channel sums,
-// the squares of the first min(cnP,3) channels and, for cnP == 4, the
-// alpha squares (cnP + 1 values, 6 when cnP == 4).  launch_sep_stats with
-// sharedPrefix reads it with cnMax == cnP.
+// [ih][hp][stat_pitch(cnP)] with hp >= iw + 1: the first cnP channel sums
+// and the squares of the first min(cnP,3) channels.  For cnP == 4 the main
+// block holds (s0, s1, s2, RGB squares) per x ([ih][hp][4]) and a second
+// block after it (s3, alpha squares) per x ([ih][hp][2]): 6 * ih * hp u32.
+// launch_sep_stats with sharedPrefix reads it with cnMax == cnP.
 cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, int iw, int ih, int cnP,
                               unsigned int *P, int hp, cudaStream_t st);
 

@@ -1405,7 +1405,7 @@ __device__ __forceinline__ void hsum_row(const HsumArgs &a, int slot, int tw, in
 // Each member's window sum is then P[x+tw] - P[x] at its own width.
 template <int CN>
 __global__ void __launch_bounds__(256) k_row_prefix(const uint8_t *__restrict__ img, long long istride, int step,
-                                                    int iw, unsigned int *P, int hp) {
+                                                    int iw, unsigned int *P, int hp, size_t alphaOff) {
     constexpr int NQ = CN == 4 ? 6 : CN + 1;
     extern __shared__ __align__(16) unsigned int sp[];  // [NQ][iw+1]
     __shared__ unsigned int wsum[kThreads / 32][NQ];
@@ -1466,13 +1466,27 @@ __global__ void __launch_bounds__(256) k_row_prefix(const uint8_t *__restrict__ 
         }
     }
     __syncthreads();
-    constexpr int NP = stat_pitch_c(CN);
+    // CN < 4: the CN+1 values interleaved per x (pitch stat_pitch(CN));
+    // CN == 4: (s0, s1, s2, RGB squares) per x, and (s3, alpha squares) per x
+    // in a second block at alphaOff, so 3-channel readers load 16 bytes
+    constexpr int NP = CN == 4 ? 4 : stat_pitch_c(CN);
     unsigned int *out = P + (size_t)r * hp * NP;
     for (int x = tid; x <= iw; x += nt) {
         unsigned int v[NP];
+        if (CN == 4) {
+            v[0] = sp[x];
+            v[1] = sp[ld + x];
+            v[2] = sp[2 * ld + x];
+            v[3] = sp[4 * ld + x];
+        } else {
 #pragma unroll
-        for (int q = 0; q < NP; q++) v[q] = q < NQ ? sp[q * ld + x] : 0u;
+            for (int q = 0; q < NP; q++) v[q] = q < NQ ? sp[q * ld + x] : 0u;
+        }
         stv<NP>(out + (size_t)x * NP, v);
+        if (CN == 4) {
+            const unsigned int w[2] = {sp[3 * ld + x], sp[5 * ld + x]};
+            stv<2>(P + alphaOff + ((size_t)r * hp + x) * 2, w);
+        }
     }
 }
 
@@ -1509,6 +1523,7 @@ __global__ void __launch_bounds__(256) k_hsum(HsumArgs a) {
 struct VstatArgs {
     const unsigned int *H;    // per-slot window sums, or (PRE) the shared row prefix
     size_t slotStride;
+    size_t alphaOff;          // PRE with a 4-channel prefix: the (s3, alpha squares) block
     int hp;
     MemberSet ms;
     int BV;
@@ -1519,10 +1534,12 @@ struct VstatArgs {
 // and 5 (alpha) when PCN == 4 (a cn = 3 member leaves alpha out).
 template <int CN, bool PRE, int PCN>
 __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &m, const DevParams &Pm) {
-    constexpr int NP = PRE ? stat_pitch_c(PCN) : stat_pitch_c(CN);
-    const int slot = blockIdx.z;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int Y0 = blockIdx.y * a.BV;
+    constexpr int NP = PRE ? (PCN == 4 ? 4 : stat_pitch_c(PCN)) : stat_pitch_c(CN);
+    // PRE (a fleet wave): members vary fastest across the grid, so the
+    // CTAs resident together read the same prefix region and share it in L2
+    const int slot = PRE ? blockIdx.x : blockIdx.z;
+    const int x = (PRE ? blockIdx.y : blockIdx.x) * blockDim.x + threadIdx.x;
+    const int Y0 = (PRE ? blockIdx.z : blockIdx.y) * a.BV;
     if (x >= m.rw || Y0 >= m.rh) return;
     const int Bv = min(a.BV, m.rh - Y0);
     const int th = m.th;
@@ -1541,11 +1558,25 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             unsigned int Bq[NP];
             ldv<NP>(Bq, h);
 #pragma unroll
-            for (int q = 0; q < CN; q++) hv[q] = A[q] - Bq[q];
-            if (PCN == 4)
-                hv[CN] = CN == 4 ? (A[4] - Bq[4]) + (A[5] - Bq[5]) : A[4] - Bq[4];
-            else
+            if (PCN == 4) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) hv[q] = A[q] - Bq[q];
+                if (CN == 4) {
+                    // the alpha block: same row and column, pitch 2
+                    const unsigned int *ha = a.H + a.alphaOff + (size_t)(h - H) / NP * 2 + (size_t)x * 2;
+                    unsigned int A2[2], B2[2];
+                    ldv<2>(A2, ha + 2 * m.tw);
+                    ldv<2>(B2, ha);
+                    hv[3] = A2[0] - B2[0];
+                    hv[CN] = (A[3] - Bq[3]) + (A2[1] - B2[1]);
+                } else {
+                    hv[CN] = A[3] - Bq[3];
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < CN; q++) hv[q] = A[q] - Bq[q];
                 hv[CN] = A[PCN] - Bq[PCN];
+            }
         }
     };
     unsigned int s[CN];
@@ -1606,7 +1637,7 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
 
 template <int CNA, int CNB, bool PRE>
 __global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
-    const DevMember &m = member_of(a.ms, blockIdx.z);
+    const DevMember &m = member_of(a.ms, PRE ? blockIdx.x : blockIdx.z);
     const DevParams &Pm = a.ms.params[m.pIdx];
     if (Pm.flat) return;
     if (Pm.cn == CNA)
@@ -1803,6 +1834,7 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     a.cnDev = cnDev;
     a.scale = scale;
     a.ms = ms;
+    a.nmem = mode == 0 ? 1 : nmembers;
     int SC = 8192 / fc.dftH;
     if (SC > 16) SC = 16;
     if (SC < 1) SC = 1;
@@ -1961,6 +1993,8 @@ static int vstat_band(const SepGrid &sg, int nmembers) {
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
                              unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix) {
+    // a shared 4-channel prefix keeps its (s3, alpha squares) block after
+    // the ih x hp x 4 main block (launch_row_prefix)
     HsumArgs h;
     h.img = img;
     h.istride = istride;
@@ -1979,11 +2013,13 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     VstatArgs v;
     v.H = H;
     v.slotStride = slotStride;
+    v.alphaOff = (size_t)ih * sg.hp * 4;
     v.hp = sg.hp;
     v.ms = ms;
     v.BV = vstat_band(sg, nmembers);
     const size_t smem = (size_t)(cnMax + 1) * (iw + 1) * sizeof(unsigned int);
-    dim3 gh(ih, 1, nmembers), gv(sg.ncx, (sg.rhMax + v.BV - 1) / v.BV, nmembers);
+    const int nb = (sg.rhMax + v.BV - 1) / v.BV;
+    dim3 gh(ih, 1, nmembers), gv = sharedPrefix ? dim3(nmembers, sg.ncx, nb) : dim3(sg.ncx, nb, nmembers);
     if (!sharedPrefix) {
         ProfScope ps("k_hsum", st);
         if (cnMax == 1) {
@@ -2030,12 +2066,13 @@ cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, i
                               unsigned int *P, int hp, cudaStream_t st) {
     const int nq = cnP == 4 ? 6 : cnP + 1;
     const size_t smem = (size_t)nq * (iw + 1) * sizeof(unsigned int);
+    const size_t ao = (size_t)ih * hp * 4;
     ProfScope ps("k_row_prefix", st);
     switch (cnP) {
-        case 1: set_smem(k_row_prefix<1>, smem); k_row_prefix<1><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
-        case 2: set_smem(k_row_prefix<2>, smem); k_row_prefix<2><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
-        case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
-        default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp); break;
+        case 1: set_smem(k_row_prefix<1>, smem); k_row_prefix<1><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp, ao); break;
+        case 2: set_smem(k_row_prefix<2>, smem); k_row_prefix<2><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp, ao); break;
+        case 3: set_smem(k_row_prefix<3>, smem); k_row_prefix<3><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp, ao); break;
+        default: set_smem(k_row_prefix<4>, smem); k_row_prefix<4><<<ih, kThreads, smem, st>>>(img, istride, step, iw, P, hp, ao); break;
     }
     count_launches(1);
     return cudaGetLastError();
