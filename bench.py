@@ -423,7 +423,9 @@ def fft_flops(n):
 
 def c2_models(L):
     """Algorithmic bytes and flops per launch of each kernel on the
-    benchmark workload (cn = 3 after the alpha scan; RGBA input)."""
+    benchmark workload (cn = 3 after the alpha scan; RGBA input): the HBM
+    bytes each kernel must read and write by design (frame, spectra,
+    window sums, per-result lanes) and the radix-4 engine's flops."""
     import ctypes as C
     tw, th, iw, ih, cn = 96, 32, 1920, 1080, 3
     rw, rh = iw - tw + 1, ih - th + 1
@@ -432,7 +434,7 @@ def c2_models(L):
     dftW, dftH, bW, bH, dh2, ntiles = list(out)
     hw = dftW // 2 + 1
     ntx, nty = -(-rw // bW), -(-rh // bH)
-    m = {k: [0.0, 0.0] for k in ("k_fwd_rows", "k_cols_fwd_mul_inv", "k_inv_rows", "k_sat_rows", "k_sat_cols")}
+    m = {k: [0.0, 0.0] for k in ("k_prep", "k_fwd_rows", "k_cols_fwd_mul_inv", "k_inv_rows", "k_hsum", "k_vstats")}
     for t in range(ntiles):
         tx, ty = t % ntx, t // ntx
         x0, y0 = tx * bW, ty * bH
@@ -447,13 +449,27 @@ def c2_models(L):
         m["k_cols_fwd_mul_inv"][0] += cn * (loaded * hw * 8 + H * hw * 8 + rows_out * hw * 8)
         m["k_cols_fwd_mul_inv"][1] += cn * hw * (2 * fft_flops(H) + 6 * H)
         m["k_inv_rows"][0] += cn * rows_out * hw * 8
-        m["k_inv_rows"][1] += cn * (rows_out // 2) * (fft_flops(dftW) + 2 * dftW) + bw * bh * 30
-    plane = (iw + 1) * (ih + 1)
-    m["k_inv_rows"][0] += plane * (cn * 4 + 8)
-    sat = plane * (4 * 4 + 2 * 8)
-    m["k_sat_rows"][0] = iw * ih * 4 + sat
-    m["k_sat_cols"][0] = 2 * sat
+        m["k_inv_rows"][1] += cn * (rows_out // 2) * (fft_flops(dftW) + 2 * dftW) + bw * bh * 8
+    hp = -(-rw // 32) * 32
+    m["k_prep"][0] = iw * ih * 4
+    m["k_inv_rows"][0] += rw * rh * 8                       # (t, den) lane per result
+    m["k_hsum"][0] = iw * ih * 4 + ih * hp * 16             # frame in, 4 window sums per (row, x) out
+    bands = -(-rh // 16)
+    m["k_vstats"][0] = bands * (16 + th) * rw * 16 + rw * rh * 8
     return m
+
+
+def measured_traffic():
+    """DRAM bytes per launch per kernel from the committed ncu summary of
+    this workload (profiles/match_c2_dram_traffic.txt), or {}."""
+    path = os.path.join(ROOT, "profiles", "match_c2_dram_traffic.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            f = line.split("#", 1)[0].split()
+            if len(f) == 2:
+                out[f[0]] = int(f[1])
+    return out
 
 
 def profile_kernels(L, step_dev, torch, reps=20):
@@ -516,8 +532,9 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind):
                        "gflops": (fl / (per / 1e3) / 1e9) if fl else None}
     top = max(((nm, v) for nm, v in kernels.items() if v["alg_bytes"]), key=lambda kv: kv[1]["share"])
     nm, v = top
+    traffic = measured_traffic().get(nm)
     return {"bound": "hbm", "kernel": nm, "achieved": v["gbs"], "peak": peak, "unit": "GB/s",
-            "frac": v["gbs"] / peak, "peak_source": peak_kind, "traffic": None, "share": v["share"],
+            "frac": v["gbs"] / peak, "peak_source": peak_kind, "traffic": traffic, "share": v["share"],
             "alg_bytes_per_launch": v["alg_bytes"], "kernels": kernels}
 
 

@@ -269,11 +269,11 @@ int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step
     TileGeom tg;
     FftClass tf;
     template_geom(G, tw, th, tg, tf);
-    CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st));
+    CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st, 0, "k_fwd_rows_tpl"));
     const float scale = 1.0f / (float(G.p.dftW) * float(G.p.dftH));
     MemberSet none;
     memset(&none, 0, sizeof none);
-    CVM_CUDA(launch_cols(0, ts0, ts0, cnS, tg, tf, 0, cnS, cnDev, scale, none, 1, st));
+    CVM_CUDA(launch_cols(0, ts0, ts0, cnS, tg, tf, 0, cnS, cnDev, scale, none, 1, st, "k_cols_tpl"));
     if (G.nclass == 2) CVM_CUDA(launch_shrink_gather(ts0, G.p.dftH, ts1, G.dh2, tf.hwp, cnS, st));
     return CVM_OK;
 }

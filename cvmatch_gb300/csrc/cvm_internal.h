@@ -130,7 +130,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 // Channels [chanFirst, min(chanCount, *cnDev)) are transformed.
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st, int chanFirst = 0);
+                            int cnS, cudaStream_t st, int chanFirst = 0, const char *label = nullptr);
 // Column pass.  mode 0: forward only, natural output (template spectra with
 // `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
 // conj-multiply + inverse, in place on the members' scratch (solo match);
@@ -138,7 +138,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
 // member's scratch (fleet tails).  nmembers targets from ms.
 cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
                         const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
-                        const MemberSet &ms, int nmembers, cudaStream_t st);
+                        const MemberSet &ms, int nmembers, cudaStream_t st, const char *label = nullptr);
 // Inverse rows + channel accumulation + the correlation-dependent end of
 // normOne from the members' lanes, first-occurrence extrema, and the
 // member's result written by its last CTA.  Partial records of a member:

@@ -1768,7 +1768,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st, int chanFirst) {
+                            int cnS, cudaStream_t st, int chanFirst, const char *label) {
     // Channels per launch so that one row pair of the group fits 128 KB of
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
@@ -1788,7 +1788,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     const int groupLikely = (cnDev && chanCount == 4 && group == 4) ? 3 : group;
     int threads = P * groupLikely * (fc.n >= 16 ? fc.n / 16 : 1);
     threads = threads < 64 ? 64 : (threads > kThreads ? kThreads : (threads + 31) / 32 * 32);
-    ProfScope ps("k_fwd_rows", st);
+    ProfScope ps(label ? label : "k_fwd_rows", st);
     if (rows_fixed_length(fc.log2n)) {
         FwdRowsArgs a;
         a.img = img;
@@ -1821,7 +1821,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
 
 cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
                         const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
-                        const MemberSet &ms, int nmembers, cudaStream_t st) {
+                        const MemberSet &ms, int nmembers, cudaStream_t st, const char *label) {
     ColsArgs a;
     a.mode = mode;
     a.in = in;
@@ -1842,7 +1842,7 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     a.logSC = ilog2i(SC);
     dim3 grid((fc.hw + SC - 1) / SC, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
-    ProfScope ps(mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv"), st);
+    ProfScope ps(label ? label : (mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv")), st);
     if (cols_fixed_length(fc.log2H)) {
         launch_cols_fixed(a, grid, smem, st);
     } else if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
