@@ -177,6 +177,54 @@ def scene_c4(seed=4, count=256):
     return frame, tpls, where
 
 
+def scene_c5(seed=5, frames=16, ncolor=64, ngray=8):
+    """A 1920x1080 RGBA frame sequence: a 1/f^2 noise + rectangles scene,
+    each frame the previous one with 5% of the rectangles moved and the
+    sigma=2 noise redrawn; 64 colour templates of 24x24..128x96 (70% crops
+    with an a*x+b shift, 30% from an independent seed) and 8 gray crops."""
+    rng = np.random.default_rng(seed)
+    H, W = 1080, 1920
+    base = pink_noise(rng, H, W)
+    bg = np.repeat(base[..., None], 3, axis=2) + rng.standard_normal((H, W, 3)).astype(np.float32) * 20
+    rects = []
+    for _ in range(60):
+        rw, rh = (int(v) for v in rng.integers(8, 200, 2))
+        rects.append([int(rng.integers(0, W - rw)), int(rng.integers(0, H - rh)), rw, rh, rng.integers(0, 256, 3)])
+    out = []
+    for _ in range(frames):
+        for i in rng.choice(len(rects), max(1, len(rects) // 20), replace=False):
+            r = rects[i]
+            r[0] = int(np.clip(r[0] + rng.integers(-40, 41), 0, W - r[2]))
+            r[1] = int(np.clip(r[1] + rng.integers(-40, 41), 0, H - r[3]))
+        img = bg.copy()
+        for x, y, rw, rh, col in rects:
+            img[y:y + rh, x:x + rw] = col
+        img += rng.standard_normal(img.shape).astype(np.float32) * 2
+        f = np.empty((H, W, 4), np.uint8)
+        f[..., :3] = to_u8(img)
+        f[..., 3] = 255
+        out.append(f)
+    other = np.random.default_rng(seed + 1000)
+    color = []
+    for _ in range(ncolor):
+        w, h = int(rng.integers(24, 129)), int(rng.integers(24, 97))
+        t = np.empty((h, w, 4), np.uint8)
+        t[..., 3] = 255
+        if rng.random() < 0.7:
+            x, y = int(rng.integers(0, W - w)), int(rng.integers(0, H - h))
+            a, b = rng.uniform(0.9, 1.1), rng.uniform(-10, 10)
+            t[..., :3] = to_u8(out[0][y:y + h, x:x + w, :3].astype(np.float32) * a + b)
+        else:
+            t[..., :3] = other.integers(0, 256, (h, w, 3), dtype=np.uint8)
+        color.append(t)
+    gray = []
+    for _ in range(ngray):
+        w, h = int(rng.integers(24, 129)), int(rng.integers(24, 97))
+        x, y = int(rng.integers(0, W - w)), int(rng.integers(0, H - h))
+        gray.append(np.ascontiguousarray(out[0][y:y + h, x:x + w]))
+    return out, color, gray
+
+
 # ------------------------------------------------------------------ helpers
 
 
@@ -206,6 +254,10 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # start timing only once samples are flowing
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -538,6 +590,66 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind):
             "alg_bytes_per_launch": v["alg_bytes"], "kernels": kernels}
 
 
+def run_stream(args):
+    """C5: a stream of 1920x1080 RGBA frames against 64 colour templates and
+    8 gray matchers on each frame's gray conversion, through cvm_stream (the
+    per-frame pipeline replayed as a CUDA graph, two frames in flight, host
+    frames copied in and results copied out).  Reports frames/s, template
+    Mpx/s (72 templates x 2.07 Mpx per frame) and the per-frame device
+    latency p50/p99 (upload start to results back, one frame queued
+    ahead), beside the same frames through Fleet.FindAll one call at a time."""
+    import ctypes as C
+    import torch
+    import cvmatch_gb300 as cvm
+    frames, color, gray = scene_c5()
+    H, W = frames[0].shape[:2]
+    cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in color])
+    gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in gray])
+    st = cvm.NewStream(cf, gf, W, H)
+    graphed, per_frame_launches = st.info()
+    nfr = args.frames
+    K = len(frames)
+    for i in range(max(3, args.warmup)):
+        st.push(frames[i % K])
+        st.pull()
+    torch.cuda.synchronize()
+    lat = []
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for i in range(nfr):
+            st.push(frames[i % K])
+            if i >= 1:
+                lat.append(st.pull()[2])
+        lat.append(st.pull()[2])
+        wall = time.perf_counter() - t0
+    fps = nfr / wall
+    mpx = (len(color) + len(gray)) * W * H / 1e6
+    # the same frames one FindAll at a time (host buffers, no graph, no overlap)
+    g_frames = [cvm.rgba_to_gray(f) for f in frames[:4]]
+    for i in range(3):
+        cf.FindAll(frames[i % 4]), gf.FindAll(g_frames[i % 4])
+    t1 = time.perf_counter()
+    nb = min(100, nfr)
+    for i in range(nb):
+        cf.FindAll(frames[i % 4])
+        gf.FindAll(cvm.rgba_to_gray(frames[i % 4]))
+    fps_plain = nb / (time.perf_counter() - t1)
+    line = {"metric": "template*Mpx/s", "value": fps * mpx, "unit": "template*Mpx/s", "n_gpus": 1,
+            "steps": nfr, "warmup": args.warmup, "ms_per_step": 1e3 / fps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "Fleet stream: 1920x1080 RGBA frames, 64 colour templates 24x24..128x96 + 8 gray "
+                                   "matchers on the gray conversion; each frame moves 5% of the rectangles and redraws "
+                                   f"sigma=2 noise ({K} precomputed frames cycled)",
+                       "frames": nfr, "templates": len(color) + len(gray), "parent": [W, H]},
+            "frames_per_s": fps, "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "graphed": graphed, "gpu_launches": per_frame_launches,
+            "findall_per_frame_fps": fps_plain, "clocks": clk.summary(),
+            "e2e": {"value": fps * mpx, "unit": "template*Mpx/s", "h2d_bytes_per_step": int(frames[0].nbytes),
+                    "d2h_bytes_per_step": int((len(color) + len(gray)) * 24)}, "secondary": True}
+    print(json.dumps(line))
+    return 0
+
+
 def run_gpu_secondary(args):
     """Secondary workloads (not the default line): 'fleet' = Fleet.FindAll
     of 256 templates on a 2560x1440 RGBA frame, 'gray' = MatchGray
@@ -697,11 +809,12 @@ def run_gpu_secondary(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map"],
+    ap.add_argument("--frames", type=int, default=1000, help="frames for --workload stream")
+    ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map", "stream"],
                     help="match (default, the reported line) or a secondary configuration")
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
@@ -710,6 +823,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "stream":
+        return run_stream(args)
     if args.workload != "match":
         return run_gpu_secondary(args)
     return run_gpu(args)

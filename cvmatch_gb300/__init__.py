@@ -26,7 +26,7 @@ from collections import namedtuple
 import numpy as np
 
 __all__ = ["Match", "MatchMap", "MatchGray", "NewMatcher", "NewGrayMatcher", "NewFleet", "Matcher",
-           "Fleet", "Result", "CvmatchError", "Threads", "Impl", "rgba_to_gray", "alpha_const",
+           "Fleet", "NewStream", "Stream", "Result", "CvmatchError", "Threads", "Impl", "rgba_to_gray", "alpha_const",
            "match_u8", "library_path", "lib"]
 
 # The Go package's knobs, kept for API compatibility.  The GPU path has no
@@ -97,6 +97,12 @@ def lib():
             L.cvm_fleet_find_all_device.argtypes = [vp, u8p, i64, i32, i32, vp, vp]
             L.cvm_fleet_free.argtypes = [vp]
             L.cvm_fleet_free.restype = None
+            L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
+            L.cvm_stream_push.argtypes = [vp, u8p, i64]
+            L.cvm_stream_pull.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
+            L.cvm_stream_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+            L.cvm_stream_free.argtypes = [vp]
+            L.cvm_stream_free.restype = None
             L.cvm_host_alloc.argtypes = [C.c_size_t]
             L.cvm_host_alloc.restype = vp
             L.cvm_host_free.argtypes = [vp]
@@ -298,3 +304,47 @@ def NewFleet(*ms) -> Fleet:
     if len(ms) == 1 and isinstance(ms[0], (list, tuple)):
         ms = tuple(ms[0])
     return Fleet(ms)
+
+
+class Stream:
+    """A stream of equal-size RGBA frames matched against a colour fleet and
+    optionally a gray fleet on each frame's gray conversion; the per-frame
+    pipeline replays as a CUDA graph, and two frames may be in flight.
+    Results equal Fleet.FindAll per frame."""
+
+    def __init__(self, color: Fleet, gray, pw: int, ph: int):
+        self._color, self._gray = color, gray  # the fleets must outlive the stream
+        h_ = C.c_void_p()
+        _check(lib().cvm_stream_new(color._h, gray._h if gray is not None else None, pw, ph, C.byref(h_)))
+        self._h = h_
+        self._pw, self._ph = pw, ph
+
+    def push(self, frame):
+        a, p, s, w, h = _view(frame, 4)
+        if (w, h) != (self._pw, self._ph):
+            raise CvmatchError(1, "cvmatch_gpu: frame size differs from the stream's")
+        _check(lib().cvm_stream_push(self._h, p, s))
+
+    def pull(self):
+        """(colour results, gray results, device ms) of the oldest frame."""
+        nc, ng = len(self._color), len(self._gray) if self._gray is not None else 0
+        oc, og = (_CResult * nc)(), (_CResult * max(ng, 1))()
+        ms = C.c_double()
+        _check(lib().cvm_stream_pull(self._h, oc, og if ng else None, C.byref(ms)))
+        return [Result(*o.tuple()) for o in oc], [Result(*o.tuple()) for o in og[:ng]], ms.value
+
+    def info(self):
+        """(graphed, kernel launches per frame)."""
+        g, n = C.c_int(), C.c_int()
+        _check(lib().cvm_stream_info(self._h, C.byref(g), C.byref(n)))
+        return bool(g.value), n.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.cvm_stream_free(h)
+            self._h = None
+
+
+def NewStream(color: Fleet, gray, pw: int, ph: int) -> Stream:
+    return Stream(color, gray, pw, ph)

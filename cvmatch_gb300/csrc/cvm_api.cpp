@@ -884,6 +884,88 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
 
 // ================================================================= C ABI
 
+// ========================================================= frame streams
+
+struct cvm_stream {
+    cvm_fleet *color = nullptr, *gray = nullptr;
+    int pw = 0, ph = 0;
+    size_t pitch = 0, gpitch = 0;
+    int nColor = 0, nGray = 0;
+    cudaStream_t cs = nullptr;  // matching
+    cudaStream_t xs = nullptr;  // frame uploads
+    struct Slot {
+        uint8_t *hFrame = nullptr;   // page-locked staging
+        uint8_t *dFrame = nullptr, *dGray = nullptr;
+        cvm_result *dOut = nullptr;  // colour results then gray results
+        cvm_result *hOut = nullptr;  // page-locked copy of dOut
+        cudaGraphExec_t exec = nullptr;
+        cudaEvent_t t0 = nullptr, copied = nullptr, done = nullptr;
+        bool busy = false;
+    } slot[2];
+    int next = 0;          // slot of the next push
+    int oldest = 0;        // slot of the next pull
+    int inflight = 0;
+    int graphed = 0;
+    int launches = 0;
+    ~cvm_stream() {
+        for (Slot &sl : slot) {
+            if (sl.busy && sl.done) cudaEventSynchronize(sl.done);
+            if (sl.exec) cudaGraphExecDestroy(sl.exec);
+            if (sl.hFrame) cudaFreeHost(sl.hFrame);
+            if (sl.hOut) cudaFreeHost(sl.hOut);
+            if (sl.dFrame) cudaFree(sl.dFrame);
+            if (sl.dGray) cudaFree(sl.dGray);
+            if (sl.dOut) cudaFree(sl.dOut);
+            for (cudaEvent_t e : {sl.t0, sl.copied, sl.done})
+                if (e) cudaEventDestroy(e);
+        }
+        if (cs) cudaStreamDestroy(cs);
+        if (xs) cudaStreamDestroy(xs);
+    }
+};
+
+namespace {
+
+// The per-frame pipeline of one slot on s->cs: both FindAlls, the gray
+// conversion between them, the results back to page-locked memory.
+int stream_pipeline(cvm_stream *s, cvm_stream::Slot &sl) {
+    CVM_TRY(fleet_find_dev(s->color, sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dOut, s->cs));
+    if (s->gray) {
+        CVM_CUDA(launch_gray(sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dGray, (long long)s->gpitch, s->cs));
+        CVM_TRY(fleet_find_dev(s->gray, sl.dGray, (long long)s->gpitch, s->pw, s->ph, sl.dOut + s->nColor, s->cs));
+    }
+    CVM_CUDA(cudaMemcpyAsync(sl.hOut, sl.dOut, (size_t)(s->nColor + s->nGray) * sizeof(cvm_result),
+                             cudaMemcpyDeviceToHost, s->cs));
+    return CVM_OK;
+}
+
+// Capture the slot's pipeline as a graph.  The caches it reads (plans,
+// member spectra) are built by an uncaptured run first.  On any capture
+// failure the stream keeps issuing the pipeline launch by launch.
+void stream_capture(cvm_stream *s, cvm_stream::Slot &sl) {
+    if (cudaStreamBeginCapture(s->cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const uint64_t l0 = g_launches.load();
+    const int rc = stream_pipeline(s, sl);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->cs, &g);
+    if (rc != CVM_OK || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return;
+    }
+    s->launches = (int)(g_launches.load() - l0);
+    if (cudaGraphInstantiate(&sl.exec, g, 0) != cudaSuccess) {
+        sl.exec = nullptr;
+        cudaGetLastError();
+    }
+    cudaGraphDestroy(g);
+}
+
+}  // namespace
+
 extern "C" {
 
 size_t cvm_last_error(char *buf, size_t len) {
@@ -1152,6 +1234,108 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 }
 
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_stream_new(cvm_fleet *color, cvm_fleet *gray, int pw, int ph, cvm_stream **out) {
+    if (!out) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil output handle");
+    *out = nullptr;
+    if (!color || color->ms.empty()) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    if (color->step != 4) return fail(CVM_ERR_MIXED_FLEET, "cvmatch_gpu: the colour fleet of a stream must be RGBA");
+    if (gray && (gray->ms.empty() || gray->step != 1))
+        return fail(CVM_ERR_MIXED_FLEET, "cvmatch_gpu: the gray fleet of a stream must hold gray matchers");
+    if (pw < 1 || ph < 1) return fail(CVM_ERR_EMPTY_IMAGE, "cvmatch: empty image");
+    CVM_TRY(ensure_device());
+    auto s = std::make_unique<cvm_stream>();
+    s->color = color;
+    s->gray = gray;
+    s->pw = pw;
+    s->ph = ph;
+    s->pitch = align_up((size_t)pw * 4, 128);
+    s->gpitch = align_up((size_t)pw, 128);
+    s->nColor = (int)color->ms.size();
+    s->nGray = gray ? (int)gray->ms.size() : 0;
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    CVM_CUDA(cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking));
+    CVM_CUDA(cudaStreamCreateWithPriority(&s->xs, cudaStreamNonBlocking, greatest));
+    const size_t nres = (size_t)(s->nColor + s->nGray);
+    for (cvm_stream::Slot &sl : s->slot) {
+        CVM_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&sl.hFrame), s->pitch * ph, cudaHostAllocDefault));
+        CVM_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&sl.hOut), nres * sizeof(cvm_result), cudaHostAllocDefault));
+        CVM_CUDA(cudaMalloc(&sl.dFrame, s->pitch * ph));
+        if (gray) CVM_CUDA(cudaMalloc(&sl.dGray, s->gpitch * ph));
+        CVM_CUDA(cudaMalloc(&sl.dOut, nres * sizeof(cvm_result)));
+        CVM_CUDA(cudaEventCreate(&sl.t0));
+        CVM_CUDA(cudaEventCreate(&sl.copied));
+        CVM_CUDA(cudaEventCreate(&sl.done));
+        CVM_CUDA(cudaMemsetAsync(sl.dFrame, 0, s->pitch * ph, s->cs));
+    }
+    // build the fleets' caches for this frame size, then capture each slot
+    CVM_TRY(stream_pipeline(s.get(), s->slot[0]));
+    CVM_CUDA(cudaStreamSynchronize(s->cs));
+    for (cvm_stream::Slot &sl : s->slot) stream_capture(s.get(), sl);
+    s->graphed = s->slot[0].exec && s->slot[1].exec;
+    if (!s->graphed) {
+        for (cvm_stream::Slot &sl : s->slot)
+            if (sl.exec) {
+                cudaGraphExecDestroy(sl.exec);
+                sl.exec = nullptr;
+            }
+    }
+    *out = s.release();
+    return CVM_OK;
+}
+
+int cvm_stream_push(cvm_stream *s, const uint8_t *rgba, int64_t stride) {
+    if (!s) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil stream");
+    if (!rgba) return fail(CVM_ERR_NIL_IMAGE, "cvmatch: nil image");
+    if (stride < (int64_t)s->pw * 4) return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*4");
+    if (s->inflight == 2) return fail(CVM_ERR_ARGS, "cvmatch_gpu: two frames in flight; pull one first");
+    cvm_stream::Slot &sl = s->slot[s->next];
+    // the slot's previous upload has left the staging buffer (its frame was pulled)
+    CVM_CUDA(cudaEventSynchronize(sl.copied));
+    const size_t row = (size_t)s->pw * 4;
+    for (int y = 0; y < s->ph; y++) memcpy(sl.hFrame + (size_t)y * s->pitch, rgba + (size_t)y * stride, row);
+    CVM_CUDA(cudaEventRecord(sl.t0, s->xs));
+    CVM_CUDA(cudaMemcpyAsync(sl.dFrame, sl.hFrame, s->pitch * s->ph, cudaMemcpyHostToDevice, s->xs));
+    CVM_CUDA(cudaEventRecord(sl.copied, s->xs));
+    CVM_CUDA(cudaStreamWaitEvent(s->cs, sl.copied, 0));
+    if (s->graphed)
+        CVM_CUDA(cudaGraphLaunch(sl.exec, s->cs));
+    else
+        CVM_TRY(stream_pipeline(s, sl));
+    CVM_CUDA(cudaEventRecord(sl.done, s->cs));
+    sl.busy = true;
+    s->next ^= 1;
+    s->inflight++;
+    return CVM_OK;
+}
+
+int cvm_stream_pull(cvm_stream *s, cvm_result *color_out, cvm_result *gray_out, double *device_ms) {
+    if (!s) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil stream");
+    if (s->inflight == 0) return fail(CVM_ERR_ARGS, "cvmatch_gpu: no frame in flight");
+    cvm_stream::Slot &sl = s->slot[s->oldest];
+    CVM_CUDA(cudaEventSynchronize(sl.done));
+    if (color_out) memcpy(color_out, sl.hOut, (size_t)s->nColor * sizeof(cvm_result));
+    if (gray_out && s->nGray) memcpy(gray_out, sl.hOut + s->nColor, (size_t)s->nGray * sizeof(cvm_result));
+    if (device_ms) {
+        float ms = 0;
+        CVM_CUDA(cudaEventElapsedTime(&ms, sl.t0, sl.done));
+        *device_ms = ms;
+    }
+    sl.busy = false;
+    s->oldest ^= 1;
+    s->inflight--;
+    return CVM_OK;
+}
+
+int cvm_stream_info(cvm_stream *s, int *graphed, int *launches) {
+    if (!s) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil stream");
+    if (graphed) *graphed = s->graphed;
+    if (launches) *launches = s->launches;
+    return CVM_OK;
+}
+
+void cvm_stream_free(cvm_stream *s) { delete s; }
 
 int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]) {
     if (tw < 1 || th < 1 || rw < 1 || rh < 1 || !out)

@@ -165,6 +165,32 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 
 void cvm_fleet_free(cvm_fleet *f);
 
+/* ------------------------------------------------------- frame streams */
+
+/* A stream of RGBA frames of one size matched against a colour fleet and,
+ * optionally, a gray fleet on each frame's gray conversion (rgbToGray,
+ * cvmatch.go:222-240) -- the loop a caller would write around
+ * Fleet.FindAll (fleet.go:176-332) for a video feed; no reference
+ * counterpart as an object.  The per-frame pipeline (frame upload, both
+ * FindAlls, the gray conversion, result read-back) is captured once as a
+ * CUDA graph per frame slot and replayed; two slots let one frame's upload
+ * overlap the previous frame's matching.  Results are identical to calling
+ * cvm_fleet_find_all per frame.  The fleets must outlive the stream. */
+typedef struct cvm_stream cvm_stream;
+int cvm_stream_new(cvm_fleet *color, cvm_fleet *gray_or_null, int pw, int ph, cvm_stream **out);
+/* Queue one frame (pw x ph RGBA, row stride in bytes); the pixels are
+ * copied before the call returns.  With both slots in flight it first
+ * waits for the oldest frame. */
+int cvm_stream_push(cvm_stream *s, const uint8_t *rgba, int64_t stride);
+/* Results of the oldest queued frame (waits for it): color_out receives the
+ * colour fleet's n results, gray_out the gray fleet's (may be null without
+ * one); device_ms (nullable) the frame's upload-to-results time. */
+int cvm_stream_pull(cvm_stream *s, cvm_result *color_out, cvm_result *gray_out, double *device_ms);
+/* 1 when the per-frame pipeline runs as a CUDA graph, 0 when it is issued
+ * launch by launch (capture unavailable); kernels per frame in *launches. */
+int cvm_stream_info(cvm_stream *s, int *graphed, int *launches);
+void cvm_stream_free(cvm_stream *s);
+
 /* ------------------------------------------------------------- support */
 
 /* The tile geometry the library plans for a tw x th template over a

@@ -518,3 +518,40 @@ def test_very_wide_colour_template_global_column_arrays():
     to, mo = oracle.match_u8(img, tpl, 4, threads=16)
     assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
     assert (t[4], t[5]) == (50, 11)
+
+
+# ------------------------------------------------------------ frame streams
+
+
+def test_stream_equals_find_all_per_frame():
+    """A frame stream (colour fleet + gray fleet on the gray conversion,
+    replayed as a CUDA graph, two frames in flight) gives exactly the
+    results of Fleet.FindAll on each frame."""
+    rng = np.random.default_rng(55)
+    H, W = 300, 420
+    frames = []
+    base = rgba(61, H, W)
+    for i in range(5):
+        f = base.copy()
+        y, x = int(rng.integers(0, H - 40)), int(rng.integers(0, W - 60))
+        f[y:y + 40, x:x + 60, :3] = rng.integers(0, 256, (40, 60, 3), dtype=np.uint8)
+        frames.append(f)
+    tc = [base[10:34, 20:60].copy(), base[100:150, 200:230].copy(), rgba(62, 24, 24), base[200:296, 300:400].copy()]
+    tg = [cvm.rgba_to_gray(base[50:80, 50:90]), cvm.rgba_to_gray(base[150:180, 250:310])]
+    cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tc])
+    gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in tg])
+    st = cvm.NewStream(cf, gf, W, H)
+    graphed, launches = st.info()
+    assert graphed and launches > 0
+    got = []
+    for i, f in enumerate(frames):
+        st.push(f)
+        if i >= 1:
+            got.append(st.pull())
+    got.append(st.pull())
+    for f, (rc, rg, ms) in zip(frames, got):
+        want_c = cf.FindAll(f)
+        want_g = gf.FindAll(cvm.rgba_to_gray(f))
+        assert [tuple(r) for r in rc] == [tuple(r) for r in want_c]
+        assert [tuple(r) for r in rg] == [tuple(r) for r in want_g]
+        assert ms > 0
