@@ -26,7 +26,7 @@ from collections import namedtuple
 import numpy as np
 
 __all__ = ["Match", "MatchMap", "MatchGray", "NewMatcher", "NewGrayMatcher", "NewFleet", "Matcher",
-           "Fleet", "NewStream", "Stream", "Result", "CvmatchError", "Threads", "Impl", "rgba_to_gray", "alpha_const",
+           "Fleet", "NewStream", "Stream", "MatchMapPeaks", "Result", "CvmatchError", "Threads", "Impl", "rgba_to_gray", "alpha_const",
            "match_u8", "library_path", "lib"]
 
 # The Go package's knobs, kept for API compatibility.  The GPU path has no
@@ -84,6 +84,9 @@ def lib():
             L.cvm_match_gray_rgba.argtypes = img_args + [R]
             L.cvm_match_u8.argtypes = img_args + [i32, i32, vp, R]
             L.cvm_match_u8_device.argtypes = img_args + [i32, i32, vp, vp, vp]
+            L.cvm_match_map_peaks.argtypes = img_args + [C.c_float, i32, i32, vp, i32, C.POINTER(C.c_int32)]
+            L.cvm_match_u8_peaks.argtypes = img_args + [i32, i32, C.c_float, i32, i32, vp, i32, C.POINTER(C.c_int32)]
+            L.cvm_peaks_device.argtypes = [vp, i32, i32, C.c_float, i32, i32, vp, i32, vp, vp]
             L.cvm_match_device.argtypes = img_args + [vp, vp, vp]
             L.cvm_rgba_to_gray.argtypes = [u8p, i64, i32, i32, vp]
             L.cvm_alpha_const.argtypes = [u8p, i64, i32, i32, C.POINTER(C.c_int)]
@@ -165,6 +168,21 @@ def MatchMap(parent, sub):
     res = np.empty((max(h, 1), max(w, 1)), np.float32)
     _check(lib().cvm_match_map(pp, ps, pw, ph, sp, ss, sw, sh, res.ctypes.data))
     return res, w, h
+
+
+def MatchMapPeaks(parent, sub, thresh: float, rx: int, ry: int, max_peaks: int = 4096):
+    """Every occurrence by the MatchMap recipe (cvmatch_test.go:324-381):
+    scores >= thresh that no neighbour within +-rx columns / +-ry rows
+    exceeds, in raster order, computed on the device.  Returns (list of
+    (x, y) up to max_peaks, total count)."""
+    pa, pp, ps, pw, ph = _view(parent, 4)
+    sa, sp, ss, sw, sh = _view(sub, 4)
+    xy = np.empty((max(max_peaks, 1), 2), np.int32)
+    cnt = C.c_int32()
+    _check(lib().cvm_match_map_peaks(pp, ps, pw, ph, sp, ss, sw, sh, float(thresh), rx, ry, xy.ctypes.data,
+                                     max_peaks, C.byref(cnt)))
+    n = min(cnt.value, max_peaks)
+    return [(int(x), int(y)) for x, y in xy[:n]], cnt.value
 
 
 def rgba_to_gray(img) -> np.ndarray:

@@ -513,9 +513,19 @@ int upload_image(PoolBuf &b, const uint8_t *src, long long stride, int w, int h,
 }
 
 // One-shot host-buffer match: upload both images, run, read back.
+// Occurrence extraction requested from a one-shot call: the map stays on
+// the device and only the occurrences come back.
+struct PeakReq {
+    float thresh;
+    int rx, ry;
+    int32_t *xy;
+    int maxPeaks;
+    int32_t *count;
+};
+
 int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8_t *tpl, long long tstride,
               int tw, int th, int mode, int cnFixed, int step, int grayFromRgba, float *map,
-              cvm_result *out) {
+              cvm_result *out, const PeakReq *pk = nullptr) {
     CVM_TRY(ensure_device());
     cudaStream_t st = thread_stream();
     PoolBuf bi, bt, gi, gt, bm, bo;
@@ -537,7 +547,7 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     }
     const int rw = iw - tw + 1, rh = ih - th + 1;
     float *dMap = nullptr;
-    if (map) {
+    if (map || pk) {
         CVM_TRY(pool_alloc(bm, (size_t)rw * rh * sizeof(float), st));
         dMap = static_cast<float *>(bm.p);
     }
@@ -559,6 +569,17 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     J.out = static_cast<cvm_result *>(bo.p);
     CVM_TRY(run_solo(J, st));
     if (map) CVM_CUDA(cudaMemcpyAsync(map, dMap, (size_t)rw * rh * sizeof(float), cudaMemcpyDeviceToHost, st));
+    PoolBuf bp;
+    if (pk) {
+        const size_t nsc = peaks_scratch_ints(rw, rh);
+        const size_t xyBytes = (size_t)std::max(pk->maxPeaks, 0) * 2 * sizeof(int32_t);
+        CVM_TRY(pool_alloc(bp, (nsc + 1) * sizeof(int) + xyBytes, st));
+        int *scr = static_cast<int *>(bp.p), *dCount = scr + nsc;
+        int32_t *dXY = reinterpret_cast<int32_t *>(dCount + 1);
+        CVM_CUDA(launch_peaks(dMap, rw, rh, pk->thresh, pk->rx, pk->ry, scr, dXY, pk->maxPeaks, dCount, st));
+        CVM_CUDA(cudaMemcpyAsync(pk->count, dCount, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        if (xyBytes) CVM_CUDA(cudaMemcpyAsync(pk->xy, dXY, xyBytes, cudaMemcpyDeviceToHost, st));
+    }
     CVM_CUDA(cudaMemcpyAsync(out, bo.p, sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
     CVM_CUDA(cudaStreamSynchronize(st));
     return CVM_OK;
@@ -994,6 +1015,43 @@ int cvm_match_map(const uint8_t *parent, int64_t pstride, int pw, int ph, const 
     if (!map) return fail(CVM_ERR_ARGS, "cvmatch_gpu: MatchMap needs a map buffer");
     cvm_result r;
     return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 1, 4, 4, 0, map, &r);
+}
+
+int cvm_match_map_peaks(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride,
+                        int sw, int sh, float thresh, int rx, int ry, int32_t *xy, int max_peaks, int32_t *count) {
+    CVM_TRY(check_image(parent, pw, ph));
+    CVM_TRY(check_image(sub, sw, sh));
+    CVM_TRY(check_match_rgba(parent, pstride, pw, ph, sub, sstride, sw, sh));
+    if (!count || max_peaks < 0 || (max_peaks > 0 && !xy) || rx < 0 || ry < 0 || ph - sh + 1 > 65535)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad occurrence request");
+    cvm_result r;
+    const PeakReq pk{thresh, rx, ry, xy, max_peaks, count};
+    return host_solo(parent, pstride, pw, ph, sub, sstride, sw, sh, 1, 4, 4, 0, nullptr, &r, &pk);
+}
+
+int cvm_match_u8_peaks(const uint8_t *img, int64_t istride, int iw, int ih, const uint8_t *tpl, int64_t tstride,
+                       int tw, int th, int cn, int step, float thresh, int rx, int ry, int32_t *xy, int max_peaks,
+                       int32_t *count) {
+    CVM_TRY(check_match_args(iw, ih, istride, tstride, tw, th, cn, step));
+    if (!img || !tpl) return fail(CVM_ERR_NIL_IMAGE, "cvmatch: nil image");
+    if (!count || max_peaks < 0 || (max_peaks > 0 && !xy) || rx < 0 || ry < 0 || ih - th + 1 > 65535)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad occurrence request");
+    cvm_result r;
+    const PeakReq pk{thresh, rx, ry, xy, max_peaks, count};
+    return host_solo(img, istride, iw, ih, tpl, tstride, tw, th, 0, cn, step, 0, nullptr, &r, &pk);
+}
+
+int cvm_peaks_device(const float *d_map, int w, int h, float thresh, int rx, int ry, int32_t *d_xy, int max_peaks,
+                     int32_t *d_count, void *stream) {
+    if (!d_map || !d_count || w < 1 || h < 1 || h > 65535 || max_peaks < 0 || (max_peaks > 0 && !d_xy) || rx < 0 ||
+        ry < 0)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad occurrence request");
+    CVM_TRY(ensure_device());
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    PoolBuf b;
+    CVM_TRY(pool_alloc(b, peaks_scratch_ints(w, h) * sizeof(int), st));
+    CVM_CUDA(launch_peaks(d_map, w, h, thresh, rx, ry, static_cast<int *>(b.p), d_xy, max_peaks, d_count, st));
+    return CVM_OK;
 }
 
 int cvm_match_gray(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride,

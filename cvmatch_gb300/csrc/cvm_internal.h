@@ -203,6 +203,14 @@ cudaError_t launch_ingest(void *dst, size_t dpitch, const void *src, size_t spit
 cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int dh2, int hwp, int cnS,
                                  cudaStream_t st);
 
+// Every occurrence of a score map (the MatchMap recipe of
+// cvmatch_test.go:324-381): scratch holds peaks_scratch_ints(w, h) ints;
+// *count (device) receives the number of occurrences, xy the first
+// maxPeaks of them in raster order as (x, y) pairs.
+size_t peaks_scratch_ints(int w, int h);
+cudaError_t launch_peaks(const float *map, int w, int h, float thresh, int rx, int ry, int *scratch, int32_t *xy,
+                         int maxPeaks, int *count, cudaStream_t st);
+
 // kernel-launch counter (exported by cvm_launch_count)
 void count_launches(unsigned n);
 

@@ -147,6 +147,26 @@ int cvm_matcher_find_device(cvm_matcher *m, const uint8_t *d_parent, int64_t pst
 
 void cvm_matcher_free(cvm_matcher *m);
 
+/* ---------------------------------------------------- every occurrence */
+
+/* The MatchMap recipe for every occurrence (cvmatch_test.go:324-381,
+ * README.md:82-90) on the device: (x, y) is an occurrence when its score is
+ * not below thresh and no score within dx in [-rx, rx], dy in [-ry, ry]
+ * (clipped to the map) is strictly greater.  *count receives the number of
+ * occurrences, xy the first max_peaks of them in raster order as (x, y)
+ * pairs.  The map never leaves the device.  No reference counterpart as a
+ * function: the reference leaves the recipe to its callers. */
+int cvm_match_map_peaks(const uint8_t *parent, int64_t pstride, int pw, int ph, const uint8_t *sub, int64_t sstride,
+                        int sw, int sh, float thresh, int rx, int ry, int32_t *xy, int max_peaks, int32_t *count);
+/* The same on matchU8's raw views (impl.go:1126-1155). */
+int cvm_match_u8_peaks(const uint8_t *img, int64_t istride, int iw, int ih, const uint8_t *tpl, int64_t tstride,
+                       int tw, int th, int cn, int step, float thresh, int rx, int ry, int32_t *xy, int max_peaks,
+                       int32_t *count);
+/* The recipe on a device-resident w x h map (from cvm_match_u8_device or
+ * cvm_match_device); d_xy/d_count are device pointers; queued on stream. */
+int cvm_peaks_device(const float *d_map, int w, int h, float thresh, int rx, int ry, int32_t *d_xy, int max_peaks,
+                     int32_t *d_count, void *stream);
+
 /* --------------------------------------------------------------- Fleet */
 
 /* NewFleet (fleet.go:85-101): the member list is copied; the matchers must

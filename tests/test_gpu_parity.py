@@ -555,3 +555,65 @@ def test_stream_equals_find_all_per_frame():
         assert [tuple(r) for r in rc] == [tuple(r) for r in want_c]
         assert [tuple(r) for r in rg] == [tuple(r) for r in want_g]
         assert ms > 0
+
+
+# ------------------------------------------------------- every occurrence
+
+
+def _recipe(m, thresh, rx, ry):
+    """The MatchMap recipe of cvmatch_test.go:324-381, in numpy."""
+    h, w = m.shape
+    out = []
+    for y, x in np.argwhere(~(m < thresh)):
+        win = m[max(0, y - ry):min(h, y + ry + 1), max(0, x - rx):min(w, x + rx + 1)]
+        if not np.any(win > m[y, x]):
+            out.append((int(x), int(y)))
+    return out
+
+
+def test_find_all_occurrences_on_device():
+    """TestFindAllOccurrences (cvmatch_test.go:324-381) with the recipe run
+    on the device: the five planted copies, nothing else, raster order."""
+    rng = np.random.default_rng(101)
+    parent = np.empty((300, 400, 4), np.uint8)
+    parent[..., :3] = rng.integers(0, 64, (300, 400, 3))
+    parent[..., 3] = 255
+    tpl = rgba(102, 24, 32)
+    spots = [(10, 12), (200, 40), (350, 260), (60, 240), (180, 150)]
+    for x, y in spots:
+        parent[y:y + 24, x:x + 32] = tpl
+    hits, n = cvm.MatchMapPeaks(parent, tpl, 0.999, 16, 12)
+    assert n == 5
+    assert hits == sorted(spots, key=lambda p: (p[1], p[0]))
+
+
+@pytest.mark.parametrize("thresh,rx,ry", [(0.2, 3, 2), (0.0, 1, 1), (0.5, 16, 12)])
+def test_occurrences_equal_recipe_and_truncate_in_raster_order(thresh, rx, ry):
+    img = rgba(71, 180, 260)
+    tpl = img[40:60, 100:130].copy()
+    m, _, _ = cvm.MatchMap(img, tpl)
+    want = _recipe(m, thresh, rx, ry)
+    hits, n = cvm.MatchMapPeaks(img, tpl, thresh, rx, ry, max_peaks=len(want) + 5)
+    assert n == len(want) and hits == want
+    k = max(1, len(want) // 3)
+    hits, n = cvm.MatchMapPeaks(img, tpl, thresh, rx, ry, max_peaks=k)
+    assert n == len(want) and hits == want[:k]
+
+
+def test_peaks_device_on_a_device_map():
+    torch = pytest.importorskip("torch")
+    L = cvm.lib()
+    rng = np.random.default_rng(9)
+    m = rng.random((70, 300)).astype(np.float32)
+    m[5, 7] = 2.0
+    d = torch.from_numpy(m).cuda()
+    xy = torch.zeros(2 * 64, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert L.cvm_peaks_device(d.data_ptr(), 300, 70, 0.9, 4, 3, xy.data_ptr(), 64, cnt.data_ptr(),
+                              torch.cuda.current_stream().cuda_stream) == 0
+    torch.cuda.synchronize()
+    want = _recipe(m, 0.9, 4, 3)
+    n = int(cnt.item())
+    assert n == len(want)
+    got = [tuple(int(v) for v in p) for p in xy.cpu().numpy().reshape(-1, 2)[:min(n, 64)]]
+    assert got == want[:64]
