@@ -100,6 +100,7 @@ def lib():
             L.cvm_fleet_find_all_device.argtypes = [vp, u8p, i64, i32, i32, vp, vp]
             L.cvm_fleet_free.argtypes = [vp]
             L.cvm_fleet_free.restype = None
+            L.cvm_fleet_set_roi.argtypes = [vp, i32, i32, i32, i32, i32]
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
             L.cvm_stream_push.argtypes = [vp, u8p, i64]
             L.cvm_stream_pull.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
@@ -306,6 +307,11 @@ class Fleet:
 
     def find_all_device(self, d_parent: int, pstride: int, pw: int, ph: int, d_out: int, stream: int = 0):
         _check(lib().cvm_fleet_find_all_device(self._h, d_parent, pstride, pw, ph, d_out, stream or None))
+
+    def SetROI(self, member: int, x: int, y: int, w: int, h: int):
+        """Restrict member (construction order) to a region of interest in
+        frame pixels; w or h <= 0 clears it (see cvm_fleet_set_roi)."""
+        _check(lib().cvm_fleet_set_roi(self._h, member, x, y, w, h))
 
     def __len__(self):
         return len(self._ms)

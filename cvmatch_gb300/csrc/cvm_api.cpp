@@ -12,6 +12,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -357,6 +358,10 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.solo.rh = rh;
     ms.solo.partBase = 0;
     ms.solo.outIdx = 0;
+    ms.solo.roiX0 = 0;
+    ms.solo.roiY0 = 0;
+    ms.solo.roiX1 = rw;
+    ms.solo.roiY1 = rh;
     ms.params = P;
     ms.map = J.map;
     ms.lanes = lanes;
@@ -689,6 +694,8 @@ struct FleetBucketGeom {
     int cnS = 1;
     std::vector<float2 *> ts;     // per member: class 0, class 1 (owned)
     DevMember *table = nullptr;   // bucket members in bucket order
+    std::vector<DevMember> tabHost;  // its host copy
+    uint64_t roiGen = 0;          // the fleet's ROI generation the table holds
     std::vector<int> members;
     size_t memberScratch[2] = {0, 0};
     ~FleetBucketGeom() {
@@ -710,6 +717,8 @@ struct cvm_fleet {
     DevParams *dP = nullptr;  // per member template statistics
     std::mutex mu;
     std::shared_ptr<FleetGeom> geom;
+    std::vector<int32_t> roi;  // per member x, y, w, h in frame pixels (w <= 0: the whole frame)
+    uint64_t roiGen = 0;       // bumped by every cvm_fleet_set_roi
     ~cvm_fleet() {
         if (dP) cudaFree(dP);
     }
@@ -719,6 +728,37 @@ namespace {
 
 // Budget for one wave of member tails' column-pass output.
 constexpr size_t kWaveBytes = size_t(4) << 30;
+
+// Member i's region of interest as result positions [r0, r2) x [r1, r3)
+// on a frame whose results span rw x rh: the positions whose tw x th
+// window lies inside the ROI (all of them without an ROI; empty when the
+// ROI cannot hold the template).  Returns false for "no ROI".
+bool member_roi(const cvm_fleet *f, int i, int rw, int rh, int tw, int th, int r[4]) {
+    r[0] = 0;
+    r[1] = 0;
+    r[2] = rw;
+    r[3] = rh;
+    if (f->roi.empty() || f->roi[4 * i + 2] <= 0 || f->roi[4 * i + 3] <= 0) return false;
+    const int x = f->roi[4 * i], y = f->roi[4 * i + 1], w = f->roi[4 * i + 2], h = f->roi[4 * i + 3];
+    r[0] = std::max(x, 0);
+    r[1] = std::max(y, 0);
+    r[2] = std::min(x + w - tw + 1, rw);
+    r[3] = std::min(y + h - th + 1, rh);
+    if (r[2] <= r[0] || r[3] <= r[1]) r[0] = r[1] = r[2] = r[3] = 0;  // empty
+    return true;
+}
+
+void table_roi(const cvm_fleet *f, const FleetBucketGeom &bg, std::vector<DevMember> &tab) {
+    for (size_t pos = 0; pos < bg.members.size(); pos++) {
+        DevMember &d = tab[pos];
+        int r[4];
+        member_roi(f, bg.members[pos], d.rw, d.rh, d.tw, d.th, r);
+        d.roiX0 = r[0];
+        d.roiY0 = r[1];
+        d.roiX1 = r[2];
+        d.roiY1 = r[3];
+    }
+}
 
 // Per parent size: every bucket's plan and every member's spectrum on its
 // bucket's plan (buildGeom, fleet.go:337-390), plus the device member
@@ -774,6 +814,9 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
             d.partBase = (int)pos * nparts;
             d.outIdx = b.members[pos];
         }
+        table_roi(f, *bg, tab);
+        bg->roiGen = f->roiGen;
+        bg->tabHost = tab;
         CVM_CUDA(cudaMalloc(&bg->table, tab.size() * sizeof(DevMember)));
         CVM_CUDA(cudaMemcpy(bg->table, tab.data(), tab.size() * sizeof(DevMember), cudaMemcpyHostToDevice));
         for (int c = 0; c < G.nclass; c++) bg->memberScratch[c] = spec_elems(G.fc[c], bg->cnS);
@@ -796,10 +839,37 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     if (pstride < (long long)pw * f->step)
         return fail(CVM_ERR_ARGS, "cvmatch: bad match arguments (%dx%d in %dx%d)", f->ms[0]->w, f->ms[0]->h, pw, ph);
     for (int i = 0; i < n; i++)
-        if (f->ms[i]->varSum == 0) CVM_CUDA(upload_bytes(dOut + i, &kFlatResult, sizeof kFlatResult, st));
+        if (f->ms[i]->varSum == 0) {
+            // a flat member scores 1 everywhere: its first result position
+            // (impl.go:1137-1144), inside its region of interest if it has one
+            cvm_matcher *m = f->ms[i];
+            int r[4];
+            cvm_result fr = kFlatResult;
+            if (member_roi(f, i, pw - m->w + 1, ph - m->h + 1, m->w, m->h, r)) {
+                if (r[2] > r[0]) {
+                    fr.min_x = fr.max_x = r[0];
+                    fr.min_y = fr.max_y = r[1];
+                } else {
+                    fr.min_v = fr.max_v = std::numeric_limits<float>::quiet_NaN();
+                    fr.min_x = fr.min_y = fr.max_x = fr.max_y = -1;
+                }
+            }
+            CVM_CUDA(upload_bytes(dOut + i, &fr, sizeof fr, st));
+        }
     if (f->buckets.empty()) return CVM_OK;
     std::shared_ptr<FleetGeom> fg;
     CVM_TRY(fleet_geom(f, pw, ph, fg));
+    {
+        // regions of interest changed since the member tables were built
+        std::lock_guard<std::mutex> lk(f->mu);
+        for (auto &bgp : fg->bg) {
+            FleetBucketGeom &bg = *bgp;
+            if (bg.roiGen == f->roiGen) continue;
+            table_roi(f, bg, bg.tabHost);
+            CVM_CUDA(upload_bytes(bg.table, bg.tabHost.data(), bg.tabHost.size() * sizeof(DevMember), st));
+            bg.roiGen = f->roiGen;
+        }
+    }
     const int cnS = f->step;
     size_t frameBytes = 0, partBytes = 0, waveBytes = 0;
     std::vector<int> wave(fg->bg.size());
@@ -879,6 +949,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         ms.params = P;
         ms.lanes = lanes;
         ms.lanesStride = (size_t)bg.rwMax * bg.rhMax;
+        ms.anyRoi = !f->roi.empty();
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -1292,6 +1363,20 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 }
 
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h) {
+    if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    const int n = (int)f->ms.size();
+    if (member < 0 || member >= n) return fail(CVM_ERR_ARGS, "cvmatch_gpu: fleet member %d of %d", member, n);
+    std::lock_guard<std::mutex> lk(f->mu);
+    if (f->roi.empty()) f->roi.assign(4 * (size_t)n, 0);
+    f->roi[4 * member] = x;
+    f->roi[4 * member + 1] = y;
+    f->roi[4 * member + 2] = w;
+    f->roi[4 * member + 3] = h;
+    f->roiGen++;
+    return CVM_OK;
+}
 
 int cvm_stream_new(cvm_fleet *color, cvm_fleet *gray, int pw, int ph, cvm_stream **out) {
     if (!out) return fail(CVM_ERR_ARGS, "cvmatch_gpu: nil output handle");

@@ -321,11 +321,12 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
         cn = a.cnDev ? min(*a.cnDev, a.chanCount) : a.chanCount;
     if (k >= cn) return;
     if (Pm && Pm->flat) return;
+    const TileBox b = tile_box(a.g, tile);
+    if (MODE == 2 && a.ms.anyRoi && roi_misses_tile(a.g, tile, b, *m)) return;  // outside the member's ROI
     const int c0 = blockIdx.x * SC;
     const int hwp = fc.hwp;
     const int wv = min(SC, fc.hw - c0);
     const size_t chanStride = (size_t)N * hwp;
-    const TileBox b = tile_box(a.g, tile);
     const float2 *tri = fc.triH;
     const float2 *src = a.in + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
     const SmemNat<LSC> sn{smem};

@@ -159,6 +159,15 @@ __device__ __forceinline__ const DevMember &member_of(const MemberSet &ms, int s
     return ms.table ? ms.table[ms.first + slot] : ms.solo;
 }
 
+// True when none of the tile's results lies in the member's region of
+// interest (the member's own result extent cuts the last column/row).
+__device__ __forceinline__ bool roi_misses_tile(const TileGeom &g, int tile, const TileBox &b, const DevMember &m) {
+    const int ty = tile / g.ntx, tx = tile - ty * g.ntx;
+    const int bw = (tx == g.ntx - 1) ? m.rw - b.x0 : g.blockW;
+    const int bh = (ty == g.nty - 1) ? m.rh - b.y0 : g.blockH;
+    return b.x0 >= m.roiX1 || b.x0 + bw <= m.roiX0 || b.y0 >= m.roiY1 || b.y0 + bh <= m.roiY0;
+}
+
 // ------------------------------------------------ first-occurrence extrema
 
 
@@ -224,6 +233,12 @@ __device__ void ext_block_reduce(Ext &e, Ext *sh) {
 
 __device__ void ext_store_result(const Ext &e, int rw, cvm_result *out) {
     cvm_result r;
+    if (e.minI == LLONG_MAX) {  // no result position (an empty region of interest)
+        r.min_v = r.max_v = __int_as_float(0x7fc00000);
+        r.min_x = r.min_y = r.max_x = r.max_y = -1;
+        *out = r;
+        return;
+    }
     r.min_v = e.minV;
     r.max_v = e.maxV;
     r.min_x = (int32_t)(e.minI % rw);

@@ -88,7 +88,10 @@ struct DevMember {
     int tw, th, rw, rh;
     int partBase;              // first partial record of this member (norm CTAs)
     int outIdx;                // result slot
-    int pad;
+    // region of interest: the result positions [roiX0, roiX1) x [roiY0,
+    // roiY1) that take part in the extrema (all of them by default);
+    // tiles and row pairs outside it are skipped
+    int roiX0, roiY0, roiX1, roiY1;
 };
 
 // Where the tail kernels find their targets: a device member table
@@ -105,6 +108,7 @@ struct MemberSet {
     size_t corrStride;         // elements between wave slots
     float2 *lanes;             // per result (t, den) of the statistics kernel, per wave slot
     size_t lanesStride;        // elements between wave slots
+    int anyRoi;                // some member of the launch has a region of interest
 };
 
 struct Partial {

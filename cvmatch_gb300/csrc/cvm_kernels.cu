@@ -534,6 +534,7 @@ __global__ void k_cols(ColsArgs a) {
     const int wv = min(SC, fc.hw - c0);
     const size_t chanStride = (size_t)H * hwp;
     const TileBox b = tile_box(a.g, tile);
+    if (m && a.ms.anyRoi && roi_misses_tile(a.g, tile, b, *m)) return;  // outside the member's ROI
     const int tid = threadIdx.x, nt = blockDim.x;
 
     const float2 *src = a.in + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
@@ -758,6 +759,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_even(ColsArgs a) {
     const int wv = min(SC, fc.hw - c0);
     const size_t chanStride = (size_t)H * hwp;
     const TileBox b = tile_box(a.g, tile);
+    if (m && a.ms.anyRoi && roi_misses_tile(a.g, tile, b, *m)) return;  // outside the member's ROI
     const float2 *tri = fc.triH;
     const float2 zero = make_float2(0.f, 0.f);
     // even-log2 passes: r16 at h = 16^p for p < L/4, then r4 at h = 16^(L/4)
@@ -925,7 +927,13 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows(InvArgs a) {
     const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
     const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
     const int pair0 = blockIdx.x * a.pairsPerCta;
-    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    // the CTA's row pairs; none when its results all lie outside the
+    // member's region of interest (no transform, no extrema)
+    int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    if (P > 0 && a.ms.anyRoi) {
+        const int ya = tb.y0 + 2 * pair0, yb = tb.y0 + min(2 * (pair0 + P), bh);
+        if (ya >= m.roiY1 || yb <= m.roiY0 || tb.x0 >= m.roiX1 || tb.x0 + bw <= m.roiX0) P = 0;
+    }
     const int n = fc.n, log2n = fc.log2n, hw = fc.hw, hwp = fc.hwp, ld = padded_len(n);
     const int tid = threadIdx.x, nt = blockDim.x;
     const bool flat = Pm.flat != 0;
@@ -1010,7 +1018,8 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows(InvArgs a) {
                     score = 0.f;
             }
             if (map) map[li] = score;
-            ext_add(e, score, li);
+            if (tb.y0 + r >= m.roiY0 && tb.y0 + r < m.roiY1 && tb.x0 + x >= m.roiX0 && tb.x0 + x < m.roiX1)
+                ext_add(e, score, li);
           }
         }
     }
@@ -1541,6 +1550,8 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     const int x = (PRE ? blockIdx.y : blockIdx.x) * blockDim.x + threadIdx.x;
     const int Y0 = (PRE ? blockIdx.z : blockIdx.y) * a.BV;
     if (x >= m.rw || Y0 >= m.rh) return;
+    // results outside the member's region of interest are never read
+    if (a.ms.anyRoi && (x < m.roiX0 || x >= m.roiX1 || Y0 >= m.roiY1 || Y0 + a.BV <= m.roiY0)) return;
     const int Bv = min(a.BV, m.rh - Y0);
     const int th = m.th;
     const size_t rp = (size_t)a.hp * NP;  // row pitch

@@ -210,6 +210,8 @@ extern "C" int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride
     ms.solo.th = th;
     ms.solo.rw = rw;
     ms.solo.rh = rh;
+    ms.solo.roiX1 = rw;
+    ms.solo.roiY1 = rh;
     ms.params = P;
     ms.map = d_map;
     ms.corr = corr;

@@ -243,7 +243,13 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
     const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
     const int pair0 = blockIdx.x * a.pairsPerCta;
-    const int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    // the CTA's row pairs; none when its results all lie outside the
+    // member's region of interest (no transform, no extrema)
+    int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    if (P > 0 && a.ms.anyRoi) {
+        const int ya = tb.y0 + 2 * pair0, yb = tb.y0 + min(2 * (pair0 + P), bh);
+        if (ya >= m.roiY1 || yb <= m.roiY0 || tb.x0 >= m.roiX1 || tb.x0 + bw <= m.roiX0) P = 0;
+    }
     const int hwp = fc.hwp, log2H = fc.log2H;
     const int tid = threadIdx.x;
     const bool flat = Pm.flat != 0;
@@ -313,10 +319,12 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     if (P > 0) {
         const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
         float *map = a.ms.map;
+        const int xlo = m.roiX0 - tb.x0, xhi = m.roiX1 - tb.x0;
         for (int rr = 0; rr < 2 * P; rr++) {
             const int r = 2 * pair0 + rr;
             if (r >= bh) break;
             const long long rowBase = (long long)(tb.y0 + r) * m.rw + tb.x0;
+            if (tb.y0 + r < m.roiY0 || tb.y0 + r >= m.roiY1) continue;  // no map here (only fleets have ROIs)
             float2 td[XIT];
 #pragma unroll
             for (int q = 0; q < XIT; q++) {
@@ -339,7 +347,7 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                             score = 0.f;
                     }
                     if (map) map[rowBase + x] = score;
-                    ext_add(e, score, rowBase + x);
+                    if (x >= xlo && x < xhi) ext_add(e, score, rowBase + x);
                 }
             }
         }

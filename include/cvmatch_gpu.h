@@ -185,6 +185,17 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 
 void cvm_fleet_free(cvm_fleet *f);
 
+/* Region of interest of one member (construction order), x, y, w, h in
+ * frame pixels; w or h <= 0 clears it.  The member's result is the
+ * first-occurrence extrema of its FindAll score map over the positions
+ * whose window lies inside the ROI, in frame coordinates; tiles and rows
+ * outside it are skipped.  An ROI that cannot hold the template gives
+ * min_v = max_v = NaN and positions -1.  (The reference keeps per-ROI
+ * crop fleets instead, examples/windowrules/engine.go:276-343; per-member
+ * ROIs on the shared frame spectra are its parked item, CLAUDE.md:463-475.)
+ * Not to be called while a FindAll on the same fleet runs. */
+int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h);
+
 /* ------------------------------------------------------- frame streams */
 
 /* A stream of RGBA frames of one size matched against a colour fleet and,

@@ -74,6 +74,8 @@ def lib():
             L.cvo_bucketize.argtypes = [C.POINTER(Member), i32, i32, vp, vp, vp, vp]
             L.cvo_fleet_find_all.argtypes = [C.POINTER(Member), i32, i32, vp, i64, i32, i32, i32,
                                              C.POINTER(Result), C.c_char_p]
+            L.cvo_fleet_find_all_maps.argtypes = [C.POINTER(Member), i32, i32, vp, i64, i32, i32, i32,
+                                                  C.POINTER(Result), vp, C.c_char_p]
             L.cvo_ref_match_f64.argtypes = [vp, i64, i32, i32, vp, i64, i32, i32, i32, i32, i32, vp]
             _lib = L
     return _lib
@@ -216,17 +218,33 @@ def bucketize(tpls):
     return [(int(tw[b]), int(th[b]), [int(m) for m in mem[offs[b]:offs[b + 1]]]) for b in range(nb)]
 
 
-def fleet_find_all(tpls, parent: np.ndarray, threads: int = 1):
+def fleet_find_all(tpls, parent: np.ndarray, threads: int = 1, want_maps: bool = False):
+    """Fleet.FindAll; with want_maps also every member's score map on its
+    bucket's plan (None for flat members): (results, maps)."""
     ms, step = _members(tpls)
     a, pstride, pw, ph, pstep = _view(parent)
     if len(tpls) and pstep != step:
         raise ValueError("parent step differs from the members'")
     out = (Result * max(len(tpls), 1))()
     err = C.create_string_buffer(256)
-    rc = lib().cvo_fleet_find_all(ms, len(tpls), step or pstep, _ptr(a), pstride, pw, ph, threads, out, err)
+    maps = None
+    mp = None
+    if want_maps:
+        maps = []
+        for t in tpls:
+            th, tw = np.asarray(t).shape[:2]
+            maps.append(np.full((ph - th + 1, pw - tw + 1), np.nan, np.float32) if tw <= pw and th <= ph else None)
+        mp = (C.c_void_p * max(len(tpls), 1))(*[m.ctypes.data if m is not None else None for m in maps])
+    rc = lib().cvo_fleet_find_all_maps(ms, len(tpls), step or pstep, _ptr(a), pstride, pw, ph, threads, out, mp, err)
     if rc != 0:
         raise OraclePanic(err.value.decode())
-    return [out[i].tuple() for i in range(len(tpls))]
+    res = [out[i].tuple() for i in range(len(tpls))]
+    if not want_maps:
+        return res
+    for i, r in enumerate(res):
+        if maps[i] is not None and np.isnan(maps[i]).all():
+            maps[i] = None  # flat member: no map (impl.go:1137-1144)
+    return res, maps
 
 
 def ref_match_f64(img: np.ndarray, tpl: np.ndarray, cn: int, threads: int = 8) -> np.ndarray:

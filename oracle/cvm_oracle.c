@@ -937,6 +937,7 @@ typedef struct {
     const size_t *off;
     int ntx, nty, lastY0;
     cvo_result *out;
+    float *const *maps;  /* per member (construction order) score map out, or NULL */
     atomic_int next;
     /* phase 1 */
     int btw, bth, rwF, rhF, cnMax, has2;
@@ -998,15 +999,18 @@ static void fl_phase2(void *vctx, int w) {
         }
         normalize_parallel(c->pp, c->pstride, c->pw, m->w, m->h, cn, c->step, rw, rh, c->inner, m->tsum,
                            m->varSum, res, res, &c->out[mi]);
+        if (c->maps && c->maps[mi]) memcpy(c->maps[mi], res, sizeof(float) * (size_t)rw * rh);
         free(res);
     }
     free(spec);
     free(z);
 }
 
-/* Fleet.FindAll + buildGeom, fleet.go:176-390. */
-int cvo_fleet_find_all(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
-                       int pw, int ph, int threads, cvo_result *out, char *err) {
+/* Fleet.FindAll + buildGeom, fleet.go:176-390; maps (optional, per member
+ * in construction order, (pw-w+1) x (ph-h+1) floats each) receive every
+ * non-flat member's score map on its bucket's plan. */
+int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                            int pw, int ph, int threads, cvo_result *out, float *const *maps, char *err) {
     if (n <= 0) {
         if (err) snprintf(err, 160, "cvmatch: empty fleet");
         return -3;
@@ -1075,7 +1079,7 @@ int cvo_fleet_find_all(const cvo_member *cms, int n, int step, const uint8_t *pp
         c.pw = pw; c.ph = ph; c.step = step; c.p = &p; c.sets = sets; c.frame = frame; c.off = off;
         c.ntx = ntx; c.nty = nty; c.lastY0 = lastY0; c.out = out;
         c.btw = btw[b]; c.bth = bth[b]; c.rwF = rwF; c.rhF = rhF; c.cnMax = cnMax;
-        c.has2 = dh2 > 0; c.p2 = &p2; c.frame_w = frame;
+        c.has2 = dh2 > 0; c.p2 = &p2; c.frame_w = frame; c.maps = maps;
         atomic_init(&c.next, 0);
         run_parallel(imin(threads, ntiles), fl_phase1, &c);
         int outer = imin(threads, nm);
@@ -1091,6 +1095,11 @@ int cvo_fleet_find_all(const cvo_member *cms, int n, int step, const uint8_t *pp
     free(btw); free(bth); free(offs); free(mem);
     free(ms);
     return 0;
+}
+
+int cvo_fleet_find_all(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                       int pw, int ph, int threads, cvo_result *out, char *err) {
+    return cvo_fleet_find_all_maps(cms, n, step, pp, pstride, pw, ph, threads, out, NULL, err);
 }
 
 /* --------------------------------------------------------- FP64 oracle */

@@ -96,6 +96,8 @@ int cvo_bucketize(const cvo_member *ms, int n, int step, int32_t *tw, int32_t *t
 int cvo_fleet_find_all(const cvo_member *ms, int n, int step, const uint8_t *parent,
                        int64_t pstride, int pw, int ph, int threads, cvo_result *out,
                        char *err);
+int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                            int pw, int ph, int threads, cvo_result *out, float *const *maps, char *err);
 
 /* Brute-force FP64 TM_CCOEFF_NORMED from the definition
  * (cvmatch_test.go:13-81); out has rw*rh doubles. */

@@ -617,3 +617,55 @@ def test_peaks_device_on_a_device_map():
     assert n == len(want)
     got = [tuple(int(v) for v in p) for p in xy.cpu().numpy().reshape(-1, 2)[:min(n, 64)]]
     assert got == want[:64]
+
+
+# ----------------------------------------------------- regions of interest
+
+
+def _roi_expect(res, m, roi, tw, th):
+    """First-occurrence extrema of a member's FindAll map over the positions
+    whose window lies inside roi = (x, y, w, h), in frame coordinates."""
+    x, y, w, h = roi
+    rh, rw = m.shape if m is not None else (None, None)
+    if m is None:  # flat member: 1 everywhere
+        return None
+    x0, y0 = max(x, 0), max(y, 0)
+    x1, y1 = min(x + w - tw + 1, rw), min(y + h - th + 1, rh)
+    if x1 <= x0 or y1 <= y0:
+        return "empty"
+    sub = m[y0:y1, x0:x1]
+    iy, ix = np.unravel_index(int(np.argmin(sub)), sub.shape)
+    jy, jx = np.unravel_index(int(np.argmax(sub)), sub.shape)
+    return (float(sub[iy, ix]), x0 + int(ix), y0 + int(iy), float(sub[jy, jx]), x0 + int(jx), y0 + int(jy))
+
+
+def test_fleet_roi_members_equal_restricted_maps():
+    parent = rgba(81, 240, 360)
+    tpls = [parent[30:54, 40:72].copy(), parent[150:190, 200:250].copy(), rgba(82, 30, 40),
+            parent[100:120, 300:340].copy(), np.full((16, 16, 4), 90, np.uint8)]
+    tpls[4][..., 3] = 255
+    rois = {0: (20, 10, 120, 90), 1: (0, 0, 150, 120), 2: (5, 5, 20, 20), 4: (60, 70, 50, 40)}
+    res, maps = oracle.fleet_find_all(tpls, parent, want_maps=True)
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    for i, r in rois.items():
+        fleet.SetROI(i, *r)
+    got = fleet.FindAll(parent)
+    for i, t in enumerate(tpls):
+        th, tw = t.shape[:2]
+        if i not in rois:
+            assert same_tuple(tuple(got[i]), res[i])
+            continue
+        want = _roi_expect(res[i], maps[i], rois[i], tw, th)
+        if want == "empty":
+            assert np.isnan(got[i][0]) and np.isnan(got[i][3]) and tuple(got[i])[1:3] == (-1, -1)
+        elif want is None:  # flat with an ROI: its first position
+            x, y = rois[i][0], rois[i][1]
+            assert tuple(got[i]) == (1.0, x, y, 1.0, x, y)
+        else:
+            assert same_tuple(tuple(got[i]), want), (i, tuple(got[i]), want)
+    # clearing the regions restores FindAll's results
+    for i in rois:
+        fleet.SetROI(i, 0, 0, 0, 0)
+    again = fleet.FindAll(parent)
+    for i in range(len(tpls)):
+        assert same_tuple(tuple(again[i]), res[i])
