@@ -228,6 +228,23 @@ def scene_c5(seed=5, frames=16, ncolor=64, ngray=8):
 # ------------------------------------------------------------------ helpers
 
 
+def slowest_rank_ms(ms: float, ws: int, device) -> float:
+    """The largest of the ranks' times (replicas run independently; the job
+    is as slow as its slowest rank)."""
+    if ws <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, ms: float, ws: int) -> float:
+    """Whole-job units per second: every rank processes units_per_rank in
+    the slowest rank's time."""
+    return ws * units_per_rank / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -402,12 +419,8 @@ def run_gpu(args):
             ends[i].record(stream)
         torch.cuda.synchronize()
     launches = (L.cvm_launch_count() - l0) // args.steps
-    ms = float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)]))
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * MPX / (ms / 1e3)
+    ms = slowest_rank_ms(float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)])), ws, dev)
+    value = replica_throughput(MPX, ms, ws)
 
     # e2e through the host-buffer entry point, pinned host frame
     hp = L.cvm_host_alloc(frame.nbytes)
@@ -425,11 +438,7 @@ def run_gpu(args):
         e2e_t.append(time.perf_counter() - t0)
         assert rc == 0
     L.cvm_host_free(hp)
-    e2e_ms = 1e3 * float(np.mean(e2e_t))
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = slowest_rank_ms(1e3 * float(np.mean(e2e_t)), ws, dev)
 
     line = None
     if rank == 0:
@@ -446,7 +455,7 @@ def run_gpu(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single"),
-                "e2e": {"value": ws * MPX / (e2e_ms / 1e3), "unit": "template*Mpx/s",
+                "e2e": {"value": replica_throughput(MPX, e2e_ms, ws), "unit": "template*Mpx/s",
                         "h2d_bytes_per_step": int(frame.nbytes + tpl.nbytes), "d2h_bytes_per_step": 24},
                 "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
                 "result": list(got)}
