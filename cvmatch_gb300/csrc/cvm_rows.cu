@@ -203,19 +203,35 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
     const int hwp = fc.hwp, log2H = fc.log2H;
     const size_t chanStride = (size_t)fc.dftH * hwp;
     float2 *tbase = a.spec + (size_t)(tile - fc.tileFirst) * a.cnS * chanStride;
-    auto emit = [&](int line, int kk) {
+    auto rows = [&](int line, float2 *&ra, float2 *&rb) {
         const int p = div_cn(line, cn), k = a.chanFirst + line - p * cn;
         const int r = 2 * (pair0 + p);
-        const float2 *zl = smem + line * LD;
-        const float2 zk = zl[padi(kk)], zn = zl[padi((N - kk) & (N - 1))];
         float2 *cb = tbase + (size_t)k * chanStride;
-        cb[(size_t)brev_bits(r, log2H) * hwp + kk] =
-            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zn.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zn.y)));
-        cb[(size_t)brev_bits(r + 1, log2H) * hwp + kk] =
-            make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zn.y)), __fmul_rn(0.5f, __fsub_rn(zn.x, zk.x)));
+        ra = cb + (size_t)brev_bits(r, log2H) * hwp;
+        rb = cb + (size_t)brev_bits(r + 1, log2H) * hwp;
     };
-    for (int it = tid; it < (lines << (LOG2N - 1)); it += nt) emit(it >> (LOG2N - 1), it & (HALF - 1));
-    for (int line = tid; line < lines; line += nt) emit(line, HALF);
+    // two spectrum columns kk, kk+1 per item: one 16-byte store per row
+    for (int it = tid; it < (lines << (LOG2N - 2)); it += nt) {
+        const int line = it >> (LOG2N - 2), kk = 2 * (it & (HALF / 2 - 1));
+        float2 *ra, *rb;
+        rows(line, ra, rb);
+        const float2 *zl = smem + line * LD;
+        const float2 z0 = zl[padi(kk)], n0 = zl[padi((N - kk) & (N - 1))];
+        const float2 z1 = zl[padi(kk + 1)], n1 = zl[padi(N - kk - 1)];
+        *reinterpret_cast<float4 *>(ra + kk) =
+            make_float4(__fmul_rn(0.5f, __fadd_rn(z0.x, n0.x)), __fmul_rn(0.5f, __fsub_rn(z0.y, n0.y)),
+                        __fmul_rn(0.5f, __fadd_rn(z1.x, n1.x)), __fmul_rn(0.5f, __fsub_rn(z1.y, n1.y)));
+        *reinterpret_cast<float4 *>(rb + kk) =
+            make_float4(__fmul_rn(0.5f, __fadd_rn(z0.y, n0.y)), __fmul_rn(0.5f, __fsub_rn(n0.x, z0.x)),
+                        __fmul_rn(0.5f, __fadd_rn(z1.y, n1.y)), __fmul_rn(0.5f, __fsub_rn(n1.x, z1.x)));
+    }
+    for (int line = tid; line < lines; line += nt) {  // kk = N/2
+        float2 *ra, *rb;
+        rows(line, ra, rb);
+        const float2 zk = smem[line * LD + padi(HALF)];
+        ra[HALF] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zk.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zk.y)));
+        rb[HALF] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zk.y)), __fmul_rn(0.5f, __fsub_rn(zk.x, zk.x)));
+    }
 }
 
 // ------------------------------------------------------------ inverse rows
@@ -262,17 +278,21 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
         const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
         for (int k = 0; k < cn; k++) {
             const float2 *cb = scr + ((size_t)tileLocal * a.cnS + k) * chanStride;
-            const int total = P << (LOG2N - 1);
+            // two spectrum columns kk, kk+1 per item (16-byte loads)
+            const int total = P << (LOG2N - 2);
 #pragma unroll 4
             for (int it = tid; it < total; it += kThreads) {
-                const int p = it >> (LOG2N - 1), kk = it & (HALF - 1);
+                const int p = it >> (LOG2N - 2), kk = 2 * (it & (HALF / 2 - 1));
                 const int r = 2 * (pair0 + p);
-                const float2 u = __ldg(cb + (size_t)brev_bits(r, log2H) * hwp + kk);
-                const float2 v = __ldg(cb + (size_t)brev_bits(r + 1, log2H) * hwp + kk);
+                const float4 u = __ldg(reinterpret_cast<const float4 *>(cb + (size_t)brev_bits(r, log2H) * hwp + kk));
+                const float4 v =
+                    __ldg(reinterpret_cast<const float4 *>(cb + (size_t)brev_bits(r + 1, log2H) * hwp + kk));
                 float2 *zl = smem + p * LD;
                 zl[padi(brevn<LOG2N>(kk))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
+                zl[padi(brevn<LOG2N>(kk + 1))] = make_float2(__fsub_rn(u.z, v.w), __fadd_rn(u.w, v.z));
                 if (kk > 0)
                     zl[padi(brevn<LOG2N>(N - kk))] = make_float2(__fadd_rn(u.x, v.y), __fsub_rn(v.x, u.y));
+                zl[padi(brevn<LOG2N>(N - kk - 1))] = make_float2(__fadd_rn(u.z, v.w), __fsub_rn(v.z, u.w));
             }
             if (tid < P) {
                 const int r = 2 * (pair0 + tid);
