@@ -209,12 +209,15 @@ def test_parent_alpha_scan_one_pixel(W, pw):
         assert np.array_equal(bits(d_map.cpu().numpy()), bits(want)), where
 
 
-@pytest.mark.parametrize("pw,ph,pad,gray", [(1024, 600, 0, False), (1001, 530, 3, False), (1501, 700, 0, True),
-                                            (1500, 700, 4, True)])
-def test_pinned_host_frame_ingest(pw, ph, pad, gray):
+@pytest.mark.parametrize("pw,ph,pad,gray,alpha_at", [(1024, 600, 0, False, None), (1001, 530, 3, False, None),
+                                                     (1501, 700, 0, True, None), (1500, 700, 4, True, None),
+                                                     (1024, 600, 0, False, (599, 1023)), (1001, 530, 3, False, (0, 1)),
+                                                     (1002, 530, 0, False, (300, 500))])
+def test_pinned_host_frame_ingest(pw, ph, pad, gray, alpha_at):
     """Frames in page-locked host memory (cvm_host_alloc) are read by a
-    kernel over the host link; 16-byte, 4-byte and 1-byte row alignments
-    must all give the oracle's map bit for bit."""
+    kernel over the host link; 16-byte, 4-byte and 1-byte row alignments,
+    and one differing alpha byte (the 4-channel path), must all give the
+    oracle's map bit for bit."""
     import ctypes as C
     L = cvm.lib()
     bpp = 1 if gray else 4
@@ -227,6 +230,8 @@ def test_pinned_host_frame_ingest(pw, ph, pad, gray):
         src = image(31 + pw, ph, pw, bpp)
         if not gray:
             src[..., 3] = 255
+            if alpha_at is not None:
+                src[alpha_at[0], alpha_at[1], 3] = 254
         buf[:, :pw * bpp] = src.reshape(ph, pw * bpp)
         view = buf[:, :pw * bpp].reshape((ph, pw) if gray else (ph, pw, bpp))
         tpl = np.ascontiguousarray(view[100:140, 200:260])
@@ -239,7 +244,7 @@ def test_pinned_host_frame_ingest(pw, ph, pad, gray):
         else:
             rc = L.cvm_match_map(hp, stride, pw, ph, tpl.ctypes.data, tpl.strides[0], 60, 40, got.ctypes.data)
         assert rc == 0
-        _, want = oracle.match_u8(view, tpl, 1 if gray else 3)
+        _, want = oracle.match_u8(view, tpl, 1 if gray else (3 if alpha_at is None else 4))
         assert np.array_equal(bits(got), bits(want))
     finally:
         L.cvm_host_free(hp)
