@@ -536,8 +536,9 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     PoolBuf bi, bt, gi, gt, bm, bo;
     long long ip, tp;
     const int bpp = grayFromRgba ? 4 : step;
-    CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st, 1));
+    // the frame's transfer first: it is the long one
     CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, st, 0));
+    CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st, 1));
     const uint8_t *dImg = static_cast<const uint8_t *>(bi.p), *dTpl = static_cast<const uint8_t *>(bt.p);
     if (grayFromRgba) {
         long long gp = (long long)align_up((size_t)iw, 128), gtp = (long long)align_up((size_t)tw, 128);
