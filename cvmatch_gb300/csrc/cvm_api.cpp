@@ -119,10 +119,12 @@ cudaStream_t thread_stream() {
 
 // Two per-thread side streams: st carries the template spectrum, st2 the
 // window statistics; fork is recorded on the caller's stream once the
-// channel count exists, join/joinStats when each chain is done.
+// channel count exists, join/joinStats when each chain is done.  A
+// host-buffer call also moves its frame in on st2 (frame marks the end),
+// while the caller's stream takes the template and the small setup.
 struct SideStream {
     cudaStream_t st = nullptr, st2 = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr, frame = nullptr;
 };
 
 SideStream &side_stream() {
@@ -139,6 +141,7 @@ SideStream &side_stream() {
         cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.frame, cudaEventDisableTiming);
     }
     return s;
 }
@@ -176,6 +179,11 @@ struct Arena {
 struct PoolBuf {
     void *p = nullptr;
     cudaStream_t st = nullptr;
+    // stream-ordered free behind the work already queued on s
+    void release(cudaStream_t s) {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+    }
     ~PoolBuf() {
         if (p) cudaFreeAsync(p, st);
     }
@@ -297,6 +305,7 @@ struct SoloJob {
     const DevParams *cachedP;     // cached template statistics
     float *map;
     cvm_result *out;
+    int frameOnSide;  // the frame arrives on the second side stream (its frame event)
 };
 
 int run_solo(const SoloJob &J, cudaStream_t st) {
@@ -374,6 +383,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     // not get SMs back from one that did (priority orders only the CTAs
     // waiting for a slot), so the gating statistics launch goes first.
     SideStream &ss = side_stream();
+    if (J.frameOnSide) CVM_CUDA(cudaStreamWaitEvent(st, ss.frame, 0));
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
                          J.cnFixed, F, st));
@@ -528,19 +538,55 @@ struct PeakReq {
     int32_t *count;
 };
 
+// A per-thread page-locked result slot the device writes through its
+// mapped address: the one-shot calls read their extrema from it after the
+// stream synchronises, with no device-to-host copy behind the last launch.
+cvm_result *host_result_slot(cvm_result **dev) {
+    struct Slot {
+        cvm_result *h = nullptr, *d = nullptr;
+        ~Slot() {
+            if (h) cudaFreeHost(h);
+        }
+    };
+    thread_local Slot s;
+    if (!s.h) {
+        void *h = nullptr, *d = nullptr;
+        if (cudaHostAlloc(&h, sizeof(cvm_result), cudaHostAllocMapped) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess || !d) {
+            cudaGetLastError();
+            cudaFreeHost(h);
+            return nullptr;
+        }
+        s.h = static_cast<cvm_result *>(h);
+        s.d = static_cast<cvm_result *>(d);
+    }
+    *dev = s.d;
+    return s.h;
+}
+
 int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8_t *tpl, long long tstride,
               int tw, int th, int mode, int cnFixed, int step, int grayFromRgba, float *map,
               cvm_result *out, const PeakReq *pk = nullptr) {
     CVM_TRY(ensure_device());
     cudaStream_t st = thread_stream();
+    SideStream &ss = side_stream();
     PoolBuf bi, bt, gi, gt, bm, bo;
     long long ip, tp;
     const int bpp = grayFromRgba ? 4 : step;
-    // the frame's transfer first: it is the long one
-    CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, st, 0));
+    // The frame moves in on the second side stream (the long transfer,
+    // started first); the template and the setup of the launches proceed on
+    // the caller's stream meanwhile, which waits for the frame only where it
+    // first reads it.  The side stream's statistics chain is ordered after
+    // that wait by the fork event.
+    CVM_TRY(upload_image(bi, img, istride, iw, ih, bpp, &ip, ss.st2, 0));
+    CVM_CUDA(cudaEventRecord(ss.frame, ss.st2));
     CVM_TRY(upload_image(bt, tpl, tstride, tw, th, bpp, &tp, st, 1));
     const uint8_t *dImg = static_cast<const uint8_t *>(bi.p), *dTpl = static_cast<const uint8_t *>(bt.p);
     if (grayFromRgba) {
+        CVM_CUDA(cudaStreamWaitEvent(st, ss.frame, 0));
         long long gp = (long long)align_up((size_t)iw, 128), gtp = (long long)align_up((size_t)tw, 128);
         CVM_TRY(pool_alloc(gi, (size_t)gp * ih, st));
         CVM_TRY(pool_alloc(gt, (size_t)gtp * th, st));
@@ -557,7 +603,11 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
         CVM_TRY(pool_alloc(bm, (size_t)rw * rh * sizeof(float), st));
         dMap = static_cast<float *>(bm.p);
     }
-    CVM_TRY(pool_alloc(bo, sizeof(cvm_result), st));
+    cvm_result *dOut = nullptr, *hOut = host_result_slot(&dOut);
+    if (!hOut) {
+        CVM_TRY(pool_alloc(bo, sizeof(cvm_result), st));
+        dOut = static_cast<cvm_result *>(bo.p);
+    }
     SoloJob J;
     memset(&J, 0, sizeof J);
     J.img = dImg;
@@ -572,7 +622,8 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     J.tw = tw;
     J.th = th;
     J.map = dMap;
-    J.out = static_cast<cvm_result *>(bo.p);
+    J.out = dOut;
+    J.frameOnSide = !grayFromRgba;
     CVM_TRY(run_solo(J, st));
     if (map) CVM_CUDA(cudaMemcpyAsync(map, dMap, (size_t)rw * rh * sizeof(float), cudaMemcpyDeviceToHost, st));
     PoolBuf bp;
@@ -586,8 +637,18 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
         CVM_CUDA(cudaMemcpyAsync(pk->count, dCount, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         if (xyBytes) CVM_CUDA(cudaMemcpyAsync(pk->xy, dXY, xyBytes, cudaMemcpyDeviceToHost, st));
     }
-    CVM_CUDA(cudaMemcpyAsync(out, bo.p, sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
+    if (!hOut) CVM_CUDA(cudaMemcpyAsync(out, bo.p, sizeof(cvm_result), cudaMemcpyDeviceToHost, st));
+    // the device buffers go back to the pool in stream order now, so the
+    // host's frees overlap the device work instead of following the wait
+    bi.release(st);
+    bt.release(st);
+    gi.release(st);
+    gt.release(st);
+    bm.release(st);
+    bp.release(st);
+    bo.release(st);
     CVM_CUDA(cudaStreamSynchronize(st));
+    if (hOut) *out = *hOut;
     return CVM_OK;
 }
 
