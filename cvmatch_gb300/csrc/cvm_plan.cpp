@@ -43,12 +43,16 @@ Plan make_plan(int tw, int th, int rw, int rh) {
             const int64_t rowFFT = 5 * int64_t(W) * ilog2(W);
             const int64_t colPass = 5 * int64_t(H) * ilog2(H) * hw;
             const int64_t specN = int64_t(H) * hw;
-            int64_t cost = 0;
-            for (int y0 = 0; y0 < rh; y0 += bH) {
-                const int bh = std::min(bH, rh - y0);
+            // Every band but a ragged last one has height bH, so the
+            // per-band sum of the reference's loop collapses to a product
+            // (the same integer total, O(1) instead of rh / bH steps).
+            auto band = [&](int bh) {
                 const int loadH = std::min(bh + th - 1, H);
-                cost += ntx * (int64_t((loadH + 1) / 2 + (bh + 1) / 2) * rowFFT + 2 * colPass + 16 * specN);
-            }
+                return ntx * (int64_t((loadH + 1) / 2 + (bh + 1) / 2) * rowFFT + 2 * colPass + 16 * specN);
+            };
+            const int64_t full = rh / bH, rest = rh - full * bH;
+            int64_t cost = full * band(bH);
+            if (rest > 0) cost += band((int)rest);
             if (bestCost < 0 || cost < bestCost || (cost == bestCost && area < bestArea)) {
                 bestCost = cost;
                 bestArea = area;

@@ -111,3 +111,20 @@ def test_product_planner_matches_oracle_shrink():
         assert L.cvm_plan(tw, th, rw, rh, out) == 0
         p = oracle.plan(tw, th, rw, rh)
         assert out[4] == oracle.shrink_dh(p, rh, th)
+
+
+def test_product_planner_matches_oracle_random_shapes():
+    """The library's planner (band sums in closed form) picks the oracle's
+    plan (the band-by-band loop of newGoPlan, impl.go:246-295) on random
+    shapes, including tall results with many short bands."""
+    import numpy as np
+    import oracle
+    L = cvm.lib()
+    rng = np.random.default_rng(7)
+    for _ in range(400):
+        tw, th = (int(v) for v in rng.integers(1, 300, 2))
+        rw, rh = (int(v) for v in rng.integers(1, 4000, 2))
+        out = (C.c_int32 * 6)()
+        assert L.cvm_plan(tw, th, rw, rh, out) == 0
+        p = oracle.plan(tw, th, rw, rh)
+        assert (out[0], out[1], out[2], out[3]) == (p.dft_w, p.dft_h, p.block_w, p.block_h), (tw, th, rw, rh)

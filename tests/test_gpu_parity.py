@@ -212,7 +212,8 @@ def test_parent_alpha_scan_one_pixel(W, pw):
 @pytest.mark.parametrize("pw,ph,pad,gray,alpha_at", [(1024, 600, 0, False, None), (1001, 530, 3, False, None),
                                                      (1501, 700, 0, True, None), (1500, 700, 4, True, None),
                                                      (1024, 600, 0, False, (599, 1023)), (1001, 530, 3, False, (0, 1)),
-                                                     (1002, 530, 0, False, (300, 500))])
+                                                     (1002, 530, 0, False, (300, 500)), (1600, 700, 0, True, None),
+                                                     (1600, 700, 16, True, None)])
 def test_pinned_host_frame_ingest(pw, ph, pad, gray, alpha_at):
     """Frames in page-locked host memory (cvm_host_alloc) are read by a
     kernel over the host link; 16-byte, 4-byte and 1-byte row alignments,
@@ -246,6 +247,51 @@ def test_pinned_host_frame_ingest(pw, ph, pad, gray, alpha_at):
         assert rc == 0
         _, want = oracle.match_u8(view, tpl, 1 if gray else (3 if alpha_at is None else 4))
         assert np.array_equal(bits(got), bits(want))
+    finally:
+        L.cvm_host_free(hp)
+
+
+def test_pinned_fused_ingest_template_cases():
+    """A page-locked frame with 16-byte rows takes the fused ingest (the
+    template's parameters derived on the host, the frame's alpha scan done
+    by the copy, the parameters the scan selects stored by its last CTA).
+    Consecutive calls alternate the outcomes: a template whose alpha varies
+    over a constant frame (cn 4), a constant template alpha other than the
+    frame's (cn 3), the frame's alpha varying (cn 4), flat templates (the
+    flat result), each equal to the oracle bit for bit."""
+    import ctypes as C
+    L = cvm.lib()
+    pw, ph = 1024, 600
+    nbytes = pw * 4 * ph
+    hp = L.cvm_host_alloc(nbytes)
+    assert hp
+    try:
+        buf = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(hp)).reshape(ph, pw, 4)
+        base = np.ascontiguousarray(image(77 + pw, ph, pw, 4)).copy()
+        base[..., 3] = 255
+        t_var = np.ascontiguousarray(base[100:140, 200:260]).copy()
+        t_var[5, 7, 3] = 3
+        t_const = np.ascontiguousarray(base[300:340, 500:560]).copy()
+        t_const[..., 3] = 7
+        t_flat = np.zeros((40, 60, 4), np.uint8)
+        t_flat[..., :3] = 90
+        t_flat[..., 3] = 255
+        t_zero = np.zeros((40, 60, 4), np.uint8)
+        cases = [(t_var, None, 4), (t_const, None, 3), (t_const, (599, 1023), 4), (t_flat, None, 3),
+                 (t_var, None, 4), (t_zero, (10, 10), 4), (t_const, None, 3)]
+        for tpl, alpha_at, cn in cases:
+            buf[:] = base
+            if alpha_at is not None:
+                buf[alpha_at[0], alpha_at[1], 3] = 254
+            got = np.empty((ph - 40 + 1, pw - 60 + 1), np.float32)
+            rc = L.cvm_match_map(hp, pw * 4, pw, ph, tpl.ctypes.data, tpl.strides[0], 60, 40, got.ctypes.data)
+            assert rc == 0
+            r = cvm._CResult()
+            rc = L.cvm_match(hp, pw * 4, pw, ph, tpl.ctypes.data, tpl.strides[0], 60, 40, C.byref(r))
+            assert rc == 0
+            want_t, want = oracle.match_u8(buf, tpl, cn)
+            assert np.array_equal(bits(got), bits(want)), (cn, alpha_at)
+            assert same_tuple(r.tuple(), want_t), (cn, alpha_at, r.tuple(), want_t)
     finally:
         L.cvm_host_free(hp)
 
