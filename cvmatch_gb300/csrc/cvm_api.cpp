@@ -322,7 +322,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     for (int c = 0; c < G->nclass; c++) {
         int P = 0;
         partOff[c] = nparts;
-        nparts += G->fc[c].ntiles * inv_rows_ctas_per_tile(G->fc[c], &P);
+        nparts += G->fc[c].ntiles * inv_rows_ctas_per_tile(G->fc[c], G->g.blockH, &P);
     }
     const size_t hElems = (size_t)stat_pitch(cnS) * J.ih * sg.hp;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
@@ -407,7 +407,8 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     }
     CVM_CUDA(cudaStreamWaitEvent(st, ss.joinStats, 0));
     for (int c = 0; c < G->nclass; c++)
-        CVM_CUDA(launch_inv_rows(G->g, G->fc[c], c, cnS, ms, 1, partOff[c], nparts, parts, &F->normDone, J.out, st));
+        CVM_CUDA(launch_inv_rows(G->g, G->fc[c], c, cnS, ms, 1, G->g.blockH, partOff[c], nparts, parts, &F->normDone,
+                                 J.out, st));
     return CVM_OK;
 }
 
@@ -851,7 +852,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         for (int c = 0; c < G.nclass; c++) {
             int P = 0;
             bg->partOff[c] = nparts;
-            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], &P);
+            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P);
         }
         bg->nparts = nparts;
         std::vector<DevMember> tab(b.members.size());
@@ -1027,8 +1028,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
             for (int c = 0; c < G.nclass; c++)
-                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, bg.partOff[c], bg.nparts, parts, counters, dOut,
-                                         st));
+                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, G.fc[c].dftH, bg.partOff[c], bg.nparts, parts,
+                                         counters, dOut, st));
         }
     }
     return CVM_OK;

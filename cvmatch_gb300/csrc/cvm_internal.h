@@ -148,11 +148,13 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
 // member's result written by its last CTA.  Partial records of a member:
 // nparts = sum over its plan classes of ntiles * inv_rows_ctas_per_tile;
 // partOffset = the records of the classes launched before this one;
-// counters[pIdx] must be zero before the first class's launch.
+// counters[pIdx] must be zero before the first class's launch.  rowsMax
+// bounds the result rows of any tile (a single match: the block height;
+// a fleet: dftH), the same value for the launch and the partial count.
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
-                            int nmembers, int partOffset, int nparts, Partial *partials, int *counters,
+                            int nmembers, int rowsMax, int partOffset, int nparts, Partial *partials, int *counters,
                             cvm_result *out, cudaStream_t st);
-int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta);
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta);
 // Normalisation + first-occurrence extrema: CW x B results per CTA, ncx x
 // nby CTAs per member, result rows in groups of G; the member's last CTA
 // writes its result to out[outIdx].  counters (one int per member of the

@@ -1875,20 +1875,23 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     return cudaGetLastError();
 }
 
-int inv_rows_ctas_per_tile(const FftClass &fc, int *pairsPerCta) {
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta) {
     // 4096 elements per CTA: the radix-16 passes (n/16 units per line) keep
     // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM)
     int P = 4096 / fc.n;
     if (P < 1) P = 1;
-    // A tile emits at most dftH rows (a fleet member's last band extends to
-    // its own result edge, still inside the loaded rows <= dftH).
-    const int pairs = (fc.dftH + 1) / 2;
+    // A tile emits at most rowsMax rows, and never more than dftH (a fleet
+    // member's last band extends to its own result edge, still inside the
+    // loaded rows <= dftH).  No CTA without rows: an idle CTA still takes an
+    // SM slot, and a third CTA on an SM makes that SM the kernel's tail.
+    const int rows = rowsMax < fc.dftH ? rowsMax : fc.dftH;
+    const int pairs = (rows + 1) / 2;
     *pairsPerCta = P;
     return (pairs + P - 1) / P;
 }
 
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
-                            int nmembers, int partOffset, int nparts, Partial *partials, int *counters,
+                            int nmembers, int rowsMax, int partOffset, int nparts, Partial *partials, int *counters,
                             cvm_result *out, cudaStream_t st) {
     InvArgs a;
     a.g = g;
@@ -1897,7 +1900,7 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.cnS = cnS;
     a.ms = ms;
     int P = 0;
-    const int ctas = inv_rows_ctas_per_tile(fc, &P);
+    const int ctas = inv_rows_ctas_per_tile(fc, rowsMax, &P);
     a.pairsPerCta = P;
     a.partOffset = partOffset;
     a.nparts = nparts;

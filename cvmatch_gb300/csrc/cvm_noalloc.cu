@@ -219,7 +219,7 @@ extern "C" int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride
         NA_CUDA(launch_fwd_rows(d_img, istride, step, cn, nullptr, g, fc[c], spec[c], cn, st));
         ms.scratch[c] = spec[c];
         NA_CUDA(launch_cols(1, spec[c], spec[c], cn, g, fc[c], c, cn, nullptr, 1.0f, ms, 1, st));
-        NA_CUDA(launch_inv_rows(g, fc[c], c, cn, ms, 1, 0, 0, nullptr, nullptr, nullptr, st));
+        NA_CUDA(launch_inv_rows(g, fc[c], c, cn, ms, 1, g.blockH, 0, 0, nullptr, nullptr, nullptr, st));
     }
     NA_CUDA(launch_norm(d_img, istride, step, ms, 1, ng, cn, parts, &F->normDone, d_out, st));
 #undef NA_CUDA
