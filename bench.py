@@ -677,6 +677,7 @@ def run_gpu_secondary(args):
         frame, tpls, _ = scene_c4(count=args.templates)
         ms = [cvm.NewMatcher(t) for t in tpls]
         fleet = cvm.NewFleet(*ms)
+        fleet.SetForm({"exact": cvm.FORM_EXACT, "fast": cvm.FORM_FAST}[args.form])
         n = len(ms)
         H, W = frame.shape[:2]
         mpx = n * W * H / 1e6
@@ -697,7 +698,7 @@ def run_gpu_secondary(args):
 
         h2d, d2h = frame.nbytes, 24 * n
         cfg = {"workload": f"Fleet.FindAll, {n} RGBA templates 16..192 x 16..128 on a 2560x1440 RGBA frame",
-               "templates": n, "parent": [W, H]}
+               "templates": n, "parent": [W, H], "form": args.form}
 
         def cpu_sample():
             k = 4
@@ -826,6 +827,8 @@ def main():
     ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map", "stream"],
                     help="match (default, the reported line) or a secondary configuration")
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
+    ap.add_argument("--form", default="exact", choices=["exact", "fast"],
+                    help="fleet member-tail arithmetic for --workload fleet (cvm_fleet_set_form)")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     args = ap.parse_args()
     if args.warmup < 3:

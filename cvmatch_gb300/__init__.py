@@ -101,6 +101,7 @@ def lib():
             L.cvm_fleet_free.argtypes = [vp]
             L.cvm_fleet_free.restype = None
             L.cvm_fleet_set_roi.argtypes = [vp, i32, i32, i32, i32, i32]
+            L.cvm_fleet_set_form.argtypes = [vp, i32]
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
             L.cvm_stream_push.argtypes = [vp, u8p, i64]
             L.cvm_stream_pull.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
@@ -284,6 +285,10 @@ def NewGrayMatcher(sub) -> Matcher:
     return Matcher(_gray(sub), 1)
 
 
+FORM_EXACT = 0
+FORM_FAST = 1
+
+
 class Fleet:
     """Many prepared matchers against one frame (fleet.go:19-50)."""
 
@@ -312,6 +317,12 @@ class Fleet:
         """Restrict member (construction order) to a region of interest in
         frame pixels; w or h <= 0 clears it (see cvm_fleet_set_roi)."""
         _check(lib().cvm_fleet_set_roi(self._h, member, x, y, w, h))
+
+    def SetForm(self, form: int):
+        """FORM_EXACT (default: the reference's float32 arithmetic, bit for
+        bit) or FORM_FAST (zero-mean templates, channels summed in the
+        frequency domain; see cvm_fleet_set_form)."""
+        _check(lib().cvm_fleet_set_form(self._h, form))
 
     def __len__(self):
         return len(self._ms)

@@ -273,13 +273,28 @@ size_t tspec_elems(const FftClass &f, int cnS) { return (size_t)cnS * f.dftH * f
 // Template spectra on plan G for cnS channels: forward rows, forward
 // columns scaled by 1/(dftW*dftH) (impl.go:535-553), then the shrunk-band
 // gather (impl.go:591-610).  cnDev limits the channels on the device.
+// The template spectrum, scaled by 1/(dftW*dftH) (buildTSpecSet,
+// impl.go:520-561).  tsum (the fast form): per-channel template sums; the
+// spectrum is then that of the zero-mean template area*T - sum(T), built
+// from exact integer samples when area*255 < 2^24 (else T - mean), and
+// scaled back by 1/area, so the correlation it yields is the numerator
+// sum(I*T) - sum(I)*sum(T)/area directly.
 int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step, int tw, int th,
-                int cnS, const int *cnDev, float2 *ts0, float2 *ts1, cudaStream_t st) {
+                int cnS, const int *cnDev, float2 *ts0, float2 *ts1, cudaStream_t st,
+                const int64_t *tsum = nullptr) {
     TileGeom tg;
     FftClass tf;
     template_geom(G, tw, th, tg, tf);
-    CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st, 0, "k_fwd_rows_tpl"));
-    const float scale = 1.0f / (float(G.p.dftW) * float(G.p.dftH));
+    float mul = 1.0f, sub[4] = {0.f, 0.f, 0.f, 0.f};
+    const double area = double(tw) * double(th);
+    if (tsum) {
+        const bool exact = area * 255.0 < 16777216.0;
+        mul = exact ? float(area) : 1.0f;
+        for (int k = 0; k < 4; k++) sub[k] = exact ? float(tsum[k]) : float(double(tsum[k]) / area);
+    }
+    CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st, 0, "k_fwd_rows_tpl", mul,
+                             tsum ? sub : nullptr));
+    const float scale = float(1.0 / (double(G.p.dftW) * double(G.p.dftH) * double(mul)));
     MemberSet none;
     memset(&none, 0, sizeof none);
     CVM_CUDA(launch_cols(0, ts0, ts0, cnS, tg, tf, 0, cnS, cnDev, scale, none, 1, st, "k_cols_tpl"));
@@ -770,6 +785,7 @@ struct FleetBucketGeom {
 
 struct FleetGeom {
     int pw = 0, ph = 0;
+    int form = CVM_FORM_EXACT;  // the form the spectra were built for
     std::vector<std::unique_ptr<FleetBucketGeom>> bg;
 };
 
@@ -782,6 +798,7 @@ struct cvm_fleet {
     std::shared_ptr<FleetGeom> geom;
     std::vector<int32_t> roi;  // per member x, y, w, h in frame pixels (w <= 0: the whole frame)
     uint64_t roiGen = 0;       // bumped by every cvm_fleet_set_roi
+    int form = CVM_FORM_EXACT; // arithmetic of the member tails (cvm_fleet_set_form)
     ~cvm_fleet() {
         if (dP) cudaFree(dP);
     }
@@ -835,11 +852,17 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
     auto fg = std::make_shared<FleetGeom>();
     fg->pw = pw;
     fg->ph = ph;
+    fg->form = f->form;
     cudaStream_t st = thread_stream();
     for (const Bucket &b : f->buckets) {
         auto bg = std::make_unique<FleetBucketGeom>();
         const int rwF = pw - b.tw + 1, rhF = ph - b.th + 1;
         CVM_TRY(make_geom(b.tw, b.th, rwF, rhF, b.th, bg->G));
+        if (f->form != CVM_FORM_EXACT)
+            for (int c = 0; c < bg->G.nclass; c++)
+                if (bg->G.fc[c].log2n < 5 || bg->G.fc[c].log2n > 12 || bg->G.fc[c].log2H < 5 || bg->G.fc[c].log2H > 12)
+                    return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: fast form needs transforms of 32..4096 (%dx%d)",
+                                bg->G.fc[c].n, bg->G.fc[c].dftH);
         bg->cnS = f->step;
         bg->members = b.members;
         const Geom &G = bg->G;
@@ -864,7 +887,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
                 bg->ts.push_back(t[c]);
             }
             CVM_TRY(build_tspec(G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, bg->cnS, nullptr,
-                                t[0], t[1], st));
+                                t[0], t[1], st, f->form != CVM_FORM_EXACT ? m->tsum : nullptr));
             DevMember &d = tab[pos];
             memset(&d, 0, sizeof d);
             d.tspec[0] = t[0];
@@ -882,7 +905,9 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         bg->tabHost = tab;
         CVM_CUDA(cudaMalloc(&bg->table, tab.size() * sizeof(DevMember)));
         CVM_CUDA(cudaMemcpy(bg->table, tab.data(), tab.size() * sizeof(DevMember), cudaMemcpyHostToDevice));
-        for (int c = 0; c < G.nclass; c++) bg->memberScratch[c] = spec_elems(G.fc[c], bg->cnS);
+        // the fast form's member tails keep one channel-summed spectrum per tile
+        for (int c = 0; c < G.nclass; c++)
+            bg->memberScratch[c] = spec_elems(G.fc[c], f->form != CVM_FORM_EXACT ? 1 : bg->cnS);
         fg->bg.push_back(std::move(bg));
     }
     CVM_CUDA(cudaStreamSynchronize(st));
@@ -984,6 +1009,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
+        const bool fast = fg->form != CVM_FORM_EXACT;
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
         float2 *lanes = nullptr;
@@ -999,8 +1025,12 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             lanes = wa.take<float2>((size_t)wave[b] * bg.rwMax * bg.rhMax);
         }
         // Phase 1: the frame's tile spectra, once per bucket (fleet.go:240-263).
+        // the fast form transforms the frame offset by -128 (the zero-mean
+        // templates make the correlation independent of the offset)
+        const float off[4] = {128.f, 128.f, 128.f, 128.f};
         for (int c = 0; c < G.nclass; c++) {
-            CVM_CUDA(launch_fwd_rows(dParent, pstride, f->step, cnS, &F->cnMax, G.g, G.fc[c], frame[c], cnS, st));
+            CVM_CUDA(launch_fwd_rows(dParent, pstride, f->step, cnS, &F->cnMax, G.g, G.fc[c], frame[c], cnS, st, 0,
+                                     nullptr, 1.0f, fast ? off : nullptr));
             MemberSet none;
             memset(&none, 0, sizeof none);
             CVM_CUDA(launch_cols(0, frame[c], frame[c], cnS, G.g, G.fc[c], c, cnS, &F->cnMax, 1.0f, none, 1, st));
@@ -1013,6 +1043,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         ms.lanes = lanes;
         ms.lanesStride = (size_t)bg.rwMax * bg.rhMax;
         ms.anyRoi = !f->roi.empty();
+        ms.form = fast ? 1 : 0;
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -1026,10 +1057,11 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
                                       cnP, prefix, 0, st, 1));
             for (int c = 0; c < G.nclass; c++)
-                CVM_CUDA(launch_cols(2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw, st));
+                CVM_CUDA(launch_cols(fast ? 3 : 2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw,
+                                     st));
             for (int c = 0; c < G.nclass; c++)
-                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, cnS, ms, nw, G.fc[c].dftH, bg.partOff[c], bg.nparts, parts,
-                                         counters, dOut, st));
+                CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, fast ? 1 : cnS, ms, nw, G.fc[c].dftH, bg.partOff[c],
+                                         bg.nparts, parts, counters, dOut, st));
         }
     }
     return CVM_OK;
@@ -1426,6 +1458,18 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 }
 
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_fleet_set_form(cvm_fleet *f, int form) {
+    if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
+    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: unknown fleet form %d", form);
+    std::lock_guard<std::mutex> lk(f->mu);
+    if (f->form != form) {
+        f->form = form;
+        f->geom.reset();  // spectra of the other form
+    }
+    return CVM_OK;
+}
 
 int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h) {
     if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");

@@ -240,7 +240,7 @@ __device__ __forceinline__ void col_passes(const IO &io, const float2 *__restric
 
 // The middle sweep (see the file header).  x[c'] is row B + S*c' of the
 // forward's natural-order output; FWD runs the forward's last pass on it.
-template <bool FWD, int L, int LSC, typename LDX>
+template <bool FWD, int L, int LSC, typename LDX, bool MUL = true>
 __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const float2 *__restrict__ ts, int hwp,
                                              int wv, const float2 *__restrict__ tri) {
     constexpr int N = 1 << L, PL = npass(L) - 1;
@@ -270,11 +270,13 @@ __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const
                 }
             }
         }
-        // spec *= conj(tspec) (mulConjGo, impl.go:376-388)
-        const float2 *tp = ts + (size_t)B * hwp + c;
+        if constexpr (MUL) {
+            // spec *= conj(tspec) (mulConjGo, impl.go:376-388)
+            const float2 *tp = ts + (size_t)B * hwp + c;
 #pragma unroll
-        for (int ci = 0; ci < M; ci++)
-            x[ci] = mul_conj(x[ci], c < wv ? __ldg(tp + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f));
+            for (int ci = 0; ci < M; ci++)
+                x[ci] = mul_conj(x[ci], c < wv ? __ldg(tp + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f));
+        }
         float2 *sp = smem + (B << LSC) + c;
         if constexpr (L & 1) {
             // inverse head(s): logical 8a+t <-> row B' + (N/8)*brev3(t)
@@ -306,10 +308,18 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
     constexpr int SC = N >= 1024 ? 8192 / N : 16, LSC = ilog2k(SC);
     extern __shared__ float2 smem[];
     const FftClass &fc = a.fc;
-    // mode 2 (a fleet wave): members vary fastest, so the CTAs resident
-    // together read the same frame tile spectrum and share it in L2
-    const int tileLocal = MODE == 2 ? blockIdx.z / a.nmem : blockIdx.z % fc.ntiles;
-    const int slot = MODE == 2 ? blockIdx.z - tileLocal * a.nmem : blockIdx.z / fc.ntiles;
+    // modes 2 and 3 (a fleet wave): the column strip is the slowest grid
+    // dimension and members vary fastest within it.  A strip partitions
+    // every operand (frame tile spectra, template spectra, output), so the
+    // CTAs of one strip -- all tiles x members -- touch a working set of
+    // (tiles x channels + members x channels) strips, a few MB that stay in
+    // L2: each frame and template spectrum leaves HBM about once per wave
+    // instead of once per (member, tile) pair.
+    constexpr bool WAVE = MODE >= 2;
+    const int pairIdx = WAVE ? blockIdx.x : blockIdx.z;
+    const int strip = WAVE ? blockIdx.z : blockIdx.x;
+    const int tileLocal = WAVE ? pairIdx / a.nmem : pairIdx % fc.ntiles;
+    const int slot = WAVE ? pairIdx - tileLocal * a.nmem : pairIdx / fc.ntiles;
     const int tile = fc.tileFirst + tileLocal;
     const int k = blockIdx.y;
     const DevMember *m = MODE == 0 ? nullptr : &member_of(a.ms, slot);
@@ -322,8 +332,8 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
     if (k >= cn) return;
     if (Pm && Pm->flat) return;
     const TileBox b = tile_box(a.g, tile);
-    if (MODE == 2 && a.ms.anyRoi && roi_misses_tile(a.g, tile, b, *m)) return;  // outside the member's ROI
-    const int c0 = blockIdx.x * SC;
+    if (WAVE && a.ms.anyRoi && roi_misses_tile(a.g, tile, b, *m)) return;  // outside the member's ROI
+    const int c0 = strip * SC;
     const int hwp = fc.hwp;
     const int wv = min(SC, fc.hw - c0);
     const size_t chanStride = (size_t)N * hwp;
@@ -331,7 +341,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
     const float2 *src = a.in + ((size_t)tileLocal * a.cnS + k) * chanStride + c0;
     const SmemNat<LSC> sn{smem};
     const SmemRev<L, LSC> sr{smem};
-    if (MODE != 2) {
+    if (!WAVE) {
         const GlobalSlots<L> gs{src, hwp, wv, min(N, (b.loadH + 1) & ~1)};
         col_pass<false, L, 0, LSC>(gs, sn, tri);
         if (MODE == 0) {
@@ -353,6 +363,27 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
                 for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
             };
             middle_sweep<true, L, LSC>(smem, ldx, ts, hwp, wv, tri);
+        } else if (MODE == 3) {
+            // fast form: sum over the member's channels of frame spectrum
+            // times conj(zero-mean template spectrum), fused multiply-adds
+            const float2 *fr = a.in + (size_t)tileLocal * a.cnS * chanStride + c0;
+            const float2 *tq = m->tspec[a.cls] + c0;
+            auto ldx = [&](float2 *x, int c, int B) {
+#pragma unroll
+                for (int ci = 0; ci < M; ci++) x[ci] = make_float2(0.f, 0.f);
+                if (c >= wv) return;
+                for (int kk = 0; kk < cn; kk++) {
+                    const float2 *p = fr + (size_t)kk * chanStride + (size_t)B * hwp + c;
+                    const float2 *q = tq + (size_t)kk * chanStride + (size_t)B * hwp + c;
+#pragma unroll
+                    for (int ci = 0; ci < M; ci++) {
+                        const float2 f = __ldg(p + (size_t)(S * ci) * hwp), t = __ldg(q + (size_t)(S * ci) * hwp);
+                        x[ci].x = fmaf(f.x, t.x, fmaf(f.y, t.y, x[ci].x));
+                        x[ci].y = fmaf(f.y, t.x, fmaf(-f.x, t.y, x[ci].y));
+                    }
+                }
+            };
+            middle_sweep<false, L, LSC, decltype(ldx), false>(smem, ldx, nullptr, hwp, wv, tri);
         } else {
             // the frame tile's stored natural-order spectrum
             auto ldx = [&](float2 *x, int c, int B) {
@@ -364,9 +395,9 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
         }
         const int ty = tile / a.g.ntx;
         const int bh = (ty == a.g.nty - 1) ? m->rh - b.y0 : a.g.blockH;
-        const GlobalInv<L> gi{a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] +
-                                  ((size_t)tileLocal * a.cnS + k) * chanStride + c0,
-                              hwp, wv, min(N, (bh + 1) & ~1)};
+        const size_t scrOff = MODE == 3 ? (size_t)tileLocal * chanStride : ((size_t)tileLocal * a.cnS + k) * chanStride;
+        const GlobalInv<L> gi{a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] + scrOff + c0, hwp, wv,
+                              min(N, (bh + 1) & ~1)};
         col_passes<true, L, 1, NP - 1, LSC>(sr, tri);
         col_pass<true, L, NP - 1, LSC>(sr, gi, tri);
     }
@@ -401,8 +432,10 @@ void launch_cols_fixed(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t s
         cols_mode<0>(a, grid, smem, st);
     else if (a.mode == 1)
         cols_mode<1>(a, grid, smem, st);
-    else
+    else if (a.mode == 2)
         cols_mode<2>(a, grid, smem, st);
+    else
+        cols_mode<3>(a, grid, smem, st);
 }
 
 }  // namespace cvm

@@ -51,7 +51,8 @@ struct InvArgs {
 
 // Arguments of the column kernels (colsR4Go, mulConjGo; mode 0: forward
 // spectrum, 1: forward + conj-multiply + inverse, 2: conj-multiply + inverse
-// of a stored natural-order spectrum).
+// of a stored natural-order spectrum, 3: the fast form's channel sum of the
+// conj-products + one inverse into channel slot 0).
 struct ColsArgs {
     int mode;
     const float2 *in;
@@ -65,7 +66,7 @@ struct ColsArgs {
     float scale;
     MemberSet ms;
     int SC, logSC;
-    int nmem;   // members of the launch (grid z = ntiles * nmem)
+    int nmem;   // members of the launch (waves: grid x = ntiles * nmem, z = strips)
 };
 
 // Arguments of the forward-rows kernels (forwardRowPair, impl.go:301-344).
@@ -80,6 +81,12 @@ struct FwdRowsArgs {
     float2 *spec;
     int cnS, pairsPerCta;
     int pix32;               // 4-byte pixels readable as aligned 32-bit words
+    // each loaded sample is pixel * mul - sub[channel] (exact for the
+    // integer values used: 1 and 0 for the reference's arithmetic, the
+    // frame offset and the zero-mean template of the fast form); padding
+    // stays zero
+    float mul;
+    float sub[4];
 };
 
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).

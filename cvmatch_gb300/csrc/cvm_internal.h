@@ -109,6 +109,10 @@ struct MemberSet {
     float2 *lanes;             // per result (t, den) of the statistics kernel, per wave slot
     size_t lanesStride;        // elements between wave slots
     int anyRoi;                // some member of the launch has a region of interest
+    // 0: the reference's arithmetic (per-channel inverses, num = corr - t);
+    // 1: the fast form (zero-mean template spectra, channels summed in the
+    // frequency domain, one inverse per tile, num = corr)
+    int form;
 };
 
 struct Partial {
@@ -132,14 +136,19 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 // Forward row pass of every tile of `fc` (or of a template: geometry with
 // one 1x1 block whose loads are the template's tw x th).
 // Channels [chanFirst, min(chanCount, *cnDev)) are transformed.
+// Each sample is pixel * mul - sub[channel] (fixed transform lengths only
+// when mul != 1 or sub is set).
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st, int chanFirst = 0, const char *label = nullptr);
+                            int cnS, cudaStream_t st, int chanFirst = 0, const char *label = nullptr,
+                            float mul = 1.0f, const float *sub = nullptr);
 // Column pass.  mode 0: forward only, natural output (template spectra with
 // `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
 // conj-multiply + inverse, in place on the members' scratch (solo match);
 // mode 2: conj-multiply + inverse from a forward frame cache `in` into each
-// member's scratch (fleet tails).  nmembers targets from ms.
+// member's scratch (fleet tails); mode 3: the fast form's channel sum of
+// the conj-products, one inverse into the member's single-channel scratch.
+// nmembers targets from ms.
 cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const TileGeom &g,
                         const FftClass &fc, int cls, int chanCount, const int *cnDev, float scale,
                         const MemberSet &ms, int nmembers, cudaStream_t st, const char *label = nullptr);

@@ -1541,7 +1541,10 @@ struct VstatArgs {
 // PRE: H is the shared row prefix built for PCN channels (window sum =
 // P[x+tw] - P[x]); its squares are plane PCN (PCN < 4) or planes 4 (RGB)
 // and 5 (alpha) when PCN == 4 (a cn = 3 member leaves alpha out).
-template <int CN, bool PRE, int PCN>
+// FAST (the fleet's fast form, zero-mean template spectra): the
+// correlation already is the numerator, so only den is stored, one float
+// per result (the first half of the member's lanes slot).
+template <int CN, bool PRE, int PCN, bool FAST = false>
 __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &m, const DevParams &Pm) {
     constexpr int NP = PRE ? (PCN == 4 ? 4 : stat_pitch_c(PCN)) : stat_pitch_c(CN);
     // PRE (a fleet wave): members vary fastest across the grid, so the
@@ -1558,6 +1561,7 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     const unsigned int *H = a.H + (PRE ? 0 : (size_t)slot * a.slotStride) + (size_t)x * NP;
     const int twoff = PRE ? m.tw * NP : 0;
     float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride + x;
+    float *dens = reinterpret_cast<float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride) + x;
     // the CN sums and the squared sum of row h's window
     auto rowvals = [&](const unsigned int *h, unsigned int *hv) {
         unsigned int A[NP];
@@ -1613,23 +1617,22 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             rowvals(H + (size_t)(y + th) * rp, hin);
             rowvals(H + (size_t)y * rp, hout);
         }
-        unsigned long long cross = (unsigned long long)s[0] * t0, sq = (unsigned long long)s[0] * s[0];
+        unsigned long long cross = 0, sq = (unsigned long long)s[0] * s[0];
+        if (!FAST) cross = (unsigned long long)s[0] * t0;
         if (CN > 1) {
-            cross += (unsigned long long)s[CN > 1 ? 1 : 0] * t1;
+            if (!FAST) cross += (unsigned long long)s[CN > 1 ? 1 : 0] * t1;
             sq += (unsigned long long)s[CN > 1 ? 1 : 0] * s[CN > 1 ? 1 : 0];
         }
         if (CN > 2) {
-            cross += (unsigned long long)s[CN > 2 ? 2 : 0] * t2;
+            if (!FAST) cross += (unsigned long long)s[CN > 2 ? 2 : 0] * t2;
             sq += (unsigned long long)s[CN > 2 ? 2 : 0] * s[CN > 2 ? 2 : 0];
         }
         if (CN > 3) {
-            cross += (unsigned long long)s[CN > 3 ? 3 : 0] * t3;
+            if (!FAST) cross += (unsigned long long)s[CN > 3 ? 3 : 0] * t3;
             sq += (unsigned long long)s[CN > 3 ? 3 : 0] * s[CN > 3 ? 3 : 0];
         }
         // the spill lanes (impl.go:902-1009) and normOne's corr-free part
-        const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);
         const float id = f32_via_f64((long long)(area * q - sq));
-        const float t = __fmul_rn(l0, Pm.numScale);
         const float diff2 = __fmul_rn(id, Pm.varScale);
         float lim = 0.5f;
         if (q < (1ull << 24)) {
@@ -1637,7 +1640,12 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             if (lim > 0.5f) lim = 0.5f;
         }
         const float den = diff2 > lim ? __fmul_rn(__fsqrt_rn(diff2), Pm.templNorm) : 0.f;
-        lanes[(size_t)y * m.rw] = make_float2(t, den);
+        if (FAST) {
+            dens[(size_t)y * m.rw] = den;
+        } else {
+            const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);
+            lanes[(size_t)y * m.rw] = make_float2(__fmul_rn(l0, Pm.numScale), den);
+        }
         if (more) {
 #pragma unroll
             for (int k = 0; k < CN; k++) s[k] += hin[k] - hout[k];
@@ -1646,15 +1654,15 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     }
 }
 
-template <int CNA, int CNB, bool PRE>
+template <int CNA, int CNB, bool PRE, bool FAST = false>
 __global__ void __launch_bounds__(256) k_vstats(VstatArgs a) {
     const DevMember &m = member_of(a.ms, PRE ? blockIdx.x : blockIdx.z);
     const DevParams &Pm = a.ms.params[m.pIdx];
     if (Pm.flat) return;
     if (Pm.cn == CNA)
-        vstat_cols<CNA, PRE, CNB>(a, m, Pm);
+        vstat_cols<CNA, PRE, CNB, FAST>(a, m, Pm);
     else if (CNB != CNA && Pm.cn == CNB)
-        vstat_cols<CNB, PRE, CNB>(a, m, Pm);
+        vstat_cols<CNB, PRE, CNB, FAST>(a, m, Pm);
 }
 
 // Frame ingest from page-locked host memory: the GPU reads the caller's
@@ -1779,7 +1787,8 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
-                            int cnS, cudaStream_t st, int chanFirst, const char *label) {
+                            int cnS, cudaStream_t st, int chanFirst, const char *label, float mul,
+                            const float *sub) {
     // Channels per launch so that one row pair of the group fits 128 KB of
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
@@ -1814,6 +1823,8 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         a.cnS = cnS;
         a.pairsPerCta = P;
         a.pix32 = step == 4 && (reinterpret_cast<uintptr_t>(img) & 3) == 0 && (istride & 3) == 0;
+        a.mul = mul;
+        for (int k = 0; k < 4; k++) a.sub[k] = sub ? sub[k] : 0.0f;
         for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
             a.chanFirst = c0;
             launch_fwd_rows_fixed(a, grid, threads, smem, st);
@@ -1821,6 +1832,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         }
         return cudaGetLastError();
     }
+    if (mul != 1.0f || sub) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
     set_smem(k_fwd_rows, smem);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
         k_fwd_rows<<<grid, threads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
@@ -1851,9 +1863,17 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     if (SC < 1) SC = 1;
     a.SC = SC;
     a.logSC = ilog2i(SC);
-    dim3 grid((fc.hw + SC - 1) / SC, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
+    // the generic kernels take (strip, channel, tile x member); the fixed
+    // heights' fleet modes take (tile x member, channel, strip)
+    const int strips = (fc.hw + SC - 1) / SC;
+    dim3 grid(strips, chanCount, fc.ntiles * (mode == 0 ? 1 : nmembers));
+    if (mode >= 2 && cols_fixed_length(fc.log2H)) grid = dim3(fc.ntiles * nmembers, mode == 3 ? 1 : chanCount, strips);
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
-    ProfScope ps(label ? label : (mode == 0 ? "k_cols_fwd" : (mode == 1 ? "k_cols_fwd_mul_inv" : "k_cols_mul_inv")), st);
+    ProfScope ps(label ? label
+                       : (mode == 0 ? "k_cols_fwd"
+                                    : (mode == 1 ? "k_cols_fwd_mul_inv" : (mode == 2 ? "k_cols_mul_inv" : "k_cols_sum_inv"))),
+                 st);
+    if (mode == 3 && !cols_fixed_length(fc.log2H)) return cudaErrorInvalidValue;  // fast form: fixed heights only
     if (cols_fixed_length(fc.log2H)) {
         launch_cols_fixed(a, grid, smem, st);
     } else if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
@@ -2052,7 +2072,16 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     }
     {
         ProfScope ps("k_vstats", st);
-        if (sharedPrefix) {
+        if (sharedPrefix && ms.form) {
+            if (cnMax == 1)
+                k_vstats<1, 1, true, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMax == 2)
+                k_vstats<2, 2, true, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMin == 3)
+                k_vstats<3, 4, true, true><<<gv, kThreads, 0, st>>>(v);
+            else
+                k_vstats<4, 4, true, true><<<gv, kThreads, 0, st>>>(v);
+        } else if (sharedPrefix) {
             if (cnMax == 1)
                 k_vstats<1, 1, true><<<gv, kThreads, 0, st>>>(v);
             else if (cnMax == 2)

@@ -190,6 +190,15 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
                         if (two) vb[g] = (float)q[istride + a.chanFirst + g];
                     }
             }
+            // pixel * mul - sub: exact for the integer operands used (x1 - 0
+            // leaves the reference's samples untouched); the missing second
+            // row of an odd tail stays zero
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                const float sg = a.sub[(a.chanFirst + g) & 3];
+                va[g] = __fsub_rn(__fmul_rn(va[g], a.mul), sg);
+                vb[g] = two ? __fsub_rn(__fmul_rn(vb[g], a.mul), sg) : 0.f;
+            }
         }
         float2 *d = smem + (p * cn) * LD + padi(brevn<LOG2N>(x));
 #pragma unroll
@@ -272,8 +281,10 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * LD);  // [P][2][N]
     Ext e;
     ext_init(e);
+    // the fast form's scratch holds one channel-summed correlation per tile
+    const bool fast = a.ms.form != 0;
     if (P > 0 && !flat) {
-        const int cn = Pm.cn;
+        const int cn = fast ? 1 : Pm.cn;
         const size_t chanStride = (size_t)fc.dftH * hwp;
         const float2 *scr = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls];
         for (int k = 0; k < cn; k++) {
@@ -345,11 +356,16 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
             if (r >= bh) break;
             const long long rowBase = (long long)(tb.y0 + r) * m.rw + tb.x0;
             if (tb.y0 + r < m.roiY0 || tb.y0 + r >= m.roiY1) continue;  // no map here (only fleets have ROIs)
+            // (t, den); the fast form stores den alone, one float per result
             float2 td[XIT];
 #pragma unroll
             for (int q = 0; q < XIT; q++) {
                 const int x = tid + q * kThreads;
-                td[q] = (!flat && x < bw) ? __ldg(lanes + rowBase + x) : make_float2(0.f, 0.f);
+                if (fast)
+                    td[q] = make_float2(0.f, (!flat && x < bw) ? __ldg(reinterpret_cast<const float *>(lanes) + rowBase + x)
+                                                               : 0.f);
+                else
+                    td[q] = (!flat && x < bw) ? __ldg(lanes + rowBase + x) : make_float2(0.f, 0.f);
             }
 #pragma unroll
             for (int q = 0; q < XIT; q++) {
@@ -357,10 +373,10 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 if (x < bw) {
                     float score = 1.f;
                     if (!flat) {
-                        const float num = __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
+                        const float num = fast ? acc[(size_t)rr * N + x] : __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
                         const float den = td[q].y, an = fabsf(num);
                         if (an < den)
-                            score = __fdiv_rn(num, den);
+                            score = fast ? __fdividef(num, den) : __fdiv_rn(num, den);
                         else if (an < __fmul_rn(den, 1.125f))
                             score = num > 0.f ? 1.f : -1.f;
                         else

@@ -196,6 +196,24 @@ void cvm_fleet_free(cvm_fleet *f);
  * Not to be called while a FindAll on the same fleet runs. */
 int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h);
 
+/* Arithmetic of a fleet's member tails.  CVM_FORM_EXACT (the default) is
+ * the reference's float32 pipeline op for op: every score equals
+ * Fleet.FindAll's bit for bit (fleet.go:176-332, impl.go:301-464,
+ * 825-849).  CVM_FORM_FAST gives up that bit identity for throughput and
+ * conditioning: templates enter as their zero-mean form area*T - sum(T)
+ * (exact integers), the frame as I - 128, so the correlation is the
+ * TM_CCOEFF_NORMED numerator itself (no float32 cancellation against
+ * sum(I)*sum(T)/area); the channels of a member are summed in the
+ * frequency domain, so each member tile takes one inverse transform
+ * instead of one per channel; the window statistics and the score
+ * ladder stay those of normOne.  Scores then differ from the reference's
+ * by rounding only (bounded against the FP64 definition in the tests).
+ * Changing the form drops the fleet's cached spectra; not to be called
+ * while a FindAll on the same fleet runs.  Transform sizes above 4096
+ * are CVM_ERR_UNSUPPORTED in the fast form. */
+enum { CVM_FORM_EXACT = 0, CVM_FORM_FAST = 1 };
+int cvm_fleet_set_form(cvm_fleet *f, int form);
+
 /* ------------------------------------------------------- frame streams */
 
 /* A stream of RGBA frames of one size matched against a colour fleet and,

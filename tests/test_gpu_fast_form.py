@@ -1,0 +1,136 @@
+"""The fleet's fast form (CVM_FORM_FAST) against the FP64 definition.
+
+The fast form leaves the reference's float32 op sequence (zero-mean
+templates, the frame offset by -128, channels summed in the frequency
+domain), so its scores are checked against the FP64 direct correlation of
+cvmatch_test.go:13-81 rather than bit for bit: every extremum within TOL
+of the FP64 map's, and the position it reports scoring within 2*TOL of
+the FP64 extremum there (ties closer than the tolerance may pick either
+position).  TOL is the reference's own worst recorded drift against FP64
+(CLAUDE.md:61-75); the measured errors are printed (pytest -s).
+"""
+import numpy as np
+import pytest
+
+import cvmatch_gb300 as cvm
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 5.5e-4
+
+
+def scene(seed, h, w):
+    """Noise background, flat rectangles and horizontal gradients (UI-like
+    near-flat windows are where float32 correlation loses the most)."""
+    rng = np.random.default_rng(seed)
+    img = np.empty((h, w, 4), np.uint8)
+    img[..., :3] = rng.integers(0, 256, (h, w, 3))
+    img[..., 3] = 255
+    for i in range(24):
+        rw, rh = rng.integers(4, max(5, w // 3)), rng.integers(4, max(5, h // 3))
+        x, y = rng.integers(0, w - rw), rng.integers(0, h - rh)
+        if i % 3 == 2:
+            ramp = np.linspace(rng.integers(0, 128), rng.integers(128, 256), rw)
+            img[y:y + rh, x:x + rw, :3] = ramp[None, :, None].astype(np.uint8)
+        else:
+            img[y:y + rh, x:x + rw, :3] = rng.integers(0, 256, 3)
+    return img
+
+
+def members(img, seed):
+    rng = np.random.default_rng(seed)
+    sizes = [(24, 24), (64, 48), (33, 17), (48, 40), (16, 16), (40, 56)]
+    tpls, at = [], []
+    for i, (w, h) in enumerate(sizes):
+        x, y = int(rng.integers(0, img.shape[1] - w)), int(rng.integers(0, img.shape[0] - h))
+        t = img[y:y + h, x:x + w].astype(np.int32)
+        if i % 2:  # a*x+b shifted copy
+            t = np.clip(np.rint(t * rng.uniform(0.9, 1.1) + rng.uniform(-10, 10)), 0, 255)
+        t = t.astype(np.uint8)
+        t[..., 3] = 255
+        tpls.append(t)
+        at.append((x, y))
+    absent = scene(seed + 100, 30, 44)  # from an independent seed
+    tpls.append(absent)
+    at.append(None)
+    return tpls, at
+
+
+def check(got, m64, name):
+    mx, mn = float(m64.max()), float(m64.min())
+    e_max, e_min = abs(got.MaxV - mx), abs(got.MinV - mn)
+    print(f"\n{name}: |max err| {e_max:.2e}  |min err| {e_min:.2e}")
+    assert e_max <= TOL and e_min <= TOL
+    assert m64[got.MaxY, got.MaxX] >= mx - 2 * TOL
+    assert m64[got.MinY, got.MinX] <= mn + 2 * TOL
+    return max(e_max, e_min)
+
+
+@pytest.mark.parametrize("gray", [False, True])
+def test_fast_fleet_vs_fp64(gray):
+    img = scene(5, 300, 420)
+    tpls, at = members(img, 7)
+    if gray:
+        ms = [cvm.NewGrayMatcher(t) for t in tpls]
+    else:
+        ms = [cvm.NewMatcher(t) for t in tpls]
+    fleet = cvm.NewFleet(*ms)
+    fleet.SetForm(cvm.FORM_FAST)
+    got = fleet.FindAll(img)
+    src = oracle.rgba_to_gray(img) if gray else img
+    worst = 0.0
+    for i, t in enumerate(tpls):
+        tt = oracle.rgba_to_gray(t) if gray else t
+        m64 = oracle.ref_match_f64(src, tt, 1 if gray else 3, threads=16)
+        worst = max(worst, check(got[i], m64, f"member {i} {t.shape[1]}x{t.shape[0]}"))
+        if at[i] is not None and i % 2 == 0:  # exact crops are found where they were cut
+            assert (got[i].MaxX, got[i].MaxY) == at[i]
+    print(f"\nworst extremum error against FP64: {worst:.2e}")
+
+
+def test_fast_fleet_varying_alpha_member():
+    img = scene(9, 240, 320)
+    t = img[50:90, 100:148].copy()
+    t.reshape(-1, 4)[::3, 3] = np.arange(t.reshape(-1, 4)[::3].shape[0]) % 256  # cn = 4 for this member
+    flat = np.full((20, 20, 4), 77, np.uint8)
+    flat[..., 3] = 255
+    tpls = [t, img[10:42, 20:52].copy(), flat]
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(x) for x in tpls])
+    fleet.SetForm(cvm.FORM_FAST)
+    got = fleet.FindAll(img)
+    check(got[0], oracle.ref_match_f64(img, t, 4, threads=16), "varying alpha (cn 4)")
+    check(got[1], oracle.ref_match_f64(img, tpls[1], 3, threads=16), "constant alpha (cn 3)")
+    assert tuple(got[2]) == (1.0, 0, 0, 1.0, 0, 0)  # flat member: impl.go:1137-1144
+
+
+def test_fast_fleet_roi_member():
+    img = scene(13, 260, 380)
+    t = img[120:150, 200:240].copy()
+    fleet = cvm.NewFleet(cvm.NewMatcher(t), cvm.NewMatcher(img[20:40, 30:60].copy()))
+    fleet.SetForm(cvm.FORM_FAST)
+    fleet.SetROI(0, 150, 90, 140, 100)
+    got = fleet.FindAll(img)
+    m64 = oracle.ref_match_f64(img, t, 3, threads=16)
+    th, tw = t.shape[:2]
+    sub = m64[90:90 + 100 - th + 1, 150:150 + 140 - tw + 1]
+    assert abs(got[0].MaxV - sub.max()) <= TOL and (got[0].MaxX, got[0].MaxY) == (200, 120)
+    assert 150 <= got[0].MinX < 150 + 140 - tw + 1 and 90 <= got[0].MinY < 90 + 100 - th + 1
+    assert abs(got[0].MinV - sub.min()) <= TOL
+
+
+def test_form_switch_restores_bit_exact_results():
+    img = scene(17, 200, 300)
+    tpls, _ = members(img, 19)
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    exact = fleet.FindAll(img)
+    want = oracle.fleet_find_all(tpls, img, threads=8)
+    fleet.SetForm(cvm.FORM_FAST)
+    fast = fleet.FindAll(img)
+    fleet.SetForm(cvm.FORM_EXACT)
+    again = fleet.FindAll(img)
+    for e, a, w in zip(exact, again, want):
+        assert tuple(e) == tuple(a) == tuple(w)
+    assert any(tuple(f) != tuple(e) for f, e in zip(fast, exact))  # the fast form is a different arithmetic
+    with pytest.raises(cvm.CvmatchError):
+        fleet.SetForm(7)
