@@ -328,6 +328,9 @@ MPX = 1920 * 1080 / 1e6
 # --------------------------------------------------------- reference arm
 
 
+FORM = {"exact": 0, "fast": 1}  # CVM_FORM_EXACT, CVM_FORM_FAST
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -386,6 +389,7 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     L = cvm.lib()
+    cvm.SetForm(FORM[args.form])
     frame, tpl, _ = scene_c2()
     d_frame = torch.from_numpy(frame).to(dev)
     d_tpl = torch.from_numpy(tpl).to(dev)
@@ -454,7 +458,7 @@ def run_gpu(args):
         line = {"metric": "template*Mpx/s", "value": value, "unit": "template*Mpx/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single"),
+                "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single", form=args.form),
                 "e2e": {"value": replica_throughput(MPX, e2e_ms, ws), "unit": "template*Mpx/s",
                         "h2d_bytes_per_step": int(frame.nbytes + tpl.nbytes), "d2h_bytes_per_step": 24},
                 "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
@@ -670,6 +674,7 @@ def run_gpu_secondary(args):
 
     dev = torch.device("cuda", 0)
     L = cvm.lib()
+    cvm.SetForm(FORM[args.form])
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -677,7 +682,7 @@ def run_gpu_secondary(args):
         frame, tpls, _ = scene_c4(count=args.templates)
         ms = [cvm.NewMatcher(t) for t in tpls]
         fleet = cvm.NewFleet(*ms)
-        fleet.SetForm({"exact": cvm.FORM_EXACT, "fast": cvm.FORM_FAST}[args.form])
+        fleet.SetForm(FORM[args.form])
         n = len(ms)
         H, W = frame.shape[:2]
         mpx = n * W * H / 1e6
@@ -731,7 +736,8 @@ def run_gpu_secondary(args):
                                          C.byref(res)) == 0
 
         h2d, d2h = frame.nbytes + tpl.nbytes, 24
-        cfg = {"workload": "MatchGray 640x480 (from RGBA), template 64x48", "parent": [W, H], "templates": 1}
+        cfg = {"workload": "MatchGray 640x480 (from RGBA), template 64x48", "parent": [W, H], "templates": 1,
+               "form": args.form}
 
         def cpu_sample():
             t0 = time.perf_counter()
@@ -769,7 +775,7 @@ def run_gpu_secondary(args):
 
         h2d, d2h = g.nbytes + tpl.nbytes, hmap.nbytes + 24
         cfg = {"workload": "MatchMap gray 3840x2160, template 256x256, full float32 map returned",
-               "parent": [W, H], "templates": 1}
+               "parent": [W, H], "templates": 1, "form": args.form}
 
         def cpu_sample():
             t0 = time.perf_counter()
@@ -828,7 +834,7 @@ def main():
                     help="match (default, the reported line) or a secondary configuration")
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
     ap.add_argument("--form", default="exact", choices=["exact", "fast"],
-                    help="fleet member-tail arithmetic for --workload fleet (cvm_fleet_set_form)")
+                    help="arithmetic: exact (the reference's bits) or fast (cvm_set_form / cvm_fleet_set_form)")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -102,6 +102,8 @@ def lib():
             L.cvm_fleet_free.restype = None
             L.cvm_fleet_set_roi.argtypes = [vp, i32, i32, i32, i32, i32]
             L.cvm_fleet_set_form.argtypes = [vp, i32]
+            L.cvm_set_form.argtypes = [i32]
+            L.cvm_get_form.argtypes = []
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
             L.cvm_stream_push.argtypes = [vp, u8p, i64]
             L.cvm_stream_pull.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
@@ -287,6 +289,15 @@ def NewGrayMatcher(sub) -> Matcher:
 
 FORM_EXACT = 0
 FORM_FAST = 1
+
+
+def SetForm(form: int) -> int:
+    """Arithmetic of one-shot matches and Matcher.Find, process-wide
+    (cvm_set_form): FORM_EXACT (default, the reference's bits) or
+    FORM_FAST.  Returns the previous form."""
+    prev = lib().cvm_get_form()
+    _check(lib().cvm_set_form(form))
+    return prev
 
 
 class Fleet:

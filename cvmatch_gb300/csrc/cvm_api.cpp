@@ -281,19 +281,19 @@ size_t tspec_elems(const FftClass &f, int cnS) { return (size_t)cnS * f.dftH * f
 // sum(I*T) - sum(I)*sum(T)/area directly.
 int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step, int tw, int th,
                 int cnS, const int *cnDev, float2 *ts0, float2 *ts1, cudaStream_t st,
-                const int64_t *tsum = nullptr) {
+                const int64_t *tsum = nullptr, const unsigned long long *tsumDev = nullptr) {
     TileGeom tg;
     FftClass tf;
     template_geom(G, tw, th, tg, tf);
     float mul = 1.0f, sub[4] = {0.f, 0.f, 0.f, 0.f};
     const double area = double(tw) * double(th);
-    if (tsum) {
-        const bool exact = area * 255.0 < 16777216.0;
-        mul = exact ? float(area) : 1.0f;
+    const bool exact = area * 255.0 < 16777216.0;
+    if (tsum || tsumDev) mul = exact ? float(area) : 1.0f;
+    if (tsum)
         for (int k = 0; k < 4; k++) sub[k] = exact ? float(tsum[k]) : float(double(tsum[k]) / area);
-    }
+    // sums on the device (one-shot calls): sub = tsum / (1 or area)
     CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st, 0, "k_fwd_rows_tpl", mul,
-                             tsum ? sub : nullptr));
+                             tsum ? sub : nullptr, tsumDev, exact ? 1.0f : float(area)));
     const float scale = float(1.0 / (double(G.p.dftW) * double(G.p.dftH) * double(mul)));
     MemberSet none;
     memset(&none, 0, sizeof none);
@@ -303,6 +303,10 @@ int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step
 }
 
 // ---------------------------------------------------------- solo pipeline
+
+// The arithmetic of one-shot matches and Matcher.Find (cvm_set_form).
+std::atomic<int> g_soloForm{CVM_FORM_EXACT};
+int solo_form() { return g_soloForm.load(std::memory_order_relaxed); }
 
 struct TemplateCache;  // a Matcher's per-geometry state
 
@@ -321,6 +325,7 @@ struct SoloJob {
     float *map;
     cvm_result *out;
     int frameOnSide;  // the frame arrives on the second side stream (its frame event)
+    int form;         // CVM_FORM_EXACT or CVM_FORM_FAST (cached spectra must be of this form)
 };
 
 int run_solo(const SoloJob &J, cudaStream_t st) {
@@ -343,8 +348,18 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                    Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
                    Arena::bytes((size_t)rw * rh, sizeof(float2));
+    const bool fast = J.form != CVM_FORM_EXACT;
+    // one channel: the fused forward + conj-multiply + inverse column pass
+    // already yields the single correlation spectrum the fast form sums to
+    const bool fastSum = fast && !(J.mode == 0 && J.cnFixed == 1);
+    if (fast)
+        for (int c = 0; c < G->nclass; c++)
+            if (G->fc[c].log2n < 5 || G->fc[c].log2n > 12 || G->fc[c].log2H < 5 || G->fc[c].log2H > 12)
+                return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: fast form needs transforms of 32..4096 (%dx%d)",
+                            G->fc[c].n, G->fc[c].dftH);
     for (int c = 0; c < G->nclass; c++) {
         bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
+        if (fastSum) bytes += Arena::bytes(spec_elems(G->fc[c], 1), sizeof(float2));
         if (!J.cachedP) bytes += Arena::bytes(tspec_elems(G->fc[c], cnS), sizeof(float2));
     }
     PoolBuf buf;
@@ -356,11 +371,12 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     Partial *parts = A.take<Partial>(nparts);
     unsigned int *H = A.take<unsigned int>(hElems);
     float2 *lanes = A.take<float2>((size_t)rw * rh);
-    float2 *spec[2] = {nullptr, nullptr};
+    float2 *spec[2] = {nullptr, nullptr}, *sum[2] = {nullptr, nullptr};
     const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
     float2 *tsOwn[2] = {nullptr, nullptr};
     for (int c = 0; c < G->nclass; c++) {
         spec[c] = A.take<float2>(spec_elems(G->fc[c], cnS));
+        if (fastSum) sum[c] = A.take<float2>(spec_elems(G->fc[c], 1));
         if (!J.cachedP) {
             tsOwn[c] = A.take<float2>(tspec_elems(G->fc[c], cnS));
             ts[c] = tsOwn[c];
@@ -390,6 +406,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.map = J.map;
     ms.lanes = lanes;
     ms.lanesStride = 0;
+    ms.form = fast ? 1 : 0;
     // The template statistics, the parent's alpha scan and the channel
     // count first (one short launch on st), then three chains: the frame's
     // row transforms (every channel the device chose, one launch) on st;
@@ -409,21 +426,33 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
                               J.mode == 1 ? 4 : J.cnFixed, H, 0, ss.st2));
     CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
     if (!J.cachedP)
-        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st));
+        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st,
+                            nullptr, fast ? P->tsum : nullptr));
     CVM_CUDA(cudaEventRecord(ss.join, ss.st));
+    // the fast form transforms the frame offset by -128 (zero-mean templates)
+    const float off[4] = {128.f, 128.f, 128.f, 128.f};
     for (int c = 0; c < G->nclass; c++)
-        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st));
+        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0, nullptr,
+                                 1.0f, fast ? off : nullptr));
+    if (fastSum) {
+        // forward columns of every channel (in place), then the channel
+        // sum of the conj-products and one inverse per tile
+        MemberSet none;
+        memset(&none, 0, sizeof none);
+        for (int c = 0; c < G->nclass; c++)
+            CVM_CUDA(launch_cols(0, spec[c], spec[c], cnS, G->g, G->fc[c], c, cnS, &P->cn, 1.0f, none, 1, st));
+    }
     CVM_CUDA(cudaStreamWaitEvent(st, ss.join, 0));
     for (int c = 0; c < G->nclass; c++) {
         const FftClass &f = G->fc[c];
-        ms.scratch[c] = spec[c];
+        ms.scratch[c] = fastSum ? sum[c] : spec[c];
         ms.scratchStride[c] = 0;
-        CVM_CUDA(launch_cols(1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
+        CVM_CUDA(launch_cols(fastSum ? 3 : 1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
     }
     CVM_CUDA(cudaStreamWaitEvent(st, ss.joinStats, 0));
     for (int c = 0; c < G->nclass; c++)
-        CVM_CUDA(launch_inv_rows(G->g, G->fc[c], c, cnS, ms, 1, G->g.blockH, partOff[c], nparts, parts, &F->normDone,
-                                 J.out, st));
+        CVM_CUDA(launch_inv_rows(G->g, G->fc[c], c, fast ? 1 : cnS, ms, 1, G->g.blockH, partOff[c], nparts, parts,
+                                 &F->normDone, J.out, st));
     return CVM_OK;
 }
 
@@ -626,6 +655,7 @@ int host_solo(const uint8_t *img, long long istride, int iw, int ih, const uint8
     }
     SoloJob J;
     memset(&J, 0, sizeof J);
+    J.form = solo_form();
     J.img = dImg;
     J.istride = ip;
     J.iw = iw;
@@ -679,6 +709,7 @@ using namespace cvm;
 
 struct MatcherGeom {
     int rw = 0, rh = 0;
+    int form = CVM_FORM_EXACT;  // the arithmetic the spectra were built for
     Geom G;
     float2 *ts[2] = {nullptr, nullptr};
     ~MatcherGeom() {
@@ -706,22 +737,23 @@ namespace {
 
 // The Matcher's cached plan and spectra for one result size, built once
 // under the handle's lock (the double-checked cache of matcher.go:114-126).
-int matcher_geom(cvm_matcher *m, int rw, int rh, std::shared_ptr<MatcherGeom> &out) {
+int matcher_geom(cvm_matcher *m, int rw, int rh, int form, std::shared_ptr<MatcherGeom> &out) {
     std::lock_guard<std::mutex> lk(m->mu);
-    if (m->geom && m->geom->rw == rw && m->geom->rh == rh) {
+    if (m->geom && m->geom->rw == rw && m->geom->rh == rh && m->geom->form == form) {
         out = m->geom;
         return CVM_OK;
     }
     auto g = std::make_shared<MatcherGeom>();
     g->rw = rw;
     g->rh = rh;
+    g->form = form;
     CVM_TRY(make_geom(m->w, m->h, rw, rh, m->h, g->G));
     const int cnS = m->step;  // colour: all four channels (cn is decided per frame)
     for (int c = 0; c < g->G.nclass; c++)
         CVM_CUDA(cudaMalloc(&g->ts[c], tspec_elems(g->G.fc[c], cnS) * sizeof(float2)));
     cudaStream_t st = thread_stream();
     CVM_TRY(build_tspec(g->G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, cnS, nullptr, g->ts[0],
-                        g->ts[1], st));
+                        g->ts[1], st, form != CVM_FORM_EXACT ? m->tsum : nullptr));
     CVM_CUDA(cudaStreamSynchronize(st));
     m->geom = g;
     out = g;
@@ -739,10 +771,12 @@ int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, 
         return CVM_OK;
     }
     const int rw = pw - m->w + 1, rh = ph - m->h + 1;
+    const int form = solo_form();
     std::shared_ptr<MatcherGeom> g;
-    CVM_TRY(matcher_geom(m, rw, rh, g));
+    CVM_TRY(matcher_geom(m, rw, rh, form, g));
     SoloJob J;
     memset(&J, 0, sizeof J);
+    J.form = form;
     J.img = dParent;
     J.istride = pstride;
     J.iw = pw;
@@ -1252,6 +1286,7 @@ int cvm_match_u8_device(const uint8_t *d_img, int64_t istride, int iw, int ih, c
     CVM_TRY(ensure_device());
     SoloJob J;
     memset(&J, 0, sizeof J);
+    J.form = solo_form();
     J.img = d_img;
     J.istride = istride;
     J.iw = iw;
@@ -1276,6 +1311,7 @@ int cvm_match_device(const uint8_t *d_parent, int64_t pstride, int pw, int ph, c
     CVM_TRY(ensure_device());
     SoloJob J;
     memset(&J, 0, sizeof J);
+    J.form = solo_form();
     J.img = d_parent;
     J.istride = pstride;
     J.iw = pw;
@@ -1458,6 +1494,15 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 }
 
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_set_form(int form) {
+    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: unknown form %d", form);
+    g_soloForm.store(form, std::memory_order_relaxed);
+    return CVM_OK;
+}
+
+int cvm_get_form(void) { return solo_form(); }
 
 int cvm_fleet_set_form(cvm_fleet *f, int form) {
     if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");

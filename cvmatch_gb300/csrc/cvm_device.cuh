@@ -87,6 +87,10 @@ struct FwdRowsArgs {
     // stays zero
     float mul;
     float sub[4];
+    // when set, sub[k] = subSums[k] / subDiv instead (template sums the
+    // device computed; float, exact when subDiv == 1)
+    const unsigned long long *subSums;
+    float subDiv;
 };
 
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).

@@ -141,7 +141,8 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
                             int cnS, cudaStream_t st, int chanFirst = 0, const char *label = nullptr,
-                            float mul = 1.0f, const float *sub = nullptr);
+                            float mul = 1.0f, const float *sub = nullptr,
+                            const unsigned long long *subSums = nullptr, float subDiv = 1.0f);
 // Column pass.  mode 0: forward only, natural output (template spectra with
 // `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
 // conj-multiply + inverse, in place on the members' scratch (solo match);

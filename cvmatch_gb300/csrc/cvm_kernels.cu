@@ -1632,7 +1632,13 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             sq += (unsigned long long)s[CN > 3 ? 3 : 0] * s[CN > 3 ? 3 : 0];
         }
         // the spill lanes (impl.go:902-1009) and normOne's corr-free part
-        const float id = f32_via_f64((long long)(area * q - sq));
+        // FAST: the exact variance numerator from its two 32-bit halves
+        // (within 1.5 ulp; the reference's two-step float64 -> float32
+        // conversion is kept otherwise)
+        const unsigned long long idv = area * q - sq;
+        const float id = FAST ? fmaf(__uint2float_rn((unsigned int)(idv >> 32)), 4294967296.0f,
+                                     __uint2float_rn((unsigned int)idv))
+                              : f32_via_f64((long long)idv);
         const float diff2 = __fmul_rn(id, Pm.varScale);
         float lim = 0.5f;
         if (q < (1ull << 24)) {
@@ -1788,7 +1794,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
                             int cnS, cudaStream_t st, int chanFirst, const char *label, float mul,
-                            const float *sub) {
+                            const float *sub, const unsigned long long *subSums, float subDiv) {
     // Channels per launch so that one row pair of the group fits 128 KB of
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
@@ -1825,6 +1831,8 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         a.pix32 = step == 4 && (reinterpret_cast<uintptr_t>(img) & 3) == 0 && (istride & 3) == 0;
         a.mul = mul;
         for (int k = 0; k < 4; k++) a.sub[k] = sub ? sub[k] : 0.0f;
+        a.subSums = subSums;
+        a.subDiv = subDiv;
         for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
             a.chanFirst = c0;
             launch_fwd_rows_fixed(a, grid, threads, smem, st);
@@ -1832,7 +1840,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         }
         return cudaGetLastError();
     }
-    if (mul != 1.0f || sub) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
+    if (mul != 1.0f || sub || subSums) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
     set_smem(k_fwd_rows, smem);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
         k_fwd_rows<<<grid, threads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,
@@ -2081,6 +2089,15 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
                 k_vstats<3, 4, true, true><<<gv, kThreads, 0, st>>>(v);
             else
                 k_vstats<4, 4, true, true><<<gv, kThreads, 0, st>>>(v);
+        } else if (ms.form) {
+            if (cnMax == 1)
+                k_vstats<1, 1, false, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMax == 2)
+                k_vstats<2, 2, false, true><<<gv, kThreads, 0, st>>>(v);
+            else if (cnMin == 3)
+                k_vstats<3, 4, false, true><<<gv, kThreads, 0, st>>>(v);
+            else
+                k_vstats<4, 4, false, true><<<gv, kThreads, 0, st>>>(v);
         } else if (sharedPrefix) {
             if (cnMax == 1)
                 k_vstats<1, 1, true><<<gv, kThreads, 0, st>>>(v);

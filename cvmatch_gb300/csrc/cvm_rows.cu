@@ -165,6 +165,9 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long istride = a.istride;
     const uint8_t *img0 = a.img + (long long)(b.y0 + 2 * pair0) * istride + (long long)b.x0 * a.step;
+    float subv[4];
+#pragma unroll
+    for (int g = 0; g < 4; g++) subv[g] = a.subSums ? __fdiv_rn(__ull2float_rn(a.subSums[g]), a.subDiv) : a.sub[g];
     // Pack rows r (real part) and r+1 (imaginary part) of every channel of
     // the group, each pixel read once for all of them.
     for (int it = tid; it < (P << LOG2N); it += nt) {
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
             // row of an odd tail stays zero
 #pragma unroll
             for (int g = 0; g < 4; g++) {
-                const float sg = a.sub[(a.chanFirst + g) & 3];
+                const float sg = subv[(a.chanFirst + g) & 3];
                 va[g] = __fsub_rn(__fmul_rn(va[g], a.mul), sg);
                 vb[g] = two ? __fsub_rn(__fmul_rn(vb[g], a.mul), sg) : 0.f;
             }

@@ -214,6 +214,19 @@ int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h);
 enum { CVM_FORM_EXACT = 0, CVM_FORM_FAST = 1 };
 int cvm_fleet_set_form(cvm_fleet *f, int form);
 
+/* The same choice for one-shot matches (cvm_match, cvm_match_map,
+ * cvm_match_gray*, cvm_match_u8*, cvm_match_device and the peaks entry
+ * points) and Matcher.Find, process-wide, read at the start of each call
+ * (a Matcher rebuilds its cached spectra when the form changed).  In the
+ * fast form each tile's channels are transformed forward, their
+ * conj-products summed, and one inverse taken; the score map is the fast
+ * form's.  The reference has no such switch (its Threads variable,
+ * cvmatch.go:42, is the nearest process-wide knob); the default stays
+ * CVM_FORM_EXACT.  cvm_match_u8_device_noalloc always computes the exact
+ * form. */
+int cvm_set_form(int form);
+int cvm_get_form(void);
+
 /* ------------------------------------------------------- frame streams */
 
 /* A stream of RGBA frames of one size matched against a colour fleet and,

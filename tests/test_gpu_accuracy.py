@@ -29,24 +29,34 @@ def _report(name, m32, m64):
     return err.max(), gi, ri, top[1] - top[0]
 
 
-def test_c1_gray_vs_fp64():
+FORMS = {"exact": cvm.FORM_EXACT, "fast": cvm.FORM_FAST}
+
+
+@pytest.fixture(params=["exact", "fast"])
+def form(request):
+    prev = cvm.SetForm(FORMS[request.param])
+    yield request.param
+    cvm.SetForm(prev)
+
+
+def test_c1_gray_vs_fp64(form):
     import bench
     rgba, tpl, _ = bench.scene_c1()
     g, t = cvm.rgba_to_gray(rgba), cvm.rgba_to_gray(tpl)
     _, m = cvm.match_u8(g, t, 1)
     m64 = oracle.ref_match_f64(g, t, 1, threads=16)
-    e, gi, ri, margin = _report("C1 MatchGray 640x480 / 64x48", m, m64)
+    e, gi, ri, margin = _report(f"C1 MatchGray 640x480 / 64x48 ({form})", m, m64)
     assert e <= TOL_REF_DRIFT
     if margin > 1e-4:
         assert gi == ri
 
 
-def test_c2_rgba_vs_fp64():
+def test_c2_rgba_vs_fp64(form):
     import bench
     frame, tpl, _ = bench.scene_c2()
     m, _, _ = cvm.MatchMap(frame, tpl)
     m64 = oracle.ref_match_f64(frame, tpl, 3, threads=16)
-    e, gi, ri, margin = _report("C2 Match RGBA 1920x1080 / 96x32", m, m64)
+    e, gi, ri, margin = _report(f"C2 Match RGBA 1920x1080 / 96x32 ({form})", m, m64)
     assert e <= TOL_REF_DRIFT
     if margin > 1e-4:
         assert gi == ri

@@ -134,3 +134,72 @@ def test_form_switch_restores_bit_exact_results():
     assert any(tuple(f) != tuple(e) for f, e in zip(fast, exact))  # the fast form is a different arithmetic
     with pytest.raises(cvm.CvmatchError):
         fleet.SetForm(7)
+
+
+# ------------------------------------------------- one-shot matches, Matcher
+
+
+@pytest.fixture
+def fast_form():
+    prev = cvm.SetForm(cvm.FORM_FAST)
+    yield
+    cvm.SetForm(prev)
+
+
+def map_check(m, m64, name, tol=TOL):
+    err = np.abs(m.astype(np.float64) - m64)
+    print(f"\n{name}: map max|err| {err.max():.2e}  >1e-4: {int((err > 1e-4).sum())} of {err.size}")
+    assert err.max() <= tol
+    return err.max()
+
+
+def test_fast_match_map_vs_fp64(fast_form):
+    img = scene(23, 260, 400)
+    t = img[100:140, 150:214].copy()
+    m, _, _ = cvm.MatchMap(img, t)
+    map_check(m, oracle.ref_match_f64(img, t, 3, threads=16), "MatchMap RGBA")
+    # Match returns the map's first-occurrence extrema
+    r = tuple(cvm.Match(img, t))
+    iy, ix = np.unravel_index(int(np.argmin(m)), m.shape)
+    jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
+    assert r == (float(m[iy, ix]), ix, iy, float(m[jy, jx]), jx, jy)
+    assert (r[4], r[5]) == (150, 100)
+    # MatchGray
+    g, gt = oracle.rgba_to_gray(img), oracle.rgba_to_gray(t)
+    _, mg = cvm.match_u8(g, gt, 1)
+    map_check(mg, oracle.ref_match_f64(g, gt, 1, threads=16), "gray")
+
+
+def test_fast_varying_alpha_map(fast_form):
+    img = scene(29, 200, 300)
+    img[..., 3] = np.arange(300, dtype=np.uint8)[None, :]  # parent alpha varies: cn = 4
+    t = img[60:90, 80:120].copy()
+    m, _, _ = cvm.MatchMap(img, t)
+    map_check(m, oracle.ref_match_f64(img, t, 4, threads=16), "MatchMap RGBA, varying alpha")
+    jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
+    assert (jx, jy) == (80, 60)
+
+
+def test_fast_matcher_equals_one_shot(fast_form):
+    img = scene(31, 240, 360)
+    t = img[30:62, 40:88].copy()
+    m = cvm.NewMatcher(t)
+    a, b = m.Find(img), cvm.Match(img, t)
+    assert tuple(a) == tuple(b)  # same zero-mean spectra from host or device sums
+    cvm.SetForm(cvm.FORM_EXACT)  # the matcher rebuilds its spectra for the exact form
+    assert tuple(m.Find(img)) == oracle.match_u8(img, t, 3, want_map=False)[0]
+
+
+def test_fast_flat_template_and_exact_default():
+    assert cvm.SetForm(cvm.FORM_FAST) == cvm.FORM_EXACT
+    try:
+        img = scene(37, 120, 160)
+        flat = np.full((20, 30, 4), 50, np.uint8)
+        flat[..., 3] = 255
+        assert tuple(cvm.Match(img, flat)) == (1.0, 0, 0, 1.0, 0, 0)  # impl.go:1137-1144
+        m, _, _ = cvm.MatchMap(img, flat)
+        assert (m == 1.0).all()
+    finally:
+        cvm.SetForm(cvm.FORM_EXACT)
+    with pytest.raises(cvm.CvmatchError):
+        cvm.SetForm(5)
