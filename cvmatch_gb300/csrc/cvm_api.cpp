@@ -434,20 +434,26 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     for (int c = 0; c < G->nclass; c++)
         CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0, nullptr,
                                  1.0f, fast ? off : nullptr));
-    if (fastSum) {
-        // forward columns of every channel (in place), then the channel
-        // sum of the conj-products and one inverse per tile
-        MemberSet none;
-        memset(&none, 0, sizeof none);
-        for (int c = 0; c < G->nclass; c++)
+    // Several channels, fast form: transforms up to 512 tall run every
+    // channel of a column strip in one CTA (mode 4: forward, channel sum of
+    // the conj-products, one inverse); taller ones store the forward
+    // column spectra of every channel (in place) and sum them in a second
+    // pass (mode 3).
+    int colMode[2] = {1, 1};
+    for (int c = 0; c < G->nclass; c++)
+        if (fastSum) colMode[c] = G->fc[c].log2H <= 9 ? 4 : 3;
+    for (int c = 0; c < G->nclass; c++)
+        if (colMode[c] == 3) {
+            MemberSet none;
+            memset(&none, 0, sizeof none);
             CVM_CUDA(launch_cols(0, spec[c], spec[c], cnS, G->g, G->fc[c], c, cnS, &P->cn, 1.0f, none, 1, st));
-    }
+        }
     CVM_CUDA(cudaStreamWaitEvent(st, ss.join, 0));
     for (int c = 0; c < G->nclass; c++) {
         const FftClass &f = G->fc[c];
         ms.scratch[c] = fastSum ? sum[c] : spec[c];
         ms.scratchStride[c] = 0;
-        CVM_CUDA(launch_cols(fastSum ? 3 : 1, spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
+        CVM_CUDA(launch_cols(colMode[c], spec[c], spec[c], cnS, G->g, f, c, cnS, nullptr, 1.0f, ms, 1, st));
     }
     CVM_CUDA(cudaStreamWaitEvent(st, ss.joinStats, 0));
     for (int c = 0; c < G->nclass; c++)

@@ -238,38 +238,79 @@ __device__ __forceinline__ void col_passes(const IO &io, const float2 *__restric
     }
 }
 
-// The middle sweep (see the file header).  x[c'] is row B + S*c' of the
-// forward's natural-order output; FWD runs the forward's last pass on it.
+// The middle sweep (see the file header): the geometry of its units.
+template <int L>
+struct Mid {
+    static constexpr int N = 1 << L, PL = npass(L) - 1;
+    static constexpr int KL = pass_kind(L, PL), HL = pass_h(L, PL);
+    static constexpr int M = ((L & 1) && KL == K4) ? 8 : 16, S = N / M;
+};
+
+// The forward cascade's last pass on x[c'] = row B + S*c' of its
+// natural-order output.
+template <int L>
+__device__ __forceinline__ void fwd_last_pass(float2 *x, int B, const float2 *__restrict__ tri) {
+    using G = Mid<L>;
+    constexpr int HL = G::HL, S = G::S;
+    if constexpr (G::KL == K16) {
+        // one radix-16 unit at quarter S = HL, butterfly index B
+        math16<false, HL>(x, tri + tw_off(L, HL) + B);
+    } else if constexpr (G::M == 16) {
+        // even L, radix-4 at HL = 4S: units j = B + S*q on x[q + 4i]
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float2 *t = tri + tw_off(L, HL) + B + S * q;
+            bfly4<false>(&x[q], &x[q + 4], &x[q + 8], &x[q + 12], __ldg(t), __ldg(t + HL), __ldg(t + 2 * HL));
+        }
+    } else {
+        // odd L, radix-4 at HL = 2S: units j = B, B + S on x[2i], x[2i+1]
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const float2 *t = tri + tw_off(L, HL) + B + S * q;
+            bfly4<false>(&x[q], &x[q + 2], &x[q + 4], &x[q + 6], __ldg(t), __ldg(t + HL), __ldg(t + 2 * HL));
+        }
+    }
+}
+
+// The inverse cascade's first pass on the same rows, stored through sp
+// (row B + S*c' at sp[(S*c') << LSC]).
+template <int L, int LSC>
+__device__ __forceinline__ void inv_first_pass(float2 *x, float2 *sp, const float2 *__restrict__ tri) {
+    using G = Mid<L>;
+    constexpr int M = G::M, S = G::S;
+    if constexpr (L & 1) {
+        // inverse head(s): logical 8a+t <-> row B' + (N/8)*brev3(t)
+#pragma unroll
+        for (int hd = 0; hd < M / 8; hd++) {
+            float2 e[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++) e[t] = x[(M / 8) * brevk(t, 3) + hd];
+            math_head<true>(e, tri);
+#pragma unroll
+            for (int t = 0; t < 8; t++) sp[(S * ((M / 8) * brevk(t, 3) + hd)) << LSC] = e[t];
+        }
+    } else {
+        // inverse radix-16 at quarter 1: logical 16a+r <-> row B + S*brev4(r)
+        float2 e[16];
+#pragma unroll
+        for (int r = 0; r < 16; r++) e[r] = x[brevk(r, 4)];
+        math16<true, 1>(e, tri);
+#pragma unroll
+        for (int r = 0; r < 16; r++) sp[(S * brevk(r, 4)) << LSC] = e[r];
+    }
+}
+
+// The middle sweep.  x[c'] is row B + S*c' of the forward's natural-order
+// output; FWD runs the forward's last pass on it.
 template <bool FWD, int L, int LSC, typename LDX, bool MUL = true>
 __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const float2 *__restrict__ ts, int hwp,
                                              int wv, const float2 *__restrict__ tri) {
-    constexpr int N = 1 << L, PL = npass(L) - 1;
-    constexpr int KL = pass_kind(L, PL), HL = pass_h(L, PL);
-    constexpr int M = ((L & 1) && KL == K4) ? 8 : 16, S = N / M, SC = 1 << LSC;
+    constexpr int M = Mid<L>::M, S = Mid<L>::S, SC = 1 << LSC;
     for (int u = threadIdx.x; u < (S << LSC); u += blockDim.x) {
         const int c = u & (SC - 1), B = u >> LSC;
         float2 x[M];
         ldx(x, c, B);
-        if constexpr (FWD) {
-            if constexpr (KL == K16) {
-                // one radix-16 unit at quarter S = HL, butterfly index B
-                math16<false, HL>(x, tri + tw_off(L, HL) + B);
-            } else if constexpr (M == 16) {
-                // even L, radix-4 at HL = 4S: units j = B + S*q on x[q + 4i]
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float2 *t = tri + tw_off(L, HL) + B + S * q;
-                    bfly4<false>(&x[q], &x[q + 4], &x[q + 8], &x[q + 12], __ldg(t), __ldg(t + HL), __ldg(t + 2 * HL));
-                }
-            } else {
-                // odd L, radix-4 at HL = 2S: units j = B, B + S on x[2i], x[2i+1]
-#pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    const float2 *t = tri + tw_off(L, HL) + B + S * q;
-                    bfly4<false>(&x[q], &x[q + 2], &x[q + 4], &x[q + 6], __ldg(t), __ldg(t + HL), __ldg(t + 2 * HL));
-                }
-            }
-        }
+        if constexpr (FWD) fwd_last_pass<L>(x, B, tri);
         if constexpr (MUL) {
             // spec *= conj(tspec) (mulConjGo, impl.go:376-388)
             const float2 *tp = ts + (size_t)B * hwp + c;
@@ -277,29 +318,131 @@ __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const
             for (int ci = 0; ci < M; ci++)
                 x[ci] = mul_conj(x[ci], c < wv ? __ldg(tp + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f));
         }
-        float2 *sp = smem + (B << LSC) + c;
-        if constexpr (L & 1) {
-            // inverse head(s): logical 8a+t <-> row B' + (N/8)*brev3(t)
-#pragma unroll
-            for (int hd = 0; hd < M / 8; hd++) {
-                float2 e[8];
-#pragma unroll
-                for (int t = 0; t < 8; t++) e[t] = x[(M / 8) * brevk(t, 3) + hd];
-                math_head<true>(e, tri);
-#pragma unroll
-                for (int t = 0; t < 8; t++) sp[(S * ((M / 8) * brevk(t, 3) + hd)) << LSC] = e[t];
-            }
-        } else {
-            // inverse radix-16 at quarter 1: logical 16a+r <-> row B + S*brev4(r)
-            float2 e[16];
-#pragma unroll
-            for (int r = 0; r < 16; r++) e[r] = x[brevk(r, 4)];
-            math16<true, 1>(e, tri);
-#pragma unroll
-            for (int r = 0; r < 16; r++) sp[(S * brevk(r, 4)) << LSC] = e[r];
-        }
+        inv_first_pass<L, LSC>(x, smem + (B << LSC) + c, tri);
     }
     __syncthreads();
+}
+
+// ------------------------------------------------ mode 4: fused channels
+// The fast form of one colour match: every channel of a column strip in
+// one CTA (channel k's [N x SC] strip at smem + k*(N << LSC)).  The
+// forward passes run over all channels together, then a sweep sums each
+// channel's conj-products with the zero-mean template spectra (fused
+// multiply-adds) and runs the inverse's first pass once into channel 0's
+// strip, then the inverse passes of that one strip.  The frame's column
+// spectra never leave shared memory.
+
+// Strip width of mode 4: 2048 / N columns (a channel strip is 16 KB).
+__host__ __device__ constexpr int sc4(int L) { return (1 << L) >= 2048 ? 1 : 2048 >> L; }
+
+template <int L, int LSC>
+struct SmemNatCh {  // channel k, row r at s[k * (N << LSC) + (r << LSC) + c]
+    float2 *s;
+    template <int R, int STEP>
+    __device__ __forceinline__ void load(float2 *e, int k, int c, int base) const {
+        SmemNat<LSC>{s + ((size_t)k << (L + LSC))}.template load<R, STEP>(e, c, base);
+    }
+    template <int R, int STEP>
+    __device__ __forceinline__ void store(const float2 *e, int k, int c, int base) const {
+        SmemNat<LSC>{s + ((size_t)k << (L + LSC))}.template store<R, STEP>(e, c, base);
+    }
+};
+
+template <int L>
+struct GlobalSlotsCh {  // forward-rows output of channel k (see GlobalSlots)
+    const float2 *src;
+    size_t chanStride;
+    int hwp, wv, loaded;
+    template <int R, int STEP>
+    __device__ __forceinline__ void load(float2 *e, int k, int c, int base) const {
+        GlobalSlots<L>{src + (size_t)k * chanStride, hwp, wv, loaded}.template load<R, STEP>(e, c, base);
+    }
+};
+
+// One forward pass p over channels [0, cn) of the strip.  Ends with a barrier.
+template <int L, int P, int LSC, typename LDF, typename STF>
+__device__ __forceinline__ void col_pass_ch(int cn, const LDF &ldf, const STF &stf, const float2 *__restrict__ tri) {
+    constexpr int N = 1 << L, K = pass_kind(L, P), H = pass_h(L, P);
+    constexpr int R = K == KHEAD ? 8 : (K == K16 ? 16 : 4), LR = ilog2k(R), LH = ilog2k(H);
+    constexpr int SC = 1 << LSC, LNU = L - LR + LSC;
+    for (int u = threadIdx.x; u < (cn << LNU); u += blockDim.x) {
+        const int k = u >> LNU, w = u & ((1 << LNU) - 1);
+        const int c = w & (SC - 1), v = w >> LSC;
+        const int j = v & (H - 1), base = ((v >> LH) << (LH + LR)) + j;
+        float2 e[R];
+        ldf.template load<R, H>(e, k, c, base);
+        if constexpr (K == KHEAD)
+            math_head<false>(e, tri);
+        else if constexpr (K == K16)
+            math16<false, H>(e, tri + tw_off(L, H) + j);
+        else
+            math4<false, H>(e, tri + tw_off(L, H) + j);
+        stf.template store<R, H>(e, k, c, base);
+    }
+    __syncthreads();
+}
+
+template <int L, int P, int PEND, int LSC>
+__device__ __forceinline__ void col_passes_ch(int cn, const SmemNatCh<L, LSC> &io, const float2 *__restrict__ tri) {
+    if constexpr (P < PEND) {
+        col_pass_ch<L, P, LSC>(cn, io, io, tri);
+        col_passes_ch<L, P + 1, PEND, LSC>(cn, io, tri);
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(256, 2) k_cols_sum_t(ColsArgs a) {
+    constexpr int N = 1 << L, NP = npass(L), SC = sc4(L), LSC = ilog2k(SC);
+    constexpr int M = Mid<L>::M, S = Mid<L>::S;
+    extern __shared__ float2 smem[];
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.z;
+    const int tile = fc.tileFirst + tileLocal;
+    const DevMember &m = a.ms.solo;
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    if (Pm.flat) return;
+    const int cn = Pm.cn;
+    const TileBox b = tile_box(a.g, tile);
+    const int c0 = blockIdx.x * SC;
+    const int hwp = fc.hwp;
+    const int wv = min(SC, fc.hw - c0);
+    const size_t chanStride = (size_t)N * hwp;
+    const float2 *tri = fc.triH;
+    const GlobalSlotsCh<L> gs{a.in + (size_t)tileLocal * a.cnS * chanStride + c0, chanStride, hwp, wv,
+                              min(N, (b.loadH + 1) & ~1)};
+    const SmemNatCh<L, LSC> sn{smem};
+    // every forward pass in shared memory (the last one too: keeping it in
+    // the sum sweep's registers beside the accumulator spills)
+    col_pass_ch<L, 0, LSC>(cn, gs, sn, tri);
+    col_passes_ch<L, 1, NP, LSC>(cn, sn, tri);
+    const float2 *ts = m.tspec[a.cls] + c0;
+    for (int u = threadIdx.x; u < (S << LSC); u += blockDim.x) {
+        const int c = u & (SC - 1), B = u >> LSC;
+        float2 acc[M];
+#pragma unroll
+        for (int ci = 0; ci < M; ci++) acc[ci] = make_float2(0.f, 0.f);
+        for (int k = 0; k < cn; k++) {
+            const float2 *p = smem + ((size_t)k << (L + LSC)) + (B << LSC) + c;
+            float2 x[M];
+#pragma unroll
+            for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
+            const float2 *tp = ts + (size_t)k * chanStride + (size_t)B * hwp + c;
+#pragma unroll
+            for (int ci = 0; ci < M; ci++) {
+                const float2 t = c < wv ? __ldg(tp + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f);
+                acc[ci].x = fmaf(x[ci].x, t.x, fmaf(x[ci].y, t.y, acc[ci].x));
+                acc[ci].y = fmaf(x[ci].y, t.x, fmaf(-x[ci].x, t.y, acc[ci].y));
+            }
+        }
+        inv_first_pass<L, LSC>(acc, smem + (B << LSC) + c, tri);
+    }
+    __syncthreads();
+    const int ty = tile / a.g.ntx;
+    const int bh = (ty == a.g.nty - 1) ? m.rh - b.y0 : a.g.blockH;
+    const SmemRev<L, LSC> sr{smem};
+    const GlobalInv<L> gi{a.ms.scratch[a.cls] + (size_t)tileLocal * chanStride + c0, hwp, wv, min(N, (bh + 1) & ~1)};
+    col_passes<true, L, 1, NP - 1, LSC>(sr, tri);
+    col_pass<true, L, NP - 1, LSC>(sr, gi, tri);
 }
 
 template <int MODE, int L>
@@ -409,6 +552,12 @@ void cols_one(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     k_cols_t<MODE, L><<<grid, kThreads, smem, st>>>(a);
 }
 
+template <int L>
+void cols_sum_one(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
+    set_smem(k_cols_sum_t<L>, smem);
+    k_cols_sum_t<L><<<grid, kThreads, smem, st>>>(a);
+}
+
 template <int MODE>
 void cols_mode(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     switch (a.fc.log2H) {
@@ -426,6 +575,21 @@ void cols_mode(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
 }  // namespace
 
 bool cols_fixed_length(int log2H) { return log2H >= 5 && log2H <= 12; }
+
+int cols_sum_width(int log2H) { return sc4(log2H); }
+
+void launch_cols_sum(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
+    switch (a.fc.log2H) {
+        case 5: cols_sum_one<5>(a, grid, smem, st); break;
+        case 6: cols_sum_one<6>(a, grid, smem, st); break;
+        case 7: cols_sum_one<7>(a, grid, smem, st); break;
+        case 8: cols_sum_one<8>(a, grid, smem, st); break;
+        case 9: cols_sum_one<9>(a, grid, smem, st); break;
+        case 10: cols_sum_one<10>(a, grid, smem, st); break;
+        case 11: cols_sum_one<11>(a, grid, smem, st); break;
+        default: cols_sum_one<12>(a, grid, smem, st); break;
+    }
+}
 
 void launch_cols_fixed(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     if (a.mode == 0)

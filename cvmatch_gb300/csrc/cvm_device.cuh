@@ -100,6 +100,10 @@ void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_
 // The column kernels specialised on dftH = 2^5 .. 2^12 (cvm_cols.cu).
 bool cols_fixed_length(int log2H);
 void launch_cols_fixed(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st);
+// Mode 4 (a colour match's fast form, fused channels): strip width for a
+// height, and the launch (grid: strips x 1 x tiles).
+int cols_sum_width(int log2H);
+void launch_cols_sum(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st);
 
 namespace {
 

@@ -1879,9 +1879,21 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     const size_t smem = (size_t)fc.dftH * SC * sizeof(float2);
     ProfScope ps(label ? label
                        : (mode == 0 ? "k_cols_fwd"
-                                    : (mode == 1 ? "k_cols_fwd_mul_inv" : (mode == 2 ? "k_cols_mul_inv" : "k_cols_sum_inv"))),
+                                    : (mode == 1 ? "k_cols_fwd_mul_inv"
+                                                 : (mode == 2 ? "k_cols_mul_inv"
+                                                              : (mode == 3 ? "k_cols_sum_inv" : "k_cols_fwd_sum_inv")))),
                  st);
     if (mode == 3 && !cols_fixed_length(fc.log2H)) return cudaErrorInvalidValue;  // fast form: fixed heights only
+    if (mode == 4) {
+        // every channel of a strip in one CTA (cnS strips of dftH x SC)
+        if (!cols_fixed_length(fc.log2H) || nmembers != 1 || ms.table) return cudaErrorInvalidValue;
+        a.SC = cols_sum_width(fc.log2H);
+        a.logSC = ilog2i(a.SC);
+        const dim3 g4((fc.hw + a.SC - 1) / a.SC, 1, fc.ntiles);
+        launch_cols_sum(a, g4, (size_t)cnS * fc.dftH * a.SC * sizeof(float2), st);
+        count_launches(1);
+        return cudaGetLastError();
+    }
     if (cols_fixed_length(fc.log2H)) {
         launch_cols_fixed(a, grid, smem, st);
     } else if ((fc.log2H & 1) == 0 && fc.dftH >= 4) {
