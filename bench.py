@@ -406,63 +406,81 @@ def run_gpu(args):
             L.cvm_last_error(buf, 512)
             raise RuntimeError(buf.value.decode())
 
-    for _ in range(max(3, args.warmup)):
-        step_dev()
-    torch.cuda.synchronize()
-    l0 = L.cvm_launch_count()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            step_dev()
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-    launches = (L.cvm_launch_count() - l0) // args.steps
-    ms = slowest_rank_ms(float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)])), ws, dev)
-    value = replica_throughput(MPX, ms, ws)
-
-    # e2e through the host-buffer entry point, pinned host frame
     hp = L.cvm_host_alloc(frame.nbytes)
     hframe = np.ctypeslib.as_array((C.c_uint8 * frame.nbytes).from_address(hp)).reshape(frame.shape)
     hframe[:] = frame
     res = cvm._CResult()
-    for _ in range(3):
-        L.cvm_match(hp, frame.strides[0], 1920, 1080, tpl.ctypes.data, tpl.strides[0], 96, 32, C.byref(res))
-    e2e_t = []
-    for i in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        rc = L.cvm_match(hp, frame.strides[0], 1920, 1080, tpl.ctypes.data, tpl.strides[0], 96, 32, C.byref(res))
-        e2e_t.append(time.perf_counter() - t0)
-        assert rc == 0
-    L.cvm_host_free(hp)
-    e2e_ms = slowest_rank_ms(1e3 * float(np.mean(e2e_t)), ws, dev)
 
-    line = None
-    if rank == 0:
+    def measure(form):
+        """Device-resident ms per step (CUDA events, L2 flushed), the e2e ms
+        through cvm_match with the pinned host frame, launches per step and
+        the clock record, in one arithmetic form."""
+        cvm.SetForm(FORM[form])
+        for _ in range(max(3, args.warmup)):
+            step_dev()
+        torch.cuda.synchronize()
+        l0 = L.cvm_launch_count()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for i in range(args.steps):
+                flush.zero_()
+                starts[i].record(stream)
+                step_dev()
+                ends[i].record(stream)
+            torch.cuda.synchronize()
+        launches = (L.cvm_launch_count() - l0) // args.steps
+        ms = slowest_rank_ms(float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)])), ws, dev)
+        # e2e through the host-buffer entry point, pinned host frame
+        for _ in range(3):
+            L.cvm_match(hp, frame.strides[0], 1920, 1080, tpl.ctypes.data, tpl.strides[0], 96, 32, C.byref(res))
+        e2e_t = []
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = L.cvm_match(hp, frame.strides[0], 1920, 1080, tpl.ctypes.data, tpl.strides[0], 96, 32, C.byref(res))
+            e2e_t.append(time.perf_counter() - t0)
+            assert rc == 0
+        e2e_ms = slowest_rank_ms(1e3 * float(np.mean(e2e_t)), ws, dev)
         out = d_out.cpu().numpy()
         got = (float(out[:1].view(np.float32)[0]), int(out[1]), int(out[2]),
                float(out[3:4].view(np.float32)[0]), int(out[4]), int(out[5]))
-        assert got == res.tuple(), (got, res.tuple())
+        assert got == res.tuple(), (got, res.tuple())  # device-resident and host-buffer calls agree
+        return ms, e2e_ms, launches, clk, got
+
+    # the reported form first, then the other one; the roofline pass below
+    # runs the reported form again
+    other = "fast" if args.form == "exact" else "exact"
+    ms, e2e_ms, launches, clk, got = measure(args.form)
+    o_ms, o_e2e, _, _, _ = measure(other)
+    cvm.SetForm(FORM[args.form])
+    value = replica_throughput(MPX, ms, ws)
+    L.cvm_host_free(hp)
+
+    line = None
+    if rank == 0:
         peak, peak_kind = measured_peaks()
-        roof = roofline(L, step_dev, torch, stream, peak, peak_kind)
+        roof = roofline(L, step_dev, torch, stream, peak, peak_kind, args.form)
         if args.timeline:
             for nm, a, b in timeline(L, step_dev, torch):
                 sys.stderr.write(f"timeline {nm:24s} {a:8.1f} {b:8.1f} us\n")
         line = {"metric": "template*Mpx/s", "value": value, "unit": "template*Mpx/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single", form=args.form),
+                "config": dict(WORKLOAD, parallelism="replicas" if ws > 1 else "single"), "form": args.form,
                 "e2e": {"value": replica_throughput(MPX, e2e_ms, ws), "unit": "template*Mpx/s",
                         "h2d_bytes_per_step": int(frame.nbytes + tpl.nbytes), "d2h_bytes_per_step": 24},
                 "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
-                "result": list(got)}
+                "result": list(got),
+                # the same workload in the other arithmetic form, measured in this run
+                "forms": {other: {"value": replica_throughput(MPX, o_ms, ws), "ms_per_step": o_ms,
+                                  "e2e": replica_throughput(MPX, o_e2e, ws), "e2e_ms_per_step": o_e2e},
+                          args.form: {"value": value, "ms_per_step": ms,
+                                      "e2e": replica_throughput(MPX, e2e_ms, ws), "e2e_ms_per_step": e2e_ms}}}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample(frame, tpl)
         print(json.dumps(line))
@@ -486,11 +504,14 @@ def fft_flops(n):
     return f
 
 
-def c2_models(L):
+def c2_models(L, form="exact"):
     """Algorithmic bytes and flops per launch of each kernel on the
     benchmark workload (cn = 3 after the alpha scan; RGBA input): the HBM
     bytes each kernel must read and write by design (frame, spectra,
-    window sums, per-result lanes) and the radix-4 engine's flops."""
+    window sums, per-result lanes) and the radix-4 engine's flops.  The
+    fast form's fused column kernel reads every channel's row spectra and
+    template spectra and writes one summed spectrum; its inverse rows read
+    that one channel and one den float per result."""
     import ctypes as C
     tw, th, iw, ih, cn = 96, 32, 1920, 1080, 3
     rw, rh = iw - tw + 1, ih - th + 1
@@ -499,7 +520,10 @@ def c2_models(L):
     dftW, dftH, bW, bH, dh2, ntiles = list(out)
     hw = dftW // 2 + 1
     ntx, nty = -(-rw // bW), -(-rh // bH)
-    m = {k: [0.0, 0.0] for k in ("k_prep", "k_fwd_rows", "k_cols_fwd_mul_inv", "k_inv_rows", "k_hsum", "k_vstats")}
+    fast = form == "fast"
+    m = {k: [0.0, 0.0] for k in ("k_prep", "k_fwd_rows", "k_cols_fwd_mul_inv", "k_cols_fwd_sum_inv", "k_inv_rows",
+                                 "k_hsum", "k_vstats")}
+    cinv = 1 if fast else cn  # channels through the inverse transforms
     for t in range(ntiles):
         tx, ty = t % ntx, t // ntx
         x0, y0 = tx * bW, ty * bH
@@ -513,21 +537,26 @@ def c2_models(L):
         m["k_fwd_rows"][1] += cn * (loaded // 2) * (fft_flops(dftW) + 6 * hw)
         m["k_cols_fwd_mul_inv"][0] += cn * (loaded * hw * 8 + H * hw * 8 + rows_out * hw * 8)
         m["k_cols_fwd_mul_inv"][1] += cn * hw * (2 * fft_flops(H) + 6 * H)
-        m["k_inv_rows"][0] += cn * rows_out * hw * 8
-        m["k_inv_rows"][1] += cn * (rows_out // 2) * (fft_flops(dftW) + 2 * dftW) + bw * bh * 8
+        m["k_cols_fwd_sum_inv"][0] += cn * (loaded * hw * 8 + H * hw * 8) + rows_out * hw * 8
+        m["k_cols_fwd_sum_inv"][1] += hw * ((cn + 1) * fft_flops(H) + 8 * cn * H)
+        m["k_inv_rows"][0] += cinv * rows_out * hw * 8
+        m["k_inv_rows"][1] += cinv * (rows_out // 2) * (fft_flops(dftW) + 2 * dftW) + bw * bh * 8
     hp = -(-rw // 32) * 32
+    lane = 4 if fast else 8                                 # den alone, or the (t, den) lane, per result
     m["k_prep"][0] = iw * ih * 4
-    m["k_inv_rows"][0] += rw * rh * 8                       # (t, den) lane per result
+    m["k_inv_rows"][0] += rw * rh * lane
     m["k_hsum"][0] = iw * ih * 4 + ih * hp * 16             # frame in, 4 window sums per (row, x) out
     bands = -(-rh // 16)
-    m["k_vstats"][0] = bands * (16 + th) * rw * 16 + rw * rh * 8
+    m["k_vstats"][0] = bands * (16 + th) * rw * 16 + rw * rh * lane
     return m
 
 
-def measured_traffic():
+def measured_traffic(form="exact"):
     """DRAM bytes per launch per kernel from the committed ncu summary of
-    this workload (profiles/match_c2_dram_traffic.txt), or {}."""
-    path = os.path.join(ROOT, "profiles", "match_c2_dram_traffic.txt")
+    this workload in this form (profiles/match_c2_dram_traffic.txt,
+    profiles/match_c2_fast_dram_traffic.txt), or {}."""
+    path = os.path.join(ROOT, "profiles", "match_c2_fast_dram_traffic.txt" if form == "fast"
+                        else "match_c2_dram_traffic.txt")
     out = {}
     if os.path.exists(path):
         for line in open(path):
@@ -582,11 +611,11 @@ def timeline(L, step_dev, torch, steps=3):
     return [(nm, round(1e3 * (a - base), 1), round(1e3 * (b - base), 1)) for nm, a, b in last]
 
 
-def roofline(L, step_dev, torch, stream, peak, peak_kind):
+def roofline(L, step_dev, torch, stream, peak, peak_kind, form="exact"):
     """The dominant kernel's algorithmic bytes over its duration, timed live
     by the library's event instrumentation."""
     rows = profile_kernels(L, step_dev, torch)
-    models = c2_models(L)
+    models = c2_models(L, form)
     total = sum(r[1] for r in rows)
     kernels = {}
     for nm, ms, n in rows:
@@ -597,7 +626,7 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind):
                        "gflops": (fl / (per / 1e3) / 1e9) if fl else None}
     top = max(((nm, v) for nm, v in kernels.items() if v["alg_bytes"]), key=lambda kv: kv[1]["share"])
     nm, v = top
-    traffic = measured_traffic().get(nm)
+    traffic = measured_traffic(form).get(nm)
     return {"bound": "hbm", "kernel": nm, "achieved": v["gbs"], "peak": peak, "unit": "GB/s",
             "frac": v["gbs"] / peak, "peak_source": peak_kind, "traffic": traffic, "share": v["share"],
             "alg_bytes_per_launch": v["alg_bytes"], "kernels": kernels}
@@ -618,6 +647,8 @@ def run_stream(args):
     H, W = frames[0].shape[:2]
     cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in color])
     gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in gray])
+    cf.SetForm(FORM[args.form])
+    gf.SetForm(FORM[args.form])
     st = cvm.NewStream(cf, gf, W, H)
     graphed, per_frame_launches = st.info()
     nfr = args.frames
@@ -653,7 +684,7 @@ def run_stream(args):
             "config": {"workload": "Fleet stream: 1920x1080 RGBA frames, 64 colour templates 24x24..128x96 + 8 gray "
                                    "matchers on the gray conversion; each frame moves 5% of the rectangles and redraws "
                                    f"sigma=2 noise ({K} precomputed frames cycled)",
-                       "frames": nfr, "templates": len(color) + len(gray), "parent": [W, H]},
+                       "frames": nfr, "templates": len(color) + len(gray), "parent": [W, H], "form": args.form},
             "frames_per_s": fps, "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
             "graphed": graphed, "gpu_launches": per_frame_launches,
             "findall_per_frame_fps": fps_plain, "clocks": clk.summary(),
@@ -833,8 +864,9 @@ def main():
     ap.add_argument("--workload", default="match", choices=["match", "fleet", "gray", "map", "stream"],
                     help="match (default, the reported line) or a secondary configuration")
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
-    ap.add_argument("--form", default="exact", choices=["exact", "fast"],
-                    help="arithmetic: exact (the reference's bits) or fast (cvm_set_form / cvm_fleet_set_form)")
+    ap.add_argument("--form", default="fast", choices=["exact", "fast"],
+                    help="arithmetic: fast (default; within 1e-5 of the FP64 definition) or exact (the "
+                         "reference's float32 bits; cvm_set_form / cvm_fleet_set_form)")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     args = ap.parse_args()
     if args.warmup < 3:

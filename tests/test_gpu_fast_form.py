@@ -203,3 +203,31 @@ def test_fast_flat_template_and_exact_default():
         cvm.SetForm(cvm.FORM_EXACT)
     with pytest.raises(cvm.CvmatchError):
         cvm.SetForm(5)
+
+
+def test_fast_stream_equals_fast_find_all():
+    """A frame stream whose fleets are in the fast form gives exactly their
+    fast-form FindAll results on every frame (same kernels, graph replay)."""
+    H, W = 260, 380
+    base = scene(41, H, W)
+    rng = np.random.default_rng(43)
+    frames = []
+    for _ in range(4):
+        f = base.copy()
+        y, x = int(rng.integers(0, H - 40)), int(rng.integers(0, W - 60))
+        f[y:y + 40, x:x + 60, :3] = rng.integers(0, 256, (40, 60, 3), dtype=np.uint8)
+        frames.append(f)
+    cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in (base[10:34, 20:60].copy(), base[100:150, 200:230].copy())])
+    gf = cvm.NewFleet(cvm.NewGrayMatcher(oracle.rgba_to_gray(base[50:80, 50:90])))
+    cf.SetForm(cvm.FORM_FAST)
+    gf.SetForm(cvm.FORM_FAST)
+    st = cvm.NewStream(cf, gf, W, H)
+    got = []
+    for i, f in enumerate(frames):
+        st.push(f)
+        if i >= 1:
+            got.append(st.pull())
+    got.append(st.pull())
+    for f, (rc, rg, _) in zip(frames, got):
+        assert [tuple(r) for r in rc] == [tuple(r) for r in cf.FindAll(f)]
+        assert [tuple(r) for r in rg] == [tuple(r) for r in gf.FindAll(oracle.rgba_to_gray(f))]
