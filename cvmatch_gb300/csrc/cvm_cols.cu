@@ -506,28 +506,7 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
                 for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
             };
             middle_sweep<true, L, LSC>(smem, ldx, ts, hwp, wv, tri);
-        } else if (MODE == 3) {
-            // fast form: sum over the member's channels of frame spectrum
-            // times conj(zero-mean template spectrum), fused multiply-adds
-            const float2 *fr = a.in + (size_t)tileLocal * a.cnS * chanStride + c0;
-            const float2 *tq = m->tspec[a.cls] + c0;
-            auto ldx = [&](float2 *x, int c, int B) {
-#pragma unroll
-                for (int ci = 0; ci < M; ci++) x[ci] = make_float2(0.f, 0.f);
-                if (c >= wv) return;
-                for (int kk = 0; kk < cn; kk++) {
-                    const float2 *p = fr + (size_t)kk * chanStride + (size_t)B * hwp + c;
-                    const float2 *q = tq + (size_t)kk * chanStride + (size_t)B * hwp + c;
-#pragma unroll
-                    for (int ci = 0; ci < M; ci++) {
-                        const float2 f = __ldg(p + (size_t)(S * ci) * hwp), t = __ldg(q + (size_t)(S * ci) * hwp);
-                        x[ci].x = fmaf(f.x, t.x, fmaf(f.y, t.y, x[ci].x));
-                        x[ci].y = fmaf(f.y, t.x, fmaf(-f.x, t.y, x[ci].y));
-                    }
-                }
-            };
-            middle_sweep<false, L, LSC, decltype(ldx), false>(smem, ldx, nullptr, hwp, wv, tri);
-        } else {
+        } else if (MODE == 2) {
             // the frame tile's stored natural-order spectrum
             auto ldx = [&](float2 *x, int c, int B) {
                 const float2 *p = src + (size_t)B * hwp + c;
@@ -535,6 +514,53 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
                 for (int ci = 0; ci < M; ci++) x[ci] = c < wv ? __ldg(p + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f);
             };
             middle_sweep<false, L, LSC>(smem, ldx, ts, hwp, wv, tri);
+        } else {
+            // Mode 3 (the fast form) sums over the member's channels frame x
+            // conj(zero-mean template) from stored spectra: the sum is staged
+            // into the strip first, U items per thread at a time (many
+            // independent loads in flight), then the inverse's first pass
+            // runs from shared memory.  (Staging the exact form's one-channel
+            // product the same way measured slower: it keeps mode 2's sweep.)
+            const float2 *fr = a.in + (size_t)tileLocal * a.cnS * chanStride + c0;
+            const float2 *tq = m->tspec[a.cls] + c0;
+            const int k0 = 0, k1 = cn;
+            constexpr int U = 8, TOTAL = N << LSC;
+            for (int i0 = threadIdx.x; i0 < TOTAL; i0 += U * kThreads) {
+                float2 acc[U];
+                size_t off[U];
+                bool ok[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int idx = i0 + u * kThreads, c = idx & (SC - 1);
+                    ok[u] = idx < TOTAL && c < wv;
+                    off[u] = (size_t)(idx >> LSC) * hwp + c;
+                    acc[u] = make_float2(0.f, 0.f);
+                }
+                for (int kk = k0; kk < k1; kk++) {
+                    const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
+                    float2 f[U], t[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        f[u] = ok[u] ? __ldg(fk + off[u]) : make_float2(0.f, 0.f);
+                        t[u] = ok[u] ? __ldg(tk + off[u]) : make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        acc[u].x = fmaf(f[u].x, t[u].x, fmaf(f[u].y, t[u].y, acc[u].x));
+                        acc[u].y = fmaf(f[u].y, t[u].x, fmaf(-f[u].x, t[u].y, acc[u].y));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    if (i0 + u * kThreads < TOTAL) smem[i0 + u * kThreads] = acc[u];
+            }
+            __syncthreads();
+            auto ldx = [&](float2 *x, int c, int B) {
+                const float2 *p = smem + (B << LSC) + c;
+#pragma unroll
+                for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
+            };
+            middle_sweep<false, L, LSC, decltype(ldx), false>(smem, ldx, nullptr, hwp, wv, tri);
         }
         const int ty = tile / a.g.ntx;
         const int bh = (ty == a.g.nty - 1) ? m->rh - b.y0 : a.g.blockH;

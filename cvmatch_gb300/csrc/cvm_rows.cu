@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
             }
             __syncthreads();
             line_fft<true, LOG2N>(smem, P, fc.triW);
+            if (fast) break;  // one channel: the epilogue reads the transformed lines directly
             for (int p = 0; p < P; p++) {
                 const float2 *zl = smem + p * LD;
                 float *a0 = acc + (size_t)(2 * p) * N, *a1 = a0 + N;
@@ -370,13 +371,20 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 else
                     td[q] = (!flat && x < bw) ? __ldg(lanes + rowBase + x) : make_float2(0.f, 0.f);
             }
+            const float2 *zl = smem + (rr >> 1) * LD;  // fast form: row rr is line rr/2's real or imaginary part
 #pragma unroll
             for (int q = 0; q < XIT; q++) {
                 const int x = tid + q * kThreads;
                 if (x < bw) {
                     float score = 1.f;
                     if (!flat) {
-                        const float num = fast ? acc[(size_t)rr * N + x] : __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
+                        float num;
+                        if (fast) {
+                            const float2 z = zl[padi(x)];
+                            num = (rr & 1) ? z.y : z.x;
+                        } else {
+                            num = __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
+                        }
                         const float den = td[q].y, an = fabsf(num);
                         if (an < den)
                             score = fast ? __fdividef(num, den) : __fdiv_rn(num, den);
