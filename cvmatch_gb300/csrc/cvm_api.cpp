@@ -915,7 +915,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         for (int c = 0; c < G.nclass; c++) {
             int P = 0;
             bg->partOff[c] = nparts;
-            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P);
+            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P, f->form != CVM_FORM_EXACT);
         }
         bg->nparts = nparts;
         std::vector<DevMember> tab(b.members.size());
@@ -1101,7 +1101,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                                      st));
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_inv_rows(G.g, G.fc[c], c, fast ? 1 : cnS, ms, nw, G.fc[c].dftH, bg.partOff[c],
-                                         bg.nparts, parts, counters, dOut, st));
+                                         bg.nparts, parts, counters, dOut, st, fast));
         }
     }
     return CVM_OK;

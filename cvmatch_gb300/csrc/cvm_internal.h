@@ -161,10 +161,12 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
 // counters[pIdx] must be zero before the first class's launch.  rowsMax
 // bounds the result rows of any tile (a single match: the block height;
 // a fleet: dftH), the same value for the launch and the partial count.
+// wide (fleets in the fast form, whose waves have CTAs to spare): twice
+// the row pairs per CTA, no channel accumulator in shared memory.
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
                             int nmembers, int rowsMax, int partOffset, int nparts, Partial *partials, int *counters,
-                            cvm_result *out, cudaStream_t st);
-int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta);
+                            cvm_result *out, cudaStream_t st, int wide = 0);
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide = 0);
 // Normalisation + first-occurrence extrema: CW x B results per CTA, ncx x
 // nby CTAs per member, result rows in groups of G; the member's last CTA
 // writes its result to out[outIdx].  counters (one int per member of the

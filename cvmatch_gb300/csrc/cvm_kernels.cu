@@ -1915,10 +1915,12 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     return cudaGetLastError();
 }
 
-int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta) {
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide) {
     // 4096 elements per CTA: the radix-16 passes (n/16 units per line) keep
-    // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM)
-    int P = 4096 / fc.n;
+    // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM);
+    // wide: 8192 elements (two units per thread per pass), ~70 KB without
+    // the accumulator
+    int P = (wide ? 8192 : 4096) / fc.n;
     if (P < 1) P = 1;
     // A tile emits at most rowsMax rows, and never more than dftH (a fleet
     // member's last band extends to its own result edge, still inside the
@@ -1932,7 +1934,7 @@ int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta) {
 
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
                             int nmembers, int rowsMax, int partOffset, int nparts, Partial *partials, int *counters,
-                            cvm_result *out, cudaStream_t st) {
+                            cvm_result *out, cudaStream_t st, int wide) {
     InvArgs a;
     a.g = g;
     a.fc = fc;
@@ -1940,7 +1942,8 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.cnS = cnS;
     a.ms = ms;
     int P = 0;
-    const int ctas = inv_rows_ctas_per_tile(fc, rowsMax, &P);
+    if (wide && (!ms.form || !rows_fixed_length(fc.log2n))) return cudaErrorInvalidValue;
+    const int ctas = inv_rows_ctas_per_tile(fc, rowsMax, &P, wide);
     a.pairsPerCta = P;
     a.partOffset = partOffset;
     a.nparts = nparts;
@@ -1948,7 +1951,7 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.counters = counters;
     a.out = out;
     dim3 grid(ctas, fc.ntiles, nmembers);
-    const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + 2 * fc.n * sizeof(float));
+    const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + (wide ? 0 : 2 * fc.n * sizeof(float)));
     ProfScope ps("k_inv_rows", st);
     if (rows_fixed_length(fc.log2n)) {
         launch_inv_rows_fixed(a, grid, smem, st);
