@@ -1645,7 +1645,10 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             lim = __fmul_rn(eps, __uint2float_rn((unsigned int)q));
             if (lim > 0.5f) lim = 0.5f;
         }
-        const float den = diff2 > lim ? __fmul_rn(__fsqrt_rn(diff2), Pm.templNorm) : 0.f;
+        // FAST: the square root from the hardware reciprocal square root
+        // (within 2 ulp) instead of the correctly rounded sequence
+        const float sd = FAST ? __fmul_rn(diff2, rsqrtf(diff2)) : __fsqrt_rn(diff2);
+        const float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
         if (FAST) {
             dens[(size_t)y * m.rw] = den;
         } else {
