@@ -84,24 +84,24 @@ __host__ __device__ constexpr int pass_kind(int L, int p) {
 // head's h=2 table) in makeTriTwiddles' concatenation (radix4.go:45-73).
 __host__ __device__ constexpr int tw_off(int L, int h) { return (L & 1) ? h - 2 : h - 1; }
 
-template <bool INV, int H>
+template <bool INV, int H, bool F = false>
 __device__ __forceinline__ void math16(float2 *e, const float2 *__restrict__ t) {
     const float2 a1 = __ldg(t), a2 = __ldg(t + H), a3 = __ldg(t + 2 * H);
 #pragma unroll
-    for (int b = 0; b < 4; b++) bfly4<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+    for (int b = 0; b < 4; b++) bfly4<INV, F>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
     const float2 *tB = t + 3 * H;
 #pragma unroll
     for (int q = 0; q < 4; q++)
-        bfly4<INV>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
+        bfly4<INV, F>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
                    __ldg(tB + 8 * H + H * q));
 }
 
-template <bool INV, int H>
+template <bool INV, int H, bool F = false>
 __device__ __forceinline__ void math4(float2 *e, const float2 *__restrict__ t) {
-    bfly4<INV>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
+    bfly4<INV, F>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
 }
 
-template <bool INV>
+template <bool INV, bool F = false>
 __device__ __forceinline__ void math_head(float2 *e, const float2 *__restrict__ t) {
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
@@ -111,7 +111,7 @@ __device__ __forceinline__ void math_head(float2 *e, const float2 *__restrict__ 
     }
 #pragma unroll
     for (int j = 0; j < 2; j++)
-        bfly4<INV>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+        bfly4<INV, F>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
 }
 
 __device__ __forceinline__ float2 mul_conj(float2 av, float2 bv) {
@@ -208,7 +208,7 @@ struct GlobalInv {
 };
 
 // One cascade pass p over all columns of the strip.  Ends with a barrier.
-template <bool INV, int L, int P, int LSC, typename LDF, typename STF>
+template <bool INV, int L, int P, int LSC, bool F, typename LDF, typename STF>
 __device__ __forceinline__ void col_pass(const LDF &ldf, const STF &stf, const float2 *__restrict__ tri) {
     constexpr int N = 1 << L, K = pass_kind(L, P), H = pass_h(L, P);
     constexpr int R = K == KHEAD ? 8 : (K == K16 ? 16 : 4), LR = ilog2k(R), LH = ilog2k(H);
@@ -219,22 +219,22 @@ __device__ __forceinline__ void col_pass(const LDF &ldf, const STF &stf, const f
         float2 e[R];
         ldf.template load<R, H>(e, c, base);
         if constexpr (K == KHEAD)
-            math_head<INV>(e, tri);
+            math_head<INV, F>(e, tri);
         else if constexpr (K == K16)
-            math16<INV, H>(e, tri + tw_off(L, H) + j);
+            math16<INV, H, F>(e, tri + tw_off(L, H) + j);
         else
-            math4<INV, H>(e, tri + tw_off(L, H) + j);
+            math4<INV, H, F>(e, tri + tw_off(L, H) + j);
         stf.template store<R, H>(e, c, base);
     }
     __syncthreads();
 }
 
 // Passes [P, PEND) in shared memory.
-template <bool INV, int L, int P, int PEND, int LSC, typename IO>
+template <bool INV, int L, int P, int PEND, int LSC, bool F, typename IO>
 __device__ __forceinline__ void col_passes(const IO &io, const float2 *__restrict__ tri) {
     if constexpr (P < PEND) {
-        col_pass<INV, L, P, LSC>(io, io, tri);
-        col_passes<INV, L, P + 1, PEND, LSC>(io, tri);
+        col_pass<INV, L, P, LSC, F>(io, io, tri);
+        col_passes<INV, L, P + 1, PEND, LSC, F>(io, tri);
     }
 }
 
@@ -274,7 +274,7 @@ __device__ __forceinline__ void fwd_last_pass(float2 *x, int B, const float2 *__
 
 // The inverse cascade's first pass on the same rows, stored through sp
 // (row B + S*c' at sp[(S*c') << LSC]).
-template <int L, int LSC>
+template <int L, int LSC, bool F = false>
 __device__ __forceinline__ void inv_first_pass(float2 *x, float2 *sp, const float2 *__restrict__ tri) {
     using G = Mid<L>;
     constexpr int M = G::M, S = G::S;
@@ -285,7 +285,7 @@ __device__ __forceinline__ void inv_first_pass(float2 *x, float2 *sp, const floa
             float2 e[8];
 #pragma unroll
             for (int t = 0; t < 8; t++) e[t] = x[(M / 8) * brevk(t, 3) + hd];
-            math_head<true>(e, tri);
+            math_head<true, F>(e, tri);
 #pragma unroll
             for (int t = 0; t < 8; t++) sp[(S * ((M / 8) * brevk(t, 3) + hd)) << LSC] = e[t];
         }
@@ -294,7 +294,7 @@ __device__ __forceinline__ void inv_first_pass(float2 *x, float2 *sp, const floa
         float2 e[16];
 #pragma unroll
         for (int r = 0; r < 16; r++) e[r] = x[brevk(r, 4)];
-        math16<true, 1>(e, tri);
+        math16<true, 1, F>(e, tri);
 #pragma unroll
         for (int r = 0; r < 16; r++) sp[(S * brevk(r, 4)) << LSC] = e[r];
     }
@@ -302,7 +302,7 @@ __device__ __forceinline__ void inv_first_pass(float2 *x, float2 *sp, const floa
 
 // The middle sweep.  x[c'] is row B + S*c' of the forward's natural-order
 // output; FWD runs the forward's last pass on it.
-template <bool FWD, int L, int LSC, typename LDX, bool MUL = true>
+template <bool FWD, int L, int LSC, typename LDX, bool MUL = true, bool F = false>
 __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const float2 *__restrict__ ts, int hwp,
                                              int wv, const float2 *__restrict__ tri) {
     constexpr int M = Mid<L>::M, S = Mid<L>::S, SC = 1 << LSC;
@@ -318,7 +318,7 @@ __device__ __forceinline__ void middle_sweep(float2 *smem, const LDX &ldx, const
             for (int ci = 0; ci < M; ci++)
                 x[ci] = mul_conj(x[ci], c < wv ? __ldg(tp + (size_t)(S * ci) * hwp) : make_float2(0.f, 0.f));
         }
-        inv_first_pass<L, LSC>(x, smem + (B << LSC) + c, tri);
+        inv_first_pass<L, LSC, F>(x, smem + (B << LSC) + c, tri);
     }
     __syncthreads();
 }
@@ -360,7 +360,7 @@ struct GlobalSlotsCh {  // forward-rows output of channel k (see GlobalSlots)
 };
 
 // One forward pass p over channels [0, cn) of the strip.  Ends with a barrier.
-template <int L, int P, int LSC, typename LDF, typename STF>
+template <int L, int P, int LSC, bool F, typename LDF, typename STF>
 __device__ __forceinline__ void col_pass_ch(int cn, const LDF &ldf, const STF &stf, const float2 *__restrict__ tri) {
     constexpr int N = 1 << L, K = pass_kind(L, P), H = pass_h(L, P);
     constexpr int R = K == KHEAD ? 8 : (K == K16 ? 16 : 4), LR = ilog2k(R), LH = ilog2k(H);
@@ -372,21 +372,21 @@ __device__ __forceinline__ void col_pass_ch(int cn, const LDF &ldf, const STF &s
         float2 e[R];
         ldf.template load<R, H>(e, k, c, base);
         if constexpr (K == KHEAD)
-            math_head<false>(e, tri);
+            math_head<false, F>(e, tri);
         else if constexpr (K == K16)
-            math16<false, H>(e, tri + tw_off(L, H) + j);
+            math16<false, H, F>(e, tri + tw_off(L, H) + j);
         else
-            math4<false, H>(e, tri + tw_off(L, H) + j);
+            math4<false, H, F>(e, tri + tw_off(L, H) + j);
         stf.template store<R, H>(e, k, c, base);
     }
     __syncthreads();
 }
 
-template <int L, int P, int PEND, int LSC>
+template <int L, int P, int PEND, int LSC, bool F>
 __device__ __forceinline__ void col_passes_ch(int cn, const SmemNatCh<L, LSC> &io, const float2 *__restrict__ tri) {
     if constexpr (P < PEND) {
-        col_pass_ch<L, P, LSC>(cn, io, io, tri);
-        col_passes_ch<L, P + 1, PEND, LSC>(cn, io, tri);
+        col_pass_ch<L, P, LSC, F>(cn, io, io, tri);
+        col_passes_ch<L, P + 1, PEND, LSC, F>(cn, io, tri);
     }
 }
 
@@ -413,8 +413,8 @@ __global__ void __launch_bounds__(256, 2) k_cols_sum_t(ColsArgs a) {
     const SmemNatCh<L, LSC> sn{smem};
     // every forward pass in shared memory (the last one too: keeping it in
     // the sum sweep's registers beside the accumulator spills)
-    col_pass_ch<L, 0, LSC>(cn, gs, sn, tri);
-    col_passes_ch<L, 1, NP, LSC>(cn, sn, tri);
+    col_pass_ch<L, 0, LSC, true>(cn, gs, sn, tri);
+    col_passes_ch<L, 1, NP, LSC, true>(cn, sn, tri);
     const float2 *ts = m.tspec[a.cls] + c0;
     for (int u = threadIdx.x; u < (S << LSC); u += blockDim.x) {
         const int c = u & (SC - 1), B = u >> LSC;
@@ -434,15 +434,15 @@ __global__ void __launch_bounds__(256, 2) k_cols_sum_t(ColsArgs a) {
                 acc[ci].y = fmaf(x[ci].y, t.x, fmaf(-x[ci].x, t.y, acc[ci].y));
             }
         }
-        inv_first_pass<L, LSC>(acc, smem + (B << LSC) + c, tri);
+        inv_first_pass<L, LSC, true>(acc, smem + (B << LSC) + c, tri);
     }
     __syncthreads();
     const int ty = tile / a.g.ntx;
     const int bh = (ty == a.g.nty - 1) ? m.rh - b.y0 : a.g.blockH;
     const SmemRev<L, LSC> sr{smem};
     const GlobalInv<L> gi{a.ms.scratch[a.cls] + (size_t)tileLocal * chanStride + c0, hwp, wv, min(N, (bh + 1) & ~1)};
-    col_passes<true, L, 1, NP - 1, LSC>(sr, tri);
-    col_pass<true, L, NP - 1, LSC>(sr, gi, tri);
+    col_passes<true, L, 1, NP - 1, LSC, true>(sr, tri);
+    col_pass<true, L, NP - 1, LSC, true>(sr, gi, tri);
 }
 
 template <int MODE, int L>
@@ -486,14 +486,14 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
     const SmemRev<L, LSC> sr{smem};
     if (!WAVE) {
         const GlobalSlots<L> gs{src, hwp, wv, min(N, (b.loadH + 1) & ~1)};
-        col_pass<false, L, 0, LSC>(gs, sn, tri);
+        col_pass<false, L, 0, LSC, false>(gs, sn, tri);
         if (MODE == 0) {
-            col_passes<false, L, 1, NP - 1, LSC>(sn, tri);
+            col_passes<false, L, 1, NP - 1, LSC, false>(sn, tri);
             const GlobalNat gn{a.out + ((size_t)tileLocal * a.cnS + k) * chanStride + c0, hwp, wv, a.scale};
-            col_pass<false, L, NP - 1, LSC>(sn, gn, tri);
+            col_pass<false, L, NP - 1, LSC, false>(sn, gn, tri);
             return;
         }
-        col_passes<false, L, 1, NP - 1, LSC>(sn, tri);
+        col_passes<false, L, 1, NP - 1, LSC, false>(sn, tri);
     }
     if (MODE != 0) {
         const float2 *ts = m->tspec[a.cls] + (size_t)k * chanStride + c0;
@@ -560,15 +560,15 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
 #pragma unroll
                 for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
             };
-            middle_sweep<false, L, LSC, decltype(ldx), false>(smem, ldx, nullptr, hwp, wv, tri);
+            middle_sweep<false, L, LSC, decltype(ldx), false, true>(smem, ldx, nullptr, hwp, wv, tri);
         }
         const int ty = tile / a.g.ntx;
         const int bh = (ty == a.g.nty - 1) ? m->rh - b.y0 : a.g.blockH;
         const size_t scrOff = MODE == 3 ? (size_t)tileLocal * chanStride : ((size_t)tileLocal * a.cnS + k) * chanStride;
         const GlobalInv<L> gi{a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] + scrOff + c0, hwp, wv,
                               min(N, (bh + 1) & ~1)};
-        col_passes<true, L, 1, NP - 1, LSC>(sr, tri);
-        col_pass<true, L, NP - 1, LSC>(sr, gi, tri);
+        col_passes<true, L, 1, NP - 1, LSC, MODE == 3>(sr, tri);
+        col_pass<true, L, NP - 1, LSC, MODE == 3>(sr, gi, tri);
     }
 }
 

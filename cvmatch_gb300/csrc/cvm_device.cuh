@@ -120,9 +120,16 @@ __device__ __forceinline__ float2 cmul_plain(float2 v, float2 w) {
     return make_float2(__fsub_rn(a, b), __fadd_rn(c, d));
 }
 
+// The fast form's complex product: two products and two fused
+// multiply-adds.
+__device__ __forceinline__ float2 cmul_fma(float2 v, float2 w) {
+    return make_float2(fmaf(v.x, w.x, -__fmul_rn(v.y, w.y)), fmaf(v.x, w.y, __fmul_rn(v.y, w.x)));
+}
+
 // One radix-4 butterfly (radix4.go:126-147); pa/pc/pb/pd are rows r, r+h,
 // r+2h, r+3h.  The inverse conjugates the twiddles and flips the rotation.
-template <bool INV>
+// F (the fast form only): the twiddle products with fused multiply-adds.
+template <bool INV, bool F = false>
 __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2 *pd, float2 bw,
                                       float2 cw, float2 dw) {
     if (INV) {
@@ -131,9 +138,9 @@ __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2
         dw.y = -dw.y;
     }
     const float2 av = *pa;
-    const float2 tb = cmul_plain(*pb, bw);
-    const float2 tc = cmul_plain(*pc, cw);
-    const float2 td = cmul_plain(*pd, dw);
+    const float2 tb = F ? cmul_fma(*pb, bw) : cmul_plain(*pb, bw);
+    const float2 tc = F ? cmul_fma(*pc, cw) : cmul_plain(*pc, cw);
+    const float2 td = F ? cmul_fma(*pd, dw) : cmul_plain(*pd, dw);
     const float s0x = __fadd_rn(av.x, tc.x), s0y = __fadd_rn(av.y, tc.y);
     const float s1x = __fsub_rn(av.x, tc.x), s1y = __fsub_rn(av.y, tc.y);
     const float s2x = __fadd_rn(tb.x, td.x), s2y = __fadd_rn(tb.y, td.y);

@@ -26,34 +26,34 @@ __device__ __forceinline__ int brevn(int x) {
 // Element i of a unit of quarter size H starting at base = blk*R*H + j
 // (j < H) sits at padi(base) + padc(H*i): for H >= 16 the pad counter is
 // linear in i, and for H < 16 the low bits j + (H*i mod 16) never reach 16.
-template <bool INV, int H>
+template <bool INV, int H, bool F = false>
 __device__ __forceinline__ void unit16(float2 *p, const float2 *__restrict__ tA, const float2 *__restrict__ tB) {
     float2 e[16];
 #pragma unroll
     for (int i = 0; i < 16; i++) e[i] = p[padc(H * i)];
     const float2 a1 = __ldg(tA), a2 = __ldg(tA + H), a3 = __ldg(tA + 2 * H);
 #pragma unroll
-    for (int b = 0; b < 4; b++) bfly4<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+    for (int b = 0; b < 4; b++) bfly4<INV, F>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
 #pragma unroll
     for (int q = 0; q < 4; q++)
-        bfly4<INV>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
-                   __ldg(tB + 8 * H + H * q));
+        bfly4<INV, F>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
+                      __ldg(tB + 8 * H + H * q));
 #pragma unroll
     for (int i = 0; i < 16; i++) p[padc(H * i)] = e[i];
 }
 
-template <bool INV, int H>
+template <bool INV, int H, bool F = false>
 __device__ __forceinline__ void unit4(float2 *p, const float2 *__restrict__ t) {
     float2 e[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) e[i] = p[padc(H * i)];
-    bfly4<INV>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
+    bfly4<INV, F>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
 #pragma unroll
     for (int i = 0; i < 4; i++) p[padc(H * i)] = e[i];
 }
 
 // The radix-2 head and the h=2 stage on 8 contiguous elements.
-template <bool INV>
+template <bool INV, bool F = false>
 __device__ __forceinline__ void unit_head(float2 *p, const float2 *__restrict__ t) {
     float2 e[8];
 #pragma unroll
@@ -66,7 +66,7 @@ __device__ __forceinline__ void unit_head(float2 *p, const float2 *__restrict__ 
     }
 #pragma unroll
     for (int j = 0; j < 2; j++)
-        bfly4<INV>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+        bfly4<INV, F>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
 #pragma unroll
     for (int i = 0; i < 8; i++) p[i] = e[i];
 }
@@ -77,37 +77,37 @@ struct Line {
     static constexpr int LD = N + (N >> 4) + 1;  // padded_len(N)
 };
 
-template <bool INV, int LOG2N, int H>
+template <bool INV, int LOG2N, int H, bool F>
 __device__ __forceinline__ void pass16(float2 *s, int lines, const float2 *tA, const float2 *tB) {
     constexpr int LU = LOG2N - 4, LH = ilog2c(H), LD = Line<LOG2N>::LD;
     const int total = lines << LU;
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int line = u >> LU, v = u & ((1 << LU) - 1);
         const int j = v & (H - 1), base = ((v >> LH) << (LH + 4)) + j;
-        unit16<INV, H>(s + line * LD + padi(base), tA + j, tB + j);
+        unit16<INV, H, F>(s + line * LD + padi(base), tA + j, tB + j);
     }
     __syncthreads();
 }
 
-template <bool INV, int LOG2N, int H>
+template <bool INV, int LOG2N, int H, bool F>
 __device__ __forceinline__ void pass4(float2 *s, int lines, const float2 *t) {
     constexpr int LU = LOG2N - 2, LH = ilog2c(H), LD = Line<LOG2N>::LD;
     const int total = lines << LU;
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int line = u >> LU, v = u & ((1 << LU) - 1);
         const int j = v & (H - 1), base = ((v >> LH) << (LH + 2)) + j;
-        unit4<INV, H>(s + line * LD + padi(base), t + j);
+        unit4<INV, H, F>(s + line * LD + padi(base), t + j);
     }
     __syncthreads();
 }
 
-template <bool INV, int LOG2N>
+template <bool INV, int LOG2N, bool F>
 __device__ __forceinline__ void pass_head(float2 *s, int lines, const float2 *t) {
     constexpr int LU = LOG2N - 3, LD = Line<LOG2N>::LD;
     const int total = lines << LU;
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int line = u >> LU, v = u & ((1 << LU) - 1);
-        unit_head<INV>(s + line * LD + padi(v << 3), t);
+        unit_head<INV, F>(s + line * LD + padi(v << 3), t);
     }
     __syncthreads();
 }
@@ -115,27 +115,28 @@ __device__ __forceinline__ void pass_head(float2 *s, int lines, const float2 *t)
 // Stage h's twiddle table starts at h - 1 (even log2) or h - 2 (odd log2,
 // after the head's h=2 table) in the concatenated table of
 // makeTriTwiddles (radix4.go:45-73).
-template <bool INV, int LOG2N, int H>
+template <bool INV, int LOG2N, int H, bool F>
 __device__ __forceinline__ void passes_from(float2 *s, int lines, const float2 *tri) {
     constexpr int N = 1 << LOG2N;
     constexpr int OFF = (LOG2N & 1) ? H - 2 : H - 1;
     if constexpr (16 * H <= N) {
-        pass16<INV, LOG2N, H>(s, lines, tri + OFF, tri + OFF + 3 * H);
-        passes_from<INV, LOG2N, 16 * H>(s, lines, tri);
+        pass16<INV, LOG2N, H, F>(s, lines, tri + OFF, tri + OFF + 3 * H);
+        passes_from<INV, LOG2N, 16 * H, F>(s, lines, tri);
     } else if constexpr (4 * H <= N) {
-        pass4<INV, LOG2N, H>(s, lines, tri + OFF);
+        pass4<INV, LOG2N, H, F>(s, lines, tri + OFF);
     }
 }
 
 // fftR4Scalar (radix4.go:106-149) over `lines` padded lines of length 2^LOG2N
-// in bit-reversed order; ends with a barrier.
-template <bool INV, int LOG2N>
+// in bit-reversed order; ends with a barrier.  F: the fast form's fused
+// twiddle products.
+template <bool INV, int LOG2N, bool F = false>
 __device__ __forceinline__ void line_fft(float2 *s, int lines, const float2 *tri) {
     if constexpr (LOG2N & 1) {
-        pass_head<INV, LOG2N>(s, lines, tri);
-        passes_from<INV, LOG2N, 8>(s, lines, tri);
+        pass_head<INV, LOG2N, F>(s, lines, tri);
+        passes_from<INV, LOG2N, 8, F>(s, lines, tri);
     } else {
-        passes_from<INV, LOG2N, 1>(s, lines, tri);
+        passes_from<INV, LOG2N, 1, F>(s, lines, tri);
     }
 }
 
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
 // z[kk] and its mirror z[N-kk]; the channels accumulate in channel order;
 // the epilogue scores with the per-result (t, den) lanes and keeps
 // first-occurrence extrema merged by each member's last CTA.
-template <int LOG2N>
+template <int LOG2N, bool FAST>
 __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     constexpr int XIT = (N + kThreads - 1) / kThreads;  // result columns per thread
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     Ext e;
     ext_init(e);
     // the fast form's scratch holds one channel-summed correlation per tile
-    const bool fast = a.ms.form != 0;
+    constexpr bool fast = FAST;
     if (P > 0 && !flat) {
         const int cn = fast ? 1 : Pm.cn;
         const size_t chanStride = (size_t)fc.dftH * hwp;
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 smem[tid * LD + padi(brevn<LOG2N>(HALF))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
             }
             __syncthreads();
-            line_fft<true, LOG2N>(smem, P, fc.triW);
+            line_fft<true, LOG2N, FAST>(smem, P, fc.triW);
             if (fast) break;  // one channel: the epilogue reads the transformed lines directly
             for (int p = 0; p < P; p++) {
                 const float2 *zl = smem + p * LD;
@@ -436,8 +437,13 @@ void fwd_one(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStre
 
 template <int L>
 void inv_one(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
-    set_smem(k_inv_rows_t<L>, smem);
-    k_inv_rows_t<L><<<grid, kThreads, smem, st>>>(a);
+    if (a.ms.form) {
+        set_smem(k_inv_rows_t<L, true>, smem);
+        k_inv_rows_t<L, true><<<grid, kThreads, smem, st>>>(a);
+    } else {
+        set_smem(k_inv_rows_t<L, false>, smem);
+        k_inv_rows_t<L, false><<<grid, kThreads, smem, st>>>(a);
+    }
 }
 
 }  // namespace
