@@ -1598,7 +1598,7 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     unsigned long long q = 0;
 #pragma unroll
     for (int k = 0; k < CN; k++) s[k] = 0u;
-#pragma unroll 4
+#pragma unroll(PRE ? 4 : 8)
     for (int dy = 0; dy < th; dy++) {
         unsigned int hv[CN + 1];
         rowvals(H + (size_t)(Y0 + dy) * rp, hv);
@@ -1610,55 +1610,69 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     const unsigned int t0 = (unsigned int)Pm.tsum[0], t1 = (unsigned int)Pm.tsum[1];
     const unsigned int t2 = (unsigned int)Pm.tsum[2], t3 = (unsigned int)Pm.tsum[3];
     const float eps = 1.1920928955078125e-06f;  // 10 * 2^-23
-    for (int y = Y0; y < Y0 + Bv; y++) {
-        unsigned int hin[CN + 1], hout[CN + 1];
-        const bool more = y + 1 < Y0 + Bv;
-        if (more) {
-            rowvals(H + (size_t)(y + th) * rp, hin);
-            rowvals(H + (size_t)y * rp, hout);
-        }
-        unsigned long long cross = 0, sq = (unsigned long long)s[0] * s[0];
-        if (!FAST) cross = (unsigned long long)s[0] * t0;
-        if (CN > 1) {
-            if (!FAST) cross += (unsigned long long)s[CN > 1 ? 1 : 0] * t1;
-            sq += (unsigned long long)s[CN > 1 ? 1 : 0] * s[CN > 1 ? 1 : 0];
-        }
-        if (CN > 2) {
-            if (!FAST) cross += (unsigned long long)s[CN > 2 ? 2 : 0] * t2;
-            sq += (unsigned long long)s[CN > 2 ? 2 : 0] * s[CN > 2 ? 2 : 0];
-        }
-        if (CN > 3) {
-            if (!FAST) cross += (unsigned long long)s[CN > 3 ? 3 : 0] * t3;
-            sq += (unsigned long long)s[CN > 3 ? 3 : 0] * s[CN > 3 ? 3 : 0];
-        }
-        // the spill lanes (impl.go:902-1009) and normOne's corr-free part
-        // FAST: the exact variance numerator from its two 32-bit halves
-        // (within 1.5 ulp; the reference's two-step float64 -> float32
-        // conversion is kept otherwise)
-        const unsigned long long idv = area * q - sq;
-        const float id = FAST ? fmaf(__uint2float_rn((unsigned int)(idv >> 32)), 4294967296.0f,
-                                     __uint2float_rn((unsigned int)idv))
-                              : f32_via_f64((long long)idv);
-        const float diff2 = __fmul_rn(id, Pm.varScale);
-        float lim = 0.5f;
-        if (q < (1ull << 24)) {
-            lim = __fmul_rn(eps, __uint2float_rn((unsigned int)q));
-            if (lim > 0.5f) lim = 0.5f;
-        }
-        // FAST: the square root from the hardware reciprocal square root
-        // (within 2 ulp) instead of the correctly rounded sequence
-        const float sd = FAST ? __fmul_rn(diff2, rsqrtf(diff2)) : __fsqrt_rn(diff2);
-        const float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
-        if (FAST) {
-            dens[(size_t)y * m.rw] = den;
-        } else {
-            const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);
-            lanes[(size_t)y * m.rw] = make_float2(__fmul_rn(l0, Pm.numScale), den);
-        }
-        if (more) {
+    // The slide in batches of RB rows: every row the batch enters and leaves
+    // is loaded first (2 * RB row loads in flight), then the batch's results
+    // are scored in order -- one wait on L2 per batch instead of per row.
+    // A fleet's prefix differences (two loads per row) keep RB = 1: the
+    // batch's registers cost more occupancy than its loads in flight gain.
+    constexpr int RB = PRE ? 1 : 4;
+    for (int yb = Y0; yb < Y0 + Bv; yb += RB) {
+        unsigned int hinB[RB][CN + 1], houtB[RB][CN + 1];
 #pragma unroll
-            for (int k = 0; k < CN; k++) s[k] += hin[k] - hout[k];
-            q += (unsigned long long)hin[CN] - (unsigned long long)hout[CN];
+        for (int r = 0; r < RB; r++)
+            if (yb + r + 1 < Y0 + Bv) {
+                rowvals(H + (size_t)(yb + r + th) * rp, hinB[r]);
+                rowvals(H + (size_t)(yb + r) * rp, houtB[r]);
+            }
+#pragma unroll
+        for (int r = 0; r < RB; r++) {
+            const int y = yb + r;
+            if (y >= Y0 + Bv) break;
+            const bool more = y + 1 < Y0 + Bv;
+            const unsigned int *hin = hinB[r], *hout = houtB[r];
+            unsigned long long cross = 0, sq = (unsigned long long)s[0] * s[0];
+            if (!FAST) cross = (unsigned long long)s[0] * t0;
+            if (CN > 1) {
+                if (!FAST) cross += (unsigned long long)s[CN > 1 ? 1 : 0] * t1;
+                sq += (unsigned long long)s[CN > 1 ? 1 : 0] * s[CN > 1 ? 1 : 0];
+            }
+            if (CN > 2) {
+                if (!FAST) cross += (unsigned long long)s[CN > 2 ? 2 : 0] * t2;
+                sq += (unsigned long long)s[CN > 2 ? 2 : 0] * s[CN > 2 ? 2 : 0];
+            }
+            if (CN > 3) {
+                if (!FAST) cross += (unsigned long long)s[CN > 3 ? 3 : 0] * t3;
+                sq += (unsigned long long)s[CN > 3 ? 3 : 0] * s[CN > 3 ? 3 : 0];
+            }
+            // the spill lanes (impl.go:902-1009) and normOne's corr-free part
+            // FAST: the exact variance numerator from its two 32-bit halves
+            // (within 1.5 ulp; the reference's two-step float64 -> float32
+            // conversion is kept otherwise)
+            const unsigned long long idv = area * q - sq;
+            const float id = FAST ? fmaf(__uint2float_rn((unsigned int)(idv >> 32)), 4294967296.0f,
+                                         __uint2float_rn((unsigned int)idv))
+                                  : f32_via_f64((long long)idv);
+            const float diff2 = __fmul_rn(id, Pm.varScale);
+            float lim = 0.5f;
+            if (q < (1ull << 24)) {
+                lim = __fmul_rn(eps, __uint2float_rn((unsigned int)q));
+                if (lim > 0.5f) lim = 0.5f;
+            }
+            // FAST: the square root from the hardware reciprocal square root
+            // (within 2 ulp) instead of the correctly rounded sequence
+            const float sd = FAST ? __fmul_rn(diff2, rsqrtf(diff2)) : __fsqrt_rn(diff2);
+            const float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
+            if (FAST) {
+                dens[(size_t)y * m.rw] = den;
+            } else {
+                const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);
+                lanes[(size_t)y * m.rw] = make_float2(__fmul_rn(l0, Pm.numScale), den);
+            }
+            if (more) {
+#pragma unroll
+                for (int k = 0; k < CN; k++) s[k] += hin[k] - hout[k];
+                q += (unsigned long long)hin[CN] - (unsigned long long)hout[CN];
+            }
         }
     }
 }
@@ -2077,9 +2091,22 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     v.hp = sg.hp;
     v.ms = ms;
     v.BV = vstat_band(sg, nmembers);
+    // One match: every band first sums th rows, so a tall template wants
+    // tall bands (up to th / 2 rows, while ~8 warps per SM remain), and
+    // narrower CTAs when the taller bands leave fewer than ~3 per SM.
+    int VT = kThreads, ncx = sg.ncx;
+    if (!sharedPrefix && !ms.table) {
+        const long long warpCols = (soloRw + 31) / 32;
+        int BV = 16;
+        while (BV < 128 && 4 * BV <= ms.solo.th && warpCols * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) >= 8 * 152)
+            BV *= 2;
+        v.BV = BV;
+        while (VT > 64 && (long long)((soloRw + VT - 1) / VT) * ((sg.rhMax + BV - 1) / BV) < 3 * 152) VT >>= 1;
+        ncx = (soloRw + VT - 1) / VT;
+    }
     const size_t smem = (size_t)(cnMax + 1) * (iw + 1) * sizeof(unsigned int);
     const int nb = (sg.rhMax + v.BV - 1) / v.BV;
-    dim3 gh(ih, 1, nmembers), gv = sharedPrefix ? dim3(nmembers, sg.ncx, nb) : dim3(sg.ncx, nb, nmembers);
+    dim3 gh(ih, 1, nmembers), gv = sharedPrefix ? dim3(nmembers, sg.ncx, nb) : dim3(ncx, nb, nmembers);
     if (!sharedPrefix) {
         ProfScope ps("k_hsum", st);
         if (cnMax == 1) {
@@ -2109,13 +2136,13 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
                 k_vstats<4, 4, true, true><<<gv, kThreads, 0, st>>>(v);
         } else if (ms.form) {
             if (cnMax == 1)
-                k_vstats<1, 1, false, true><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<1, 1, false, true><<<gv, VT, 0, st>>>(v);
             else if (cnMax == 2)
-                k_vstats<2, 2, false, true><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<2, 2, false, true><<<gv, VT, 0, st>>>(v);
             else if (cnMin == 3)
-                k_vstats<3, 4, false, true><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<3, 4, false, true><<<gv, VT, 0, st>>>(v);
             else
-                k_vstats<4, 4, false, true><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<4, 4, false, true><<<gv, VT, 0, st>>>(v);
         } else if (sharedPrefix) {
             if (cnMax == 1)
                 k_vstats<1, 1, true><<<gv, kThreads, 0, st>>>(v);
@@ -2127,13 +2154,13 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
                 k_vstats<4, 4, true><<<gv, kThreads, 0, st>>>(v);
         } else {
             if (cnMax == 1)
-                k_vstats<1, 1, false><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<1, 1, false><<<gv, VT, 0, st>>>(v);
             else if (cnMax == 2)
-                k_vstats<2, 2, false><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<2, 2, false><<<gv, VT, 0, st>>>(v);
             else if (cnMin == 3)
-                k_vstats<3, 4, false><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<3, 4, false><<<gv, VT, 0, st>>>(v);
             else
-                k_vstats<4, 4, false><<<gv, kThreads, 0, st>>>(v);
+                k_vstats<4, 4, false><<<gv, VT, 0, st>>>(v);
         }
     }
     count_launches(sharedPrefix ? 1 : 2);
