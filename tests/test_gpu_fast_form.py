@@ -231,3 +231,55 @@ def test_fast_stream_equals_fast_find_all():
     for f, (rc, rg, _) in zip(frames, got):
         assert [tuple(r) for r in rc] == [tuple(r) for r in cf.FindAll(f)]
         assert [tuple(r) for r in rg] == [tuple(r) for r in gf.FindAll(oracle.rgba_to_gray(f))]
+
+
+# ------------------------------------------------ more inputs, fast form
+
+
+def _recipe(m, thresh, rx, ry):
+    """The MatchMap recipe of cvmatch_test.go:324-381, in numpy."""
+    h, w = m.shape
+    out = []
+    for y, x in np.argwhere(~(m < thresh)):
+        win = m[max(0, y - ry):min(h, y + ry + 1), max(0, x - rx):min(w, x + rx + 1)]
+        if not np.any(win > m[y, x]):
+            out.append((int(x), int(y)))
+    return out
+
+
+def test_fast_peaks_equal_recipe_on_the_fast_map(fast_form):
+    img = scene(47, 180, 260)
+    tpl = img[40:60, 100:130].copy()
+    m, _, _ = cvm.MatchMap(img, tpl)
+    want = _recipe(m, 0.3, 4, 3)
+    hits, n = cvm.MatchMapPeaks(img, tpl, 0.3, 4, 3, max_peaks=len(want) + 3)
+    assert n == len(want) and hits == want and n > 0
+
+
+def test_fast_sub_image_strides(fast_form):
+    big = scene(53, 300, 420)
+    view = big[20:260, 30:400]           # a sub-image: row stride wider than its width
+    t = big[120:150, 200:248]            # template as a view too
+    m, _, _ = cvm.MatchMap(view, t)
+    map_check(m, oracle.ref_match_f64(np.ascontiguousarray(view), np.ascontiguousarray(t), 3, threads=16),
+              "sub-image views")
+    jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
+    assert (jx, jy) == (170, 100)
+
+
+def test_fast_template_alpha_varies(fast_form):
+    img = scene(59, 200, 280)
+    t = img[50:80, 60:100].copy()
+    t[::2, ::3, 3] = 7                    # the template's alpha varies: cn = 4
+    m, _, _ = cvm.MatchMap(img, t)
+    map_check(m, oracle.ref_match_f64(img, t, 4, threads=16), "template alpha varies")
+
+
+@pytest.mark.parametrize("cn,step", [(2, 2), (4, 4), (3, 4)])
+def test_fast_match_u8_channels(fast_form, cn, step):
+    rng = np.random.default_rng(61 + cn)
+    img = scene(67, 160, 230)[..., :step].copy()
+    img[40:90, 60:140] = rng.integers(0, 256, (50, 80, step), dtype=np.uint8)
+    t = img[50:80, 70:110].copy()
+    _, m = cvm.match_u8(img, t, cn)
+    map_check(m, oracle.ref_match_f64(img, t, cn, threads=16), f"match_u8 cn={cn} step={step}")
