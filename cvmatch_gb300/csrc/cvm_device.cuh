@@ -91,6 +91,7 @@ struct FwdRowsArgs {
     // device computed; float, exact when subDiv == 1)
     const unsigned long long *subSums;
     float subDiv;
+    int fma;                 // the fast form's samples: fused twiddle products
 };
 
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).

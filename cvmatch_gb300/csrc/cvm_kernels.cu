@@ -1850,6 +1850,9 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         for (int k = 0; k < 4; k++) a.sub[k] = sub ? sub[k] : 0.0f;
         a.subSums = subSums;
         a.subDiv = subDiv;
+        // a sample transform marks the fast form (the exact form packs the
+        // reference's samples untouched): its butterflies may fuse
+        a.fma = (mul != 1.0f || sub || subSums) ? 1 : 0;
         for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
             a.chanFirst = c0;
             launch_fwd_rows_fixed(a, grid, threads, smem, st);

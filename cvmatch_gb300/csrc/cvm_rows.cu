@@ -148,7 +148,7 @@ __device__ __forceinline__ int div_cn(int line, int cn) {
 
 // ------------------------------------------------------------ forward rows
 
-template <int LOG2N>
+template <int LOG2N, bool F>
 __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     extern __shared__ float2 smem[];
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
             if (g < cn) d[g * LD] = make_float2(va[g], vb[g]);
     }
     __syncthreads();
-    line_fft<false, LOG2N>(smem, lines, fc.triW);
+    line_fft<false, LOG2N, F>(smem, lines, fc.triW);
     // Untangle (impl.go:331-341) into the two real-row spectra at their
     // bit-reversed column-transform slots.
     const int hwp = fc.hwp, log2H = fc.log2H;
@@ -431,8 +431,13 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
 
 template <int L>
 void fwd_one(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
-    set_smem(k_fwd_rows_t<L>, smem);
-    k_fwd_rows_t<L><<<grid, threads, smem, st>>>(a);
+    if (a.fma) {
+        set_smem(k_fwd_rows_t<L, true>, smem);
+        k_fwd_rows_t<L, true><<<grid, threads, smem, st>>>(a);
+    } else {
+        set_smem(k_fwd_rows_t<L, false>, smem);
+        k_fwd_rows_t<L, false><<<grid, threads, smem, st>>>(a);
+    }
 }
 
 template <int L>
