@@ -128,3 +128,17 @@ def test_product_planner_matches_oracle_random_shapes():
         assert L.cvm_plan(tw, th, rw, rh, out) == 0
         p = oracle.plan(tw, th, rw, rh)
         assert (out[0], out[1], out[2], out[3]) == (p.dft_w, p.dft_h, p.block_w, p.block_h), (tw, th, rw, rh)
+
+
+def test_form_setters_validate_without_device_work():
+    """cvm_set_form / cvm_get_form: the process-wide form of one-shot
+    matches; an unknown form is refused and leaves the form unchanged."""
+    L = cvm.lib()
+    assert L.cvm_get_form() == cvm.FORM_EXACT
+    rc, msg = _err(L.cvm_set_form(7))
+    assert rc == 1 and "unknown form 7" in msg
+    assert L.cvm_get_form() == cvm.FORM_EXACT
+    assert L.cvm_set_form(cvm.FORM_FAST) == 0 and L.cvm_get_form() == cvm.FORM_FAST
+    assert cvm.SetForm(cvm.FORM_EXACT) == cvm.FORM_FAST and L.cvm_get_form() == cvm.FORM_EXACT
+    rc, msg = _err(L.cvm_fleet_set_form(None, cvm.FORM_FAST))
+    assert rc == 3 and msg == "cvmatch: empty fleet"
