@@ -214,6 +214,20 @@ __device__ __forceinline__ void ext_add(Ext &e, float v, long long i) {
     }
 }
 
+// A thread that visits its results in increasing index order keeps the
+// first occurrence with strict comparisons alone; ties between threads are
+// broken by index when the partial extrema merge (ext_merge).
+__device__ __forceinline__ void ext_add_inc(Ext &e, float v, long long i) {
+    if (v < e.minV) {
+        e.minV = v;
+        e.minI = i;
+    }
+    if (v > e.maxV) {
+        e.maxV = v;
+        e.maxI = i;
+    }
+}
+
 __device__ __forceinline__ void ext_merge(Ext &e, const Ext &o) {
     if (o.minV < e.minV || (o.minV == e.minV && o.minI < e.minI)) {
         e.minV = o.minV;

@@ -395,7 +395,8 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                             score = 0.f;
                     }
                     if (map) map[rowBase + x] = score;
-                    if (x >= xlo && x < xhi) ext_add(e, score, rowBase + x);
+                    // rows ascend, and x ascends within a row: increasing indices
+                    if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase + x);
                 }
             }
         }
