@@ -283,3 +283,31 @@ def test_fast_match_u8_channels(fast_form, cn, step):
     t = img[50:80, 70:110].copy()
     _, m = cvm.match_u8(img, t, cn)
     map_check(m, oracle.ref_match_f64(img, t, cn, threads=16), f"match_u8 cn={cn} step={step}")
+
+
+def test_fast_large_gray_template_mean_subtracted(fast_form):
+    """A gray template of 258 x 256 pixels: area * 255 >= 2^24, so the
+    zero-mean spectrum is built from T - mean(T) in float instead of the
+    exact integers area*T - sum(T)."""
+    rng = np.random.default_rng(71)
+    img = oracle.rgba_to_gray(scene(73, 420, 560))
+    img[100:356, 150:408] = rng.integers(0, 256, (256, 258), dtype=np.uint8)
+    t = img[100:356, 150:408].copy()
+    assert t.shape[0] * t.shape[1] * 255 >= 1 << 24
+    _, m = cvm.match_u8(img, t, 1)
+    map_check(m, oracle.ref_match_f64(img, t, 1, threads=16), "258x256 gray template")
+    jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
+    assert (jx, jy) == (150, 100)
+
+
+def test_fast_form_refuses_transforms_above_4096(fast_form):
+    """A 4100-px-wide template needs 8192-point row transforms: the exact
+    form runs them (generic kernels), the fast form refuses cleanly."""
+    img = np.ascontiguousarray(scene(79, 60, 4200))
+    tpl = img[11:51, 50:4150].copy()
+    with pytest.raises(cvm.CvmatchError) as e:
+        cvm.match_u8(img, tpl, 4)
+    assert e.value.code == 11 and "fast form" in str(e.value)
+    cvm.SetForm(cvm.FORM_EXACT)
+    t, _ = cvm.match_u8(img, tpl, 4, want_map=False)
+    assert (t[4], t[5]) == (50, 11)
