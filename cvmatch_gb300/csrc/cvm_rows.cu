@@ -140,6 +140,69 @@ __device__ __forceinline__ void line_fft(float2 *s, int lines, const float2 *tri
     }
 }
 
+// The cascade's last pass for log2 n = L: its quarter size and radix (16 or
+// 4), following the pass list of line_fft (odd L: the head, then radix-16
+// passes from quarter 8; even L: from quarter 1; a trailing radix-4 pass
+// when two stages remain).
+__host__ __device__ constexpr int last_pass_h(int L) {
+    int h = (L & 1) ? 8 : 1, lastH = h;
+    while (true) {
+        if (16 * h <= (1 << L)) {
+            lastH = h;
+            h *= 16;
+        } else {
+            if (4 * h <= (1 << L)) lastH = h;
+            return lastH;
+        }
+    }
+}
+__host__ __device__ constexpr int last_pass_r(int L) {
+    return 16 * last_pass_h(L) <= (1 << L) ? 16 : 4;
+}
+
+// Every pass but the last (the fast form scores the last pass's outputs
+// from registers); ends with a barrier.
+template <bool INV, int LOG2N, int H, bool F>
+__device__ __forceinline__ void passes_but_last(float2 *s, int lines, const float2 *tri) {
+    constexpr int N = 1 << LOG2N;
+    constexpr int OFF = (LOG2N & 1) ? H - 2 : H - 1;
+    if constexpr (H != last_pass_h(LOG2N) && 16 * H <= N) {
+        pass16<INV, LOG2N, H, F>(s, lines, tri + OFF, tri + OFF + 3 * H);
+        passes_but_last<INV, LOG2N, 16 * H, F>(s, lines, tri);
+    }
+}
+
+template <bool INV, int LOG2N, bool F>
+__device__ __forceinline__ void line_fft_but_last(float2 *s, int lines, const float2 *tri) {
+    if constexpr (LOG2N & 1) {
+        pass_head<INV, LOG2N, F>(s, lines, tri);
+        passes_but_last<INV, LOG2N, 8, F>(s, lines, tri);
+    } else {
+        passes_but_last<INV, LOG2N, 1, F>(s, lines, tri);
+    }
+}
+
+// The last pass's unit at p (quarter H, R elements at padc(H*i)), computed
+// into e without storing.
+template <bool INV, int H, int R, bool F>
+__device__ __forceinline__ void last_unit(const float2 *p, const float2 *__restrict__ tri, int j, float2 *e) {
+#pragma unroll
+    for (int i = 0; i < R; i++) e[i] = p[padc(H * i)];
+    if constexpr (R == 16) {
+        const float2 *tA = tri + j, *tB = tri + 3 * H + j;
+        const float2 a1 = __ldg(tA), a2 = __ldg(tA + H), a3 = __ldg(tA + 2 * H);
+#pragma unroll
+        for (int b = 0; b < 4; b++) bfly4<INV, F>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            bfly4<INV, F>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
+                          __ldg(tB + 8 * H + H * q));
+    } else {
+        const float2 *t = tri + j;
+        bfly4<INV, F>(&e[0], &e[1], &e[2], &e[3], __ldg(t), __ldg(t + H), __ldg(t + 2 * H));
+    }
+}
+
 // floor(line / cn) for cn in 1..4 and line < 2^15.
 __device__ __forceinline__ int div_cn(int line, int cn) {
     const int magic = cn == 1 ? 65536 : (cn == 2 ? 32768 : (cn == 3 ? 21846 : 16384));
@@ -316,6 +379,12 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 smem[tid * LD + padi(brevn<LOG2N>(HALF))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
             }
             __syncthreads();
+            if constexpr (FAST && last_pass_r(LOG2N) == 4) {
+                // one channel, a radix-4 last pass: it runs in the epilogue,
+                // which scores its outputs from registers
+                line_fft_but_last<true, LOG2N, true>(smem, P, fc.triW);
+                break;
+            }
             line_fft<true, LOG2N, FAST>(smem, P, fc.triW);
             if (fast) break;  // one channel: the epilogue reads the transformed lines directly
             for (int p = 0; p < P; p++) {
@@ -352,7 +421,62 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
         }
         return;
     }
-    if (P > 0) {
+    if (FAST && last_pass_r(LOG2N) == 4 && P > 0 && !flat) {
+        // The last pass of every line, each unit's outputs scored straight
+        // from registers: x = base + H*i of line p are results x of rows 2p
+        // (real part) and 2p+1 (imaginary part).  A thread owns at most one
+        // unit per line and visits lines in order, so its results ascend in
+        // raster order (ext_add_inc).
+        constexpr int LH = last_pass_h(LOG2N), LR = last_pass_r(LOG2N);
+        constexpr int LLR = LR == 16 ? 4 : 2, LLH = ilog2c(LH), LU = LOG2N - LLR;
+        constexpr int OFF = (LOG2N & 1) ? LH - 2 : LH - 1;
+        const float *dens = reinterpret_cast<const float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride);
+        float *map = a.ms.map;
+        const int xlo = m.roiX0 - tb.x0, xhi = m.roiX1 - tb.x0;
+        for (int u = tid; u < (P << LU); u += kThreads) {
+            const int line = u >> LU, v = u & ((1 << LU) - 1);
+            const int j = v & (LH - 1), base = ((v >> LLH) << (LLH + LLR)) + j;
+            // the unit's den values first: their loads overlap its butterflies
+            long long rowBase[2];
+            float dv[2][LR];
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                const int yy = tb.y0 + 2 * (pair0 + line) + half;
+                rowBase[half] = (long long)yy * m.rw + tb.x0;
+#pragma unroll
+                for (int i = 0; i < LR; i++) {
+                    const int x = base + LH * i;
+                    dv[half][i] = (x < bw && 2 * (pair0 + line) + half < bh) ? __ldg(dens + rowBase[half] + x) : 0.f;
+                }
+            }
+            float2 z[LR];
+            last_unit<true, LH, LR, true>(smem + line * LD + padi(base), fc.triW + OFF, j, z);
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                const int r = 2 * (pair0 + line) + half;
+                if (r >= bh) break;
+                const int yy = tb.y0 + r;
+                if (yy < m.roiY0 || yy >= m.roiY1) continue;
+#pragma unroll
+                for (int i = 0; i < LR; i++) {
+                    const int x = base + LH * i;
+                    if (x < bw) {
+                        const float num = half ? z[i].y : z[i].x;
+                        const float den = dv[half][i], an = fabsf(num);
+                        float score;
+                        if (an < den)
+                            score = __fdividef(num, den);
+                        else if (an < __fmul_rn(den, 1.125f))
+                            score = num > 0.f ? 1.f : -1.f;
+                        else
+                            score = 0.f;
+                        if (map) map[rowBase[half] + x] = score;
+                        if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase[half] + x);
+                    }
+                }
+            }
+        }
+    } else if (P > 0) {
         const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
         float *map = a.ms.map;
         const int xlo = m.roiX0 - tb.x0, xhi = m.roiX1 - tb.x0;
