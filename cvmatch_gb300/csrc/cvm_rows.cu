@@ -350,6 +350,9 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     ext_init(e);
     // the fast form's scratch holds one channel-summed correlation per tile
     constexpr bool fast = FAST;
+    // a radix-4 last pass is fused with the scoring (both forms; not for
+    // the fixed-scratch entry point, which takes the raw correlation)
+    const bool fuse = last_pass_r(LOG2N) == 4 && a.ms.lanes != nullptr;
     if (P > 0 && !flat) {
         const int cn = fast ? 1 : Pm.cn;
         const size_t chanStride = (size_t)fc.dftH * hwp;
@@ -379,10 +382,10 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 smem[tid * LD + padi(brevn<LOG2N>(HALF))] = make_float2(__fsub_rn(u.x, v.y), __fadd_rn(u.y, v.x));
             }
             __syncthreads();
-            if constexpr (FAST && last_pass_r(LOG2N) == 4) {
-                // one channel, a radix-4 last pass: it runs in the epilogue,
-                // which scores its outputs from registers
-                line_fft_but_last<true, LOG2N, true>(smem, P, fc.triW);
+            if (fuse && k == cn - 1) {
+                // the last channel's last pass runs in the epilogue, which
+                // finishes the channel sum and scores from registers
+                line_fft_but_last<true, LOG2N, FAST>(smem, P, fc.triW);
                 break;
             }
             line_fft<true, LOG2N, FAST>(smem, P, fc.triW);
@@ -421,24 +424,29 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
         }
         return;
     }
-    if (FAST && last_pass_r(LOG2N) == 4 && P > 0 && !flat) {
+    if (fuse && P > 0 && !flat) {
         // The last pass of every line, each unit's outputs scored straight
         // from registers: x = base + H*i of line p are results x of rows 2p
         // (real part) and 2p+1 (imaginary part).  A thread owns at most one
         // unit per line and visits lines in order, so its results ascend in
-        // raster order (ext_add_inc).
+        // raster order (ext_add_inc).  The exact form adds the earlier
+        // channels' sum to the last channel's output (the accumulation's
+        // own rounded add, in channel order) and subtracts t, as the
+        // unfused epilogue does.
         constexpr int LH = last_pass_h(LOG2N), LR = last_pass_r(LOG2N);
         constexpr int LLR = LR == 16 ? 4 : 2, LLH = ilog2c(LH), LU = LOG2N - LLR;
         constexpr int OFF = (LOG2N & 1) ? LH - 2 : LH - 1;
-        const float *dens = reinterpret_cast<const float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride);
+        const float2 *lanes = a.ms.lanes + (size_t)slot * a.ms.lanesStride;
+        const float *dens = reinterpret_cast<const float *>(lanes);
+        const int cnSum = FAST ? 1 : Pm.cn;
         float *map = a.ms.map;
         const int xlo = m.roiX0 - tb.x0, xhi = m.roiX1 - tb.x0;
         for (int u = tid; u < (P << LU); u += kThreads) {
             const int line = u >> LU, v = u & ((1 << LU) - 1);
             const int j = v & (LH - 1), base = ((v >> LLH) << (LLH + LLR)) + j;
-            // the unit's den values first: their loads overlap its butterflies
+            // the unit's (t, den) values first: their loads overlap its butterflies
             long long rowBase[2];
-            float dv[2][LR];
+            float2 dv[2][LR];
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 const int yy = tb.y0 + 2 * (pair0 + line) + half;
@@ -446,11 +454,15 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
 #pragma unroll
                 for (int i = 0; i < LR; i++) {
                     const int x = base + LH * i;
-                    dv[half][i] = (x < bw && 2 * (pair0 + line) + half < bh) ? __ldg(dens + rowBase[half] + x) : 0.f;
+                    const bool in = x < bw && 2 * (pair0 + line) + half < bh;
+                    if (FAST)
+                        dv[half][i] = make_float2(0.f, in ? __ldg(dens + rowBase[half] + x) : 0.f);
+                    else
+                        dv[half][i] = in ? __ldg(lanes + rowBase[half] + x) : make_float2(0.f, 0.f);
                 }
             }
             float2 z[LR];
-            last_unit<true, LH, LR, true>(smem + line * LD + padi(base), fc.triW + OFF, j, z);
+            last_unit<true, LH, LR, FAST>(smem + line * LD + padi(base), fc.triW + OFF, j, z);
 #pragma unroll
             for (int half = 0; half < 2; half++) {
                 const int r = 2 * (pair0 + line) + half;
@@ -461,11 +473,15 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
                 for (int i = 0; i < LR; i++) {
                     const int x = base + LH * i;
                     if (x < bw) {
-                        const float num = half ? z[i].y : z[i].x;
-                        const float den = dv[half][i], an = fabsf(num);
+                        float num = half ? z[i].y : z[i].x;
+                        if (!FAST) {
+                            if (cnSum > 1) num = __fadd_rn(acc[(size_t)(2 * line + half) * N + x], num);
+                            num = __fsub_rn(num, dv[half][i].x);
+                        }
+                        const float den = dv[half][i].y, an = fabsf(num);
                         float score;
                         if (an < den)
-                            score = __fdividef(num, den);
+                            score = FAST ? __fdividef(num, den) : __fdiv_rn(num, den);
                         else if (an < __fmul_rn(den, 1.125f))
                             score = num > 0.f ? 1.f : -1.f;
                         else
