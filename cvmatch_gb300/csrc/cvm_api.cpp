@@ -124,6 +124,7 @@ cudaStream_t thread_stream() {
 // while the caller's stream takes the template and the small setup.
 struct SideStream {
     cudaStream_t st = nullptr, st2 = nullptr;
+    cudaStream_t stats = nullptr;  // a colour match's window statistics, at the caller's priority
     cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr, frame = nullptr;
 };
 
@@ -138,6 +139,7 @@ SideStream &side_stream() {
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
         cudaStreamCreateWithPriority(&s.st, cudaStreamNonBlocking, greatest);
         cudaStreamCreateWithPriority(&s.st2, cudaStreamNonBlocking, greatest < least ? greatest + 1 : greatest);
+        cudaStreamCreateWithPriority(&s.stats, cudaStreamNonBlocking, least);
         cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
@@ -419,12 +421,21 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
                          J.cnFixed, F, st));
+    // A fast-form colour match with a short template (the fused column pass
+    // dominates; the statistics have slack until the inverse rows) queues its
+    // statistics after the frame's row transform, at the caller's priority,
+    // so they fill the SMs the transforms leave instead of displacing the
+    // row transform; otherwise they start at once, above it.
+    const bool statsLate = fastSum && J.th <= 64;
+    cudaStream_t sst = statsLate ? ss.stats : ss.st2;
     CVM_CUDA(cudaEventRecord(ss.fork, st));
     CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
-    CVM_CUDA(cudaStreamWaitEvent(ss.st2, ss.fork, 0));
-    CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg, J.mode == 1 ? 3 : J.cnFixed,
-                              J.mode == 1 ? 4 : J.cnFixed, H, 0, ss.st2));
-    CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
+    CVM_CUDA(cudaStreamWaitEvent(sst, ss.fork, 0));
+    if (!statsLate) {
+        CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
+                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst));
+        CVM_CUDA(cudaEventRecord(ss.joinStats, sst));
+    }
     if (!J.cachedP)
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st,
                             nullptr, fast ? P->tsum : nullptr));
@@ -434,6 +445,11 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     for (int c = 0; c < G->nclass; c++)
         CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0, nullptr,
                                  1.0f, fast ? off : nullptr));
+    if (statsLate) {
+        CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
+                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst));
+        CVM_CUDA(cudaEventRecord(ss.joinStats, sst));
+    }
     // Several channels, fast form: transforms up to 512 tall run every
     // channel of a column strip in one CTA (mode 4: forward, channel sum of
     // the conj-products, one inverse); taller ones store the forward
