@@ -126,6 +126,7 @@ struct SideStream {
     cudaStream_t st = nullptr, st2 = nullptr;
     cudaStream_t stats = nullptr;  // a colour match's window statistics, at the caller's priority
     cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr, frame = nullptr;
+    cudaEvent_t hsumDone = nullptr;  // a late statistics chain's horizontal sums
 };
 
 SideStream &side_stream() {
@@ -144,6 +145,7 @@ SideStream &side_stream() {
         cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.frame, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.hsumDone, cudaEventDisableTiming);
     }
     return s;
 }
@@ -446,9 +448,13 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0, nullptr,
                                  1.0f, fast ? off : nullptr));
     if (statsLate) {
+        // the horizontal sums at the caller's priority, the vertical pass
+        // (which gates the inverse rows) back above it on the second side stream
+        CVM_CUDA(cudaStreamWaitEvent(ss.st2, ss.fork, 0));
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
-                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst));
-        CVM_CUDA(cudaEventRecord(ss.joinStats, sst));
+                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst, 0, ss.st2,
+                                  ss.hsumDone));
+        CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
     }
     // Several channels, fast form: transforms up to 512 tall run every
     // channel of a column strip in one CTA (mode 4: forward, channel sum of

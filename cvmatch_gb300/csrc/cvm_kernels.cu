@@ -2069,7 +2069,8 @@ static int vstat_band(const SepGrid &sg, int nmembers) {
 
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
-                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix) {
+                             unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix,
+                             cudaStream_t vst, cudaEvent_t vev) {
     // a shared 4-channel prefix keeps its (s3, alpha squares) block after
     // the ih x hp x 4 main block (launch_row_prefix)
     HsumArgs h;
@@ -2125,6 +2126,13 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
             set_smem(k_hsum<4, 4>, smem);
             k_hsum<4, 4><<<gh, kThreads, smem, st>>>(h);
         }
+    }
+    if (vst && vev) {
+        // the vertical pass on its own stream, after the horizontal sums
+        cudaError_t e = cudaEventRecord(vev, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(vst, vev, 0);
+        if (e != cudaSuccess) return e;
+        st = vst;
     }
     {
         ProfScope ps("k_vstats", st);
