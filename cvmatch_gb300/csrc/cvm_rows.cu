@@ -273,7 +273,6 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
             if (g < cn) d[g * LD] = make_float2(va[g], vb[g]);
     }
     __syncthreads();
-    line_fft<false, LOG2N, F>(smem, lines, fc.triW);
     // Untangle (impl.go:331-341) into the two real-row spectra at their
     // bit-reversed column-transform slots.
     const int hwp = fc.hwp, log2H = fc.log2H;
@@ -286,6 +285,50 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
         ra = cb + (size_t)brev_bits(r, log2H) * hwp;
         rb = cb + (size_t)brev_bits(r + 1, log2H) * hwp;
     };
+    // spectrum column kk of both rows from z[kk] and its mirror n = z[(N - kk) mod N]
+    auto emit = [&](float2 *ra, float2 *rb, int kk, float2 z, float2 n) {
+        ra[kk] = make_float2(__fmul_rn(0.5f, __fadd_rn(z.x, n.x)), __fmul_rn(0.5f, __fsub_rn(z.y, n.y)));
+        rb[kk] = make_float2(__fmul_rn(0.5f, __fadd_rn(z.y, n.y)), __fmul_rn(0.5f, __fsub_rn(n.x, z.x)));
+    };
+    if constexpr (last_pass_r(LOG2N) == 4) {
+        // A radix-4 last pass (quarter H = N/4) fused with the untangle: unit
+        // j holds z[j + H*i], and the mirror of each of its outputs below N/2
+        // lies in unit H - j, so one item runs units j and H - j and writes
+        // their four columns of both rows from registers (j = 0 and j = H/2
+        // are their own mirrors; unit 0 also holds z[N/2]).  The same rounded
+        // operations as the separate pass and untangle.
+        line_fft_but_last<false, LOG2N, F>(smem, lines, fc.triW);
+        constexpr int H = last_pass_h(LOG2N), OFF = (LOG2N & 1) ? H - 2 : H - 1, PER = H / 2 + 1;
+        const float2 *tri = fc.triW + OFF;
+        for (int it = tid; it < lines * PER; it += nt) {
+            const int line = it / PER, j = it - line * PER;
+            float2 *ra, *rb;
+            rows(line, ra, rb);
+            const float2 *zl = smem + line * LD;
+            float2 za[4];
+            last_unit<false, H, 4, F>(zl + padi(j), tri, j, za);
+            if (j == 0) {
+                emit(ra, rb, 0, za[0], za[0]);
+                emit(ra, rb, H, za[1], za[3]);
+                const float2 zk = za[2];  // kk = N/2
+                ra[HALF] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.x, zk.x)), __fmul_rn(0.5f, __fsub_rn(zk.y, zk.y)));
+                rb[HALF] = make_float2(__fmul_rn(0.5f, __fadd_rn(zk.y, zk.y)), __fmul_rn(0.5f, __fsub_rn(zk.x, zk.x)));
+            } else if (j == H / 2) {
+                emit(ra, rb, j, za[0], za[3]);
+                emit(ra, rb, j + H, za[1], za[2]);
+            } else {
+                const int jp = H - j;
+                float2 zb[4];
+                last_unit<false, H, 4, F>(zl + padi(jp), tri, jp, zb);
+                emit(ra, rb, j, za[0], zb[3]);
+                emit(ra, rb, j + H, za[1], zb[2]);
+                emit(ra, rb, jp, zb[0], za[3]);
+                emit(ra, rb, jp + H, zb[1], za[2]);
+            }
+        }
+        return;
+    }
+    line_fft<false, LOG2N, F>(smem, lines, fc.triW);
     // two spectrum columns kk, kk+1 per item: one 16-byte store per row
     for (int it = tid; it < (lines << (LOG2N - 2)); it += nt) {
         const int line = it >> (LOG2N - 2), kk = 2 * (it & (HALF / 2 - 1));
