@@ -311,3 +311,40 @@ def test_fast_form_refuses_transforms_above_4096(fast_form):
     cvm.SetForm(cvm.FORM_EXACT)
     t, _ = cvm.match_u8(img, tpl, 4, want_map=False)
     assert (t[4], t[5]) == (50, 11)
+
+
+# ------------------------------------------ plan classes and buckets, fast form
+
+
+def test_fast_shrunk_last_band_solo_and_fleet(fast_form):
+    """A 64x48 template on a 337x292 frame plans 256x128 tiles whose last
+    band is shrunk to 64 rows (a second plan class, shrinkDH,
+    impl.go:573-582): the one-shot map and the fleet member (its own bucket)
+    against FP64."""
+    img = scene(83, 292, 337)
+    t = img[120:168, 200:264].copy()
+    p = oracle.plan(64, 48, 337 - 63, 292 - 47)
+    assert oracle.shrink_dh(p, 292 - 47, 48) > 0
+    m, _, _ = cvm.MatchMap(img, t)
+    m64 = oracle.ref_match_f64(img, t, 3, threads=16)
+    map_check(m, m64, "shrunk last band, one-shot")
+    small = img[10:30, 20:44].copy()
+    fleet = cvm.NewFleet(cvm.NewMatcher(t), cvm.NewMatcher(small))
+    fleet.SetForm(cvm.FORM_FAST)
+    got = fleet.FindAll(img)
+    check(got[0], m64, "shrunk last band, fleet member")
+    check(got[1], oracle.ref_match_f64(img, small, 3, threads=16), "fleet member in the same bucket")
+    assert (got[0].MaxX, got[0].MaxY) == (200, 120)
+
+
+def test_fast_fleet_several_buckets(fast_form):
+    """Wide, tall and square members fall into different buckets (bucketize,
+    fleet.go:111-171), each with its own plan and frame spectra."""
+    img = scene(89, 260, 400)
+    tpls = [img[40:48, 52:352].copy(), img[30:230, 300:308].copy(), img[100:140, 100:140].copy(),
+            img[10:26, 10:26].copy()]
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    fleet.SetForm(cvm.FORM_FAST)
+    got = fleet.FindAll(img)
+    for i, t in enumerate(tpls):
+        check(got[i], oracle.ref_match_f64(img, t, 3, threads=16), f"bucket member {i} {t.shape[1]}x{t.shape[0]}")
