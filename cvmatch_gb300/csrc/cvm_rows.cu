@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
 // the epilogue scores with the per-result (t, den) lanes and keeps
 // first-occurrence extrema merged by each member's last CTA.
 template <int LOG2N, bool FAST>
-__global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
+__global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 3) k_inv_rows_t(InvArgs a) {
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     constexpr int XIT = (N + kThreads - 1) / kThreads;  // result columns per thread
     extern __shared__ float2 smem[];
@@ -395,7 +395,9 @@ __global__ void __launch_bounds__(256, 3) k_inv_rows_t(InvArgs a) {
     constexpr bool fast = FAST;
     // a radix-4 last pass is fused with the scoring (both forms; not for
     // the fixed-scratch entry point, which takes the raw correlation)
-    const bool fuse = last_pass_r(LOG2N) == 4 && a.ms.lanes != nullptr;
+    // (a radix-16 last pass only in the fast form, which budgets the
+    // registers for it: two CTAs per SM)
+    const bool fuse = (last_pass_r(LOG2N) == 4 || FAST) && a.ms.lanes != nullptr;
     if (P > 0 && !flat) {
         const int cn = fast ? 1 : Pm.cn;
         const size_t chanStride = (size_t)fc.dftH * hwp;
