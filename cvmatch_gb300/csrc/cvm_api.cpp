@@ -285,19 +285,19 @@ size_t tspec_elems(const FftClass &f, int cnS) { return (size_t)cnS * f.dftH * f
 // sum(I*T) - sum(I)*sum(T)/area directly.
 int build_tspec(const Geom &G, const uint8_t *d_tpl, long long tstride, int step, int tw, int th,
                 int cnS, const int *cnDev, float2 *ts0, float2 *ts1, cudaStream_t st,
-                const int64_t *tsum = nullptr, const unsigned long long *tsumDev = nullptr) {
+                const int64_t *tsum = nullptr, const unsigned long long *tsumDev = nullptr, int selfSums = 0) {
     TileGeom tg;
     FftClass tf;
     template_geom(G, tw, th, tg, tf);
     float mul = 1.0f, sub[4] = {0.f, 0.f, 0.f, 0.f};
     const double area = double(tw) * double(th);
     const bool exact = area * 255.0 < 16777216.0;
-    if (tsum || tsumDev) mul = exact ? float(area) : 1.0f;
+    if (tsum || tsumDev || selfSums) mul = exact ? float(area) : 1.0f;
     if (tsum)
         for (int k = 0; k < 4; k++) sub[k] = exact ? float(tsum[k]) : float(double(tsum[k]) / area);
     // sums on the device (one-shot calls): sub = tsum / (1 or area)
     CVM_CUDA(launch_fwd_rows(d_tpl, tstride, step, cnS, cnDev, tg, tf, ts0, cnS, st, 0, "k_fwd_rows_tpl", mul,
-                             tsum ? sub : nullptr, tsumDev, exact ? 1.0f : float(area)));
+                             tsum ? sub : nullptr, tsumDev, exact ? 1.0f : float(area), selfSums));
     const float scale = float(1.0 / (double(G.p.dftW) * double(G.p.dftH) * double(mul)));
     MemberSet none;
     memset(&none, 0, sizeof none);
@@ -419,6 +419,22 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     // not get SMs back from one that did (priority orders only the CTAs
     // waiting for a slot), so the gating statistics launch goes first.
     SideStream &ss = side_stream();
+    // A one-shot colour match on a device-resident frame starts its template
+    // spectrum at once, beside the statistics launch: all four channels
+    // (the frame's alpha plane decides later whether the fourth is used)
+    // and, in the fast form, the zero-mean samples from sums the row kernel
+    // takes itself -- the spectrum depends on nothing the statistics launch
+    // computes.  (With a host frame in flight the same early chain measured
+    // slower end to end, with the ingest kernel and with the copy engine
+    // alike: host-buffer calls keep the template behind the frame.)
+    const bool early = !J.frameOnSide && !J.cachedP && J.mode == 1 && (long long)J.tw * J.th <= 65536;
+    if (early) {
+        CVM_CUDA(cudaEventRecord(ss.fork, st));  // the template and the pool's spectrum buffers
+        CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
+        CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, nullptr, tsOwn[0], tsOwn[1], ss.st,
+                            nullptr, nullptr, fast ? 1 : 0));
+        CVM_CUDA(cudaEventRecord(ss.join, ss.st));
+    }
     if (J.frameOnSide) CVM_CUDA(cudaStreamWaitEvent(st, ss.frame, 0));
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
@@ -431,17 +447,17 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     const bool statsLate = fastSum && J.th <= 64;
     cudaStream_t sst = statsLate ? ss.stats : ss.st2;
     CVM_CUDA(cudaEventRecord(ss.fork, st));
-    CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
+    if (!early) CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
     CVM_CUDA(cudaStreamWaitEvent(sst, ss.fork, 0));
     if (!statsLate) {
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
                                   J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst));
         CVM_CUDA(cudaEventRecord(ss.joinStats, sst));
     }
-    if (!J.cachedP)
+    if (!J.cachedP && !early)
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st,
                             nullptr, fast ? P->tsum : nullptr));
-    CVM_CUDA(cudaEventRecord(ss.join, ss.st));
+    if (!early) CVM_CUDA(cudaEventRecord(ss.join, ss.st));
     // the fast form transforms the frame offset by -128 (zero-mean templates)
     const float off[4] = {128.f, 128.f, 128.f, 128.f};
     for (int c = 0; c < G->nclass; c++)

@@ -92,6 +92,10 @@ struct FwdRowsArgs {
     const unsigned long long *subSums;
     float subDiv;
     int fma;                 // the fast form's samples: fused twiddle products
+    // the fast form's zero-mean template without its sums on the device:
+    // every CTA sums the template (this launch's one tile) itself, and
+    // sub[k] = sum_k / subDiv
+    int selfSums;
 };
 
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).

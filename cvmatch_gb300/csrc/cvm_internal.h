@@ -142,7 +142,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
                             int cnS, cudaStream_t st, int chanFirst = 0, const char *label = nullptr,
                             float mul = 1.0f, const float *sub = nullptr,
-                            const unsigned long long *subSums = nullptr, float subDiv = 1.0f);
+                            const unsigned long long *subSums = nullptr, float subDiv = 1.0f, int selfSums = 0);
 // Column pass.  mode 0: forward only, natural output (template spectra with
 // `scale`, fleet frame caches), channels from cnDev; mode 1: forward +
 // conj-multiply + inverse, in place on the members' scratch (solo match);

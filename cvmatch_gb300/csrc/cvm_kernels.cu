@@ -1811,7 +1811,7 @@ cudaError_t launch_prep(const uint8_t *tpl, long long tstride, int tw, int th, i
 cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int chanCount,
                             const int *cnDev, const TileGeom &g, const FftClass &fc, float2 *spec,
                             int cnS, cudaStream_t st, int chanFirst, const char *label, float mul,
-                            const float *sub, const unsigned long long *subSums, float subDiv) {
+                            const float *sub, const unsigned long long *subSums, float subDiv, int selfSums) {
     // Channels per launch so that one row pair of the group fits 128 KB of
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
@@ -1850,9 +1850,10 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         for (int k = 0; k < 4; k++) a.sub[k] = sub ? sub[k] : 0.0f;
         a.subSums = subSums;
         a.subDiv = subDiv;
+        a.selfSums = selfSums;
         // a sample transform marks the fast form (the exact form packs the
         // reference's samples untouched): its butterflies may fuse
-        a.fma = (mul != 1.0f || sub || subSums) ? 1 : 0;
+        a.fma = (mul != 1.0f || sub || subSums || selfSums) ? 1 : 0;
         for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
             a.chanFirst = c0;
             launch_fwd_rows_fixed(a, grid, threads, smem, st);
@@ -1860,7 +1861,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         }
         return cudaGetLastError();
     }
-    if (mul != 1.0f || sub || subSums) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
+    if (mul != 1.0f || sub || subSums || selfSums) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
     set_smem(k_fwd_rows, smem);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
         k_fwd_rows<<<grid, threads, smem, st>>>(img, istride, step, chanCount, cnDev, c0, group, g, fc,

@@ -230,8 +230,36 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
     const long long istride = a.istride;
     const uint8_t *img0 = a.img + (long long)(b.y0 + 2 * pair0) * istride + (long long)b.x0 * a.step;
     float subv[4];
+    if (a.selfSums) {
+        // the template's own channel sums (this launch's one tile is the
+        // whole template): exact integers, reduced per warp then per CTA
+        __shared__ unsigned long long ssum[4];
+        if (tid < 4) ssum[tid] = 0ull;
+        __syncthreads();
+        unsigned long long sv[4] = {0ull, 0ull, 0ull, 0ull};
+        const uint8_t *t0 = a.img + (long long)b.y0 * istride + (long long)b.x0 * a.step;
+        const int npx = b.loadW * b.loadH;
+        for (int i = tid; i < npx; i += nt) {
+            const int y = i / b.loadW, x = i - y * b.loadW;
+            const uint8_t *q = t0 + (long long)y * istride + (long long)x * a.step;
 #pragma unroll
-    for (int g = 0; g < 4; g++) subv[g] = a.subSums ? __fdiv_rn(__ull2float_rn(a.subSums[g]), a.subDiv) : a.sub[g];
+            for (int c = 0; c < 4; c++)
+                if (c < a.step) sv[c] += q[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sv[c] += __shfl_down_sync(0xffffffffu, sv[c], o);
+            if ((tid & 31) == 0 && sv[c]) atomicAdd(&ssum[c], sv[c]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 4; c++) subv[c] = __fdiv_rn(__ull2float_rn(ssum[c]), a.subDiv);
+    } else {
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+            subv[g] = a.subSums ? __fdiv_rn(__ull2float_rn(a.subSums[g]), a.subDiv) : a.sub[g];
+    }
     // Pack rows r (real part) and r+1 (imaginary part) of every channel of
     // the group, each pixel read once for all of them.
     for (int it = tid; it < (P << LOG2N); it += nt) {
