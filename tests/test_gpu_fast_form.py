@@ -348,3 +348,35 @@ def test_fast_fleet_several_buckets(fast_form):
     got = fleet.FindAll(img)
     for i, t in enumerate(tpls):
         check(got[i], oracle.ref_match_f64(img, t, 3, threads=16), f"bucket member {i} {t.shape[1]}x{t.shape[0]}")
+
+
+@pytest.mark.parametrize("alpha", ["const", "template", "parent"])
+def test_fast_device_resident_colour_match(fast_form, alpha):
+    """cvm_match_device in the fast form (its template spectrum starts
+    beside the statistics launch, all four channels, from sums the row
+    kernel takes itself) with constant alpha planes (cn 3) or a template
+    or parent alpha plane that varies (cn 4), against FP64."""
+    torch = pytest.importorskip("torch")
+    L = cvm.lib()
+    img = scene(97, 210, 330)
+    t = img[60:100, 120:168].copy()
+    if alpha == "template":
+        t[::3, ::2, 3] = 9
+    if alpha == "parent":
+        img[5, 7, 3] = 3
+    cn = 3 if alpha == "const" else 4
+    th, tw = t.shape[:2]
+    rw, rh = img.shape[1] - tw + 1, img.shape[0] - th + 1
+    d_img, d_tpl = torch.from_numpy(img).cuda(), torch.from_numpy(t).cuda()
+    d_map = torch.empty((rh, rw), dtype=torch.float32, device="cuda")
+    d_out = torch.zeros(6, dtype=torch.int32, device="cuda")
+    for _ in range(2):  # the second call reuses the pooled buffers
+        rc = L.cvm_match_device(d_img.data_ptr(), img.strides[0], img.shape[1], img.shape[0], d_tpl.data_ptr(),
+                                t.strides[0], tw, th, d_map.data_ptr(), d_out.data_ptr(),
+                                torch.cuda.current_stream().cuda_stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        m = d_map.cpu().numpy()
+        map_check(m, oracle.ref_match_f64(img, t, cn, threads=16), f"device-resident, alpha {alpha}")
+        jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
+        assert (jx, jy) == (120, 60)
