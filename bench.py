@@ -847,6 +847,9 @@ def run_gpu_secondary(args):
     rows = profile_kernels(L, step_dev, torch, reps=3)
     tot = sum(r[1] for r in rows) or 1.0
     line["kernels"] = {nm: {"ms_per_launch": t / max(n, 1), "launches": n, "share": t / tot} for nm, t, n in rows}
+    if args.timeline:
+        for nm, a, b in timeline(L, step_dev, torch):
+            sys.stderr.write(f"timeline {nm:24s} {a:8.1f} {b:8.1f} us\n")
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample()
     print(json.dumps(line))

@@ -349,9 +349,12 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         nparts += G->fc[c].ntiles * inv_rows_ctas_per_tile(G->fc[c], G->g.blockH, &P);
     }
     const size_t hElems = (size_t)stat_pitch(cnS) * J.ih * sg.hp;
+    // a tall template with a fixed channel count: 16-row block sums of the
+    // window sums, from which every vertical band starts
+    const size_t bElems = (J.mode == 0 && J.th >= 64) ? (size_t)stat_pitch(J.cnFixed) * (J.ih / 16) * sg.hp : 0;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                    Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
-                   Arena::bytes((size_t)rw * rh, sizeof(float2));
+                   Arena::bytes((size_t)rw * rh, sizeof(float2)) + (bElems ? Arena::bytes(bElems, sizeof(unsigned int)) : 0);
     const bool fast = J.form != CVM_FORM_EXACT;
     // one channel: the fused forward + conj-multiply + inverse column pass
     // already yields the single correlation spectrum the fast form sums to
@@ -374,6 +377,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     DevFrame *F = A.take<DevFrame>(1);
     Partial *parts = A.take<Partial>(nparts);
     unsigned int *H = A.take<unsigned int>(hElems);
+    unsigned int *blk = bElems ? A.take<unsigned int>(bElems) : nullptr;
     float2 *lanes = A.take<float2>((size_t)rw * rh);
     float2 *spec[2] = {nullptr, nullptr}, *sum[2] = {nullptr, nullptr};
     const float2 *ts[2] = {J.cachedTs[0], J.cachedTs[1]};
@@ -451,7 +455,8 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     CVM_CUDA(cudaStreamWaitEvent(sst, ss.fork, 0));
     if (!statsLate) {
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
-                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst));
+                                  J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst, 0, nullptr,
+                                  nullptr, blk));
         CVM_CUDA(cudaEventRecord(ss.joinStats, sst));
     }
     if (!J.cachedP && !early)

@@ -1536,7 +1536,28 @@ struct VstatArgs {
     int hp;
     MemberSet ms;
     int BV;
+    // one match with a tall template: the window sums summed over 16-row
+    // blocks (row b = H rows 16b .. 16b+15, H's layout), so a band starts
+    // from th/16 block rows and at most 15 single rows (nullptr: none)
+    const unsigned int *blk;
 };
+
+// The 16-row block sums of one match's horizontal window sums (u32,
+// modular like H: every sum the slide forms from them is exact).
+__global__ void k_vblock(const unsigned int *__restrict__ H, unsigned int *__restrict__ B, int nblk,
+                         size_t rowElems) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (e >= rowElems || b >= nblk) return;
+    const unsigned int *h = H + (size_t)b * 16 * rowElems + e;
+    unsigned int v[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __ldg(h + (size_t)i * rowElems);
+    unsigned int sum = 0u;
+#pragma unroll
+    for (int i = 0; i < 16; i++) sum += v[i];
+    B[(size_t)b * rowElems + e] = sum;
+}
 
 // PRE: H is the shared row prefix built for PCN channels (window sum =
 // P[x+tw] - P[x]); its squares are plane PCN (PCN < 4) or planes 4 (RGB)
@@ -1598,8 +1619,21 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
     unsigned long long q = 0;
 #pragma unroll
     for (int k = 0; k < CN; k++) s[k] = 0u;
+    int dy0 = 0;
+    if (!PRE && a.blk) {
+        // whole 16-row blocks first (Y0 is a multiple of 16: BV is)
+        const unsigned int *Bx = a.blk + (size_t)x * NP;
+#pragma unroll 4
+        for (; dy0 + 16 <= th; dy0 += 16) {
+            unsigned int hv[CN + 1];
+            rowvals(Bx + (size_t)((Y0 + dy0) >> 4) * rp, hv);
+#pragma unroll
+            for (int k = 0; k < CN; k++) s[k] += hv[k];
+            q += hv[CN];
+        }
+    }
 #pragma unroll(PRE ? 4 : 8)
-    for (int dy = 0; dy < th; dy++) {
+    for (int dy = dy0; dy < th; dy++) {
         unsigned int hv[CN + 1];
         rowvals(H + (size_t)(Y0 + dy) * rp, hv);
 #pragma unroll
@@ -2071,7 +2105,7 @@ static int vstat_band(const SepGrid &sg, int nmembers) {
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
                              unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix,
-                             cudaStream_t vst, cudaEvent_t vev) {
+                             cudaStream_t vst, cudaEvent_t vev, unsigned int *blk) {
     // a shared 4-channel prefix keeps its (s3, alpha squares) block after
     // the ih x hp x 4 main block (launch_row_prefix)
     HsumArgs h;
@@ -2096,6 +2130,7 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     v.hp = sg.hp;
     v.ms = ms;
     v.BV = vstat_band(sg, nmembers);
+    v.blk = nullptr;
     // One match: every band first sums th rows, so a tall template wants
     // tall bands (up to th / 2 rows, while ~8 warps per SM remain), and
     // narrower CTAs when the taller bands leave fewer than ~3 per SM.
@@ -2103,8 +2138,14 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
     if (!sharedPrefix && !ms.table) {
         const long long warpCols = (soloRw + 31) / 32;
         int BV = 16;
-        while (BV < 128 && 4 * BV <= ms.solo.th && warpCols * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) >= 8 * 152)
-            BV *= 2;
+        if (blk) {
+            // the band starts from block sums: short bands, many of them
+            v.blk = blk;
+            BV = 32;
+        } else {
+            while (BV < 128 && 4 * BV <= ms.solo.th && warpCols * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) >= 8 * 152)
+                BV *= 2;
+        }
         v.BV = BV;
         while (VT > 64 && (long long)((soloRw + VT - 1) / VT) * ((sg.rhMax + BV - 1) / BV) < 3 * 152) VT >>= 1;
         ncx = (soloRw + VT - 1) / VT;
@@ -2126,6 +2167,16 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
         } else {
             set_smem(k_hsum<4, 4>, smem);
             k_hsum<4, 4><<<gh, kThreads, smem, st>>>(h);
+        }
+    }
+    if (v.blk) {
+        ProfScope ps("k_vblock", st);
+        const size_t rowElems = (size_t)sg.hp * stat_pitch(cnMax);
+        const int nblk = ih / 16;
+        if (nblk > 0) {
+            k_vblock<<<dim3((unsigned)((rowElems + kThreads - 1) / kThreads), nblk), kThreads, 0, st>>>(
+                H, blk, nblk, rowElems);
+            count_launches(1);
         }
     }
     if (vst && vev) {
