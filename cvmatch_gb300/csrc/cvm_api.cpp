@@ -474,7 +474,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         CVM_CUDA(cudaStreamWaitEvent(ss.st2, ss.fork, 0));
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
                                   J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst, 0, ss.st2,
-                                  ss.hsumDone));
+                                  ss.hsumDone, blk));
         CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
     }
     // Several channels, fast form: transforms up to 512 tall run every

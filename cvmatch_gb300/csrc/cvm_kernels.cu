@@ -2169,6 +2169,13 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
             k_hsum<4, 4><<<gh, kThreads, smem, st>>>(h);
         }
     }
+    if (vst && vev) {
+        // the vertical pass on its own stream, after the horizontal sums
+        cudaError_t e = cudaEventRecord(vev, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(vst, vev, 0);
+        if (e != cudaSuccess) return e;
+        st = vst;
+    }
     if (v.blk) {
         ProfScope ps("k_vblock", st);
         const size_t rowElems = (size_t)sg.hp * stat_pitch(cnMax);
@@ -2178,13 +2185,6 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
                 H, blk, nblk, rowElems);
             count_launches(1);
         }
-    }
-    if (vst && vev) {
-        // the vertical pass on its own stream, after the horizontal sums
-        cudaError_t e = cudaEventRecord(vev, st);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(vst, vev, 0);
-        if (e != cudaSuccess) return e;
-        st = vst;
     }
     {
         ProfScope ps("k_vstats", st);
