@@ -391,7 +391,7 @@ __device__ __forceinline__ void col_passes_ch(int cn, const SmemNatCh<L, LSC> &i
 }
 
 template <int L>
-__global__ void __launch_bounds__(256, 2) k_cols_sum_t(ColsArgs a) {
+__global__ void __launch_bounds__(256, 3) k_cols_sum_t(ColsArgs a) {
     constexpr int N = 1 << L, NP = npass(L), SC = sc4(L), LSC = ilog2k(SC);
     constexpr int M = Mid<L>::M, S = Mid<L>::S;
     extern __shared__ float2 smem[];
