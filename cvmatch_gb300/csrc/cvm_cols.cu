@@ -86,10 +86,22 @@ __host__ __device__ constexpr int tw_off(int L, int h) { return (L & 1) ? h - 2 
 
 template <bool INV, int H, bool F = false>
 __device__ __forceinline__ void math16(float2 *e, const float2 *__restrict__ t) {
+    const float2 *tB = t + 3 * H;
+    if constexpr (F && H == 1) {
+        // quarter 1: the first stage's twiddles and the second stage's
+        // column 0 are all 1
+#pragma unroll
+        for (int b = 0; b < 4; b++) bfly4_one<INV>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3]);
+        bfly4_one<INV>(&e[0], &e[4], &e[8], &e[12]);
+#pragma unroll
+        for (int q = 1; q < 4; q++)
+            bfly4<INV, F>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + q), __ldg(tB + 4 + q),
+                          __ldg(tB + 8 + q));
+        return;
+    }
     const float2 a1 = __ldg(t), a2 = __ldg(t + H), a3 = __ldg(t + 2 * H);
 #pragma unroll
     for (int b = 0; b < 4; b++) bfly4<INV, F>(&e[4 * b], &e[4 * b + 1], &e[4 * b + 2], &e[4 * b + 3], a1, a2, a3);
-    const float2 *tB = t + 3 * H;
 #pragma unroll
     for (int q = 0; q < 4; q++)
         bfly4<INV, F>(&e[q], &e[q + 4], &e[q + 8], &e[q + 12], __ldg(tB + H * q), __ldg(tB + 4 * H + H * q),
@@ -109,9 +121,14 @@ __device__ __forceinline__ void math_head(float2 *e, const float2 *__restrict__ 
         e[i] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
         e[i + 1] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
     }
+    if constexpr (F) {
+        bfly4_one<INV>(&e[0], &e[2], &e[4], &e[6]);
+        bfly4<INV, F>(&e[1], &e[3], &e[5], &e[7], __ldg(t + 1), __ldg(t + 3), __ldg(t + 5));
+    } else {
 #pragma unroll
-    for (int j = 0; j < 2; j++)
-        bfly4<INV, F>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+        for (int j = 0; j < 2; j++)
+            bfly4<INV, F>(&e[j], &e[j + 2], &e[j + 4], &e[j + 6], __ldg(t + j), __ldg(t + 2 + j), __ldg(t + 4 + j));
+    }
 }
 
 __device__ __forceinline__ float2 mul_conj(float2 av, float2 bv) {

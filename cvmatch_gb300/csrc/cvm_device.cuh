@@ -164,6 +164,23 @@ __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2
     *pd = make_float2(__fsub_rn(s1x, rr), __fsub_rn(s1y, ri));
 }
 
+// bfly4 with all three twiddles equal to 1 (quarter size 1, or column 0 of
+// a stage): the fast form skips the products, which change nothing but the
+// sign of a zero; the exact form keeps the reference's products.
+template <bool INV>
+__device__ __forceinline__ void bfly4_one(float2 *pa, float2 *pc, float2 *pb, float2 *pd) {
+    const float2 av = *pa, tb = *pb, tc = *pc, td = *pd;
+    const float s0x = av.x + tc.x, s0y = av.y + tc.y;
+    const float s1x = av.x - tc.x, s1y = av.y - tc.y;
+    const float s2x = tb.x + td.x, s2y = tb.y + td.y;
+    const float s3x = tb.x - td.x, s3y = tb.y - td.y;
+    const float rr = INV ? -s3y : s3y, ri = INV ? s3x : -s3x;
+    *pa = make_float2(s0x + s2x, s0y + s2y);
+    *pc = make_float2(s1x + rr, s1y + ri);
+    *pb = make_float2(s0x - s2x, s0y - s2y);
+    *pd = make_float2(s1x - rr, s1y - ri);
+}
+
 // Padded shared-memory line layout: one spare slot every 16 elements keeps
 // the strided pass accesses free of bank conflicts.
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
