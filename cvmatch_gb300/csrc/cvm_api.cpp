@@ -124,9 +124,11 @@ cudaStream_t thread_stream() {
 // while the caller's stream takes the template and the small setup.
 struct SideStream {
     cudaStream_t st = nullptr, st2 = nullptr;
-    cudaStream_t stats = nullptr;  // a colour match's window statistics, at the caller's priority
+    cudaStream_t stats = nullptr;  // the caller's priority: a one-shot match's frame rows or late statistics
     cudaEvent_t fork = nullptr, join = nullptr, joinStats = nullptr, frame = nullptr;
     cudaEvent_t hsumDone = nullptr;  // a late statistics chain's horizontal sums
+    cudaEvent_t prep = nullptr;      // a one-shot match's k_prep done
+    cudaEvent_t rows = nullptr;      // a one-shot match's frame row transform done (stats stream)
 };
 
 SideStream &side_stream() {
@@ -146,6 +148,8 @@ SideStream &side_stream() {
         cudaEventCreateWithFlags(&s.joinStats, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.frame, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&s.hsumDone, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.prep, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s.rows, cudaEventDisableTiming);
     }
     return s;
 }
@@ -415,22 +419,23 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.lanes = lanes;
     ms.lanesStride = 0;
     ms.form = fast ? 1 : 0;
-    // The template statistics, the parent's alpha scan and the channel
-    // count first (one short launch on st), then three chains: the frame's
-    // row transforms (every channel the device chose, one launch) on st;
-    // the template spectrum on the first side stream; the window
-    // statistics on the second.  A launch that does not start first does
-    // not get SMs back from one that did (priority orders only the CTAs
-    // waiting for a slot), so the gating statistics launch goes first.
+    // One short launch (k_prep: the template statistics, the parent's
+    // alpha scan, the channel count) on st, then chains: the frame's row
+    // transform (on st, or on the rows stream beside k_prep); the template
+    // spectrum on the first side stream; the window statistics on the
+    // second; the column and inverse-row passes on st.  A launch that does
+    // not start first does not get SMs back from one that did (priority
+    // orders only the CTAs waiting for a slot), so k_prep is the launch
+    // that is ready first.
     SideStream &ss = side_stream();
     // A one-shot colour match on a device-resident frame starts its template
-    // spectrum at once, beside the statistics launch: all four channels
-    // (the frame's alpha plane decides later whether the fourth is used)
-    // and, in the fast form, the zero-mean samples from sums the row kernel
-    // takes itself -- the spectrum depends on nothing the statistics launch
-    // computes.  (With a host frame in flight the same early chain measured
-    // slower end to end, with the ingest kernel and with the copy engine
-    // alike: host-buffer calls keep the template behind the frame.)
+    // spectrum at once, beside k_prep: all four channels (the frame's alpha
+    // plane decides later whether the fourth is used) and, in the fast form,
+    // the zero-mean samples from sums the row kernel takes itself -- the
+    // spectrum depends on nothing k_prep computes.  (With a host frame in
+    // flight the same early chain measured slower end to end, with the
+    // ingest kernel and with the copy engine alike: host-buffer calls keep
+    // the template behind the frame.)
     const bool early = !J.frameOnSide && !J.cachedP && J.mode == 1 && (long long)J.tw * J.th <= 65536;
     if (early) {
         CVM_CUDA(cudaEventRecord(ss.fork, st));  // the template and the pool's spectrum buffers
@@ -439,20 +444,43 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
                             nullptr, nullptr, fast ? 1 : 0));
         CVM_CUDA(cudaEventRecord(ss.join, ss.st));
     }
+    // A fast-form colour match with a short template (the fused column pass
+    // dominates; the statistics have slack until the inverse rows) queues its
+    // horizontal sums behind the frame's row transform, at the caller's
+    // priority, so they fill the SMs the transforms leave instead of
+    // displacing the row transform; otherwise the statistics start after
+    // k_prep, above it.
+    const bool statsLate = fastSum && J.th <= 64;
+    // Otherwise, on a frame of 2^20 pixels or more, the frame's row
+    // transform of every channel the alpha scans cannot drop (all but a
+    // colour match's alpha plane) runs on the rows stream (the caller's
+    // priority) from before k_prep, which only the alpha plane's transform,
+    // the statistics and the template chain wait for; k_prep, ready at once
+    // on the caller's stream, still places its CTAs first.  (A small frame
+    // or a late statistics chain loses more to the extra cross-stream
+    // waits and the side chains it exposes: C1 70.3 -> 73.4 us, C2 fast
+    // 92.8 -> 96.6 us; C2 exact 118.5 -> 113 us, C3 fast 209.6 -> 202.7 us.)
+    const bool split = !statsLate && (long long)J.iw * J.ih >= (1LL << 20);
     if (J.frameOnSide) CVM_CUDA(cudaStreamWaitEvent(st, ss.frame, 0));
+    if (split) {
+        CVM_CUDA(cudaEventRecord(ss.fork, st));  // the frame, P and F zeroed, the pool's buffers
+        CVM_CUDA(cudaStreamWaitEvent(ss.stats, ss.fork, 0));
+    }
     CVM_CUDA(launch_prep(J.cachedP ? nullptr : J.tpl, J.tstride, J.tw, J.th, J.step, cnS,
                          J.mode == 1 ? J.img : nullptr, J.istride, J.iw, J.ih, P, 1, J.cachedP ? 0 : 1, J.mode,
                          J.cnFixed, F, st));
-    // A fast-form colour match with a short template (the fused column pass
-    // dominates; the statistics have slack until the inverse rows) queues its
-    // statistics after the frame's row transform, at the caller's priority,
-    // so they fill the SMs the transforms leave instead of displacing the
-    // row transform; otherwise they start at once, above it.
-    const bool statsLate = fastSum && J.th <= 64;
+    // the fast form transforms the frame offset by -128 (zero-mean templates)
+    const float off[4] = {128.f, 128.f, 128.f, 128.f};
+    if (split) {
+        for (int c = 0; c < G->nclass; c++)
+            CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, J.mode == 1 ? 3 : cnS, nullptr, G->g, G->fc[c],
+                                     spec[c], cnS, ss.stats, 0, nullptr, 1.0f, fast ? off : nullptr));
+        CVM_CUDA(cudaEventRecord(ss.rows, ss.stats));
+    }
     cudaStream_t sst = statsLate ? ss.stats : ss.st2;
-    CVM_CUDA(cudaEventRecord(ss.fork, st));
-    if (!early) CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.fork, 0));
-    CVM_CUDA(cudaStreamWaitEvent(sst, ss.fork, 0));
+    CVM_CUDA(cudaEventRecord(ss.prep, st));
+    if (!early) CVM_CUDA(cudaStreamWaitEvent(ss.st, ss.prep, 0));
+    CVM_CUDA(cudaStreamWaitEvent(sst, ss.prep, 0));
     if (!statsLate) {
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
                                   J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst, 0, nullptr,
@@ -463,20 +491,27 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
         CVM_TRY(build_tspec(*G, J.tpl, J.tstride, J.step, J.tw, J.th, cnS, &P->cn, tsOwn[0], tsOwn[1], ss.st,
                             nullptr, fast ? P->tsum : nullptr));
     if (!early) CVM_CUDA(cudaEventRecord(ss.join, ss.st));
-    // the fast form transforms the frame offset by -128 (zero-mean templates)
-    const float off[4] = {128.f, 128.f, 128.f, 128.f};
-    for (int c = 0; c < G->nclass; c++)
-        CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0, nullptr,
-                                 1.0f, fast ? off : nullptr));
+    if (split) {
+        // a colour match's alpha plane, when the alpha scans chose four channels
+        if (J.mode == 1)
+            for (int c = 0; c < G->nclass; c++)
+                CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, 4, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 3,
+                                         nullptr, 1.0f, fast ? off : nullptr));
+    } else {
+        // every channel the device chose, one launch
+        for (int c = 0; c < G->nclass; c++)
+            CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0,
+                                     nullptr, 1.0f, fast ? off : nullptr));
+    }
     if (statsLate) {
         // the horizontal sums at the caller's priority, the vertical pass
         // (which gates the inverse rows) back above it on the second side stream
-        CVM_CUDA(cudaStreamWaitEvent(ss.st2, ss.fork, 0));
         CVM_CUDA(launch_sep_stats(J.img, J.istride, J.step, J.iw, J.ih, ms, 1, J.tw, rw, sg,
                                   J.mode == 1 ? 3 : J.cnFixed, J.mode == 1 ? 4 : J.cnFixed, H, 0, sst, 0, ss.st2,
                                   ss.hsumDone, blk));
         CVM_CUDA(cudaEventRecord(ss.joinStats, ss.st2));
     }
+    if (split) CVM_CUDA(cudaStreamWaitEvent(st, ss.rows, 0));
     // Several channels, fast form: transforms up to 512 tall run every
     // channel of a column strip in one CTA (mode 4: forward, channel sum of
     // the conj-products, one inverse); taller ones store the forward

@@ -1850,7 +1850,7 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     // shared memory; row pairs per CTA fill ~32 KB when rows are short.
     int group = 16384 / fc.n;
     if (group < 1) group = 1;
-    if (group > chanCount) group = chanCount;
+    if (group > chanCount - chanFirst) group = chanCount - chanFirst;
     int P = 4096 / (fc.n * group);
     if (P < 1) P = 1;
     // Largest row count of any tile: blockH + thL - 1, capped by dftH.
