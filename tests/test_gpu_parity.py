@@ -720,3 +720,86 @@ def test_fleet_roi_members_equal_restricted_maps():
     again = fleet.FindAll(parent)
     for i in range(len(tpls)):
         assert same_tuple(tuple(again[i]), res[i])
+
+
+# ------------------------------------------- frames of 2^20 pixels or more
+# One-shot matches on frames this large (statistics not queued late) run the
+# frame's row transform beside k_prep and the alpha plane's transform in a
+# second launch that only does work when the alpha scans choose four
+# channels; the bar stays bit identity with the oracle.
+
+def test_large_frame_constant_alpha_bit_exact():
+    img = rgba(61, 1024, 1024)  # 2^20 pixels, alpha 255: cn = 3
+    sub = img[300:330, 500:540].copy()
+    m, _, _ = cvm.MatchMap(img, sub)
+    t = cvm.Match(img, sub)
+    to, mo = oracle.match_u8(img, sub, 3, threads=16)
+    assert np.array_equal(bits(m), bits(mo))
+    assert same_tuple(t, to) and (t[4], t[5]) == (500, 300)
+
+
+def test_large_frame_varying_alpha_bit_exact():
+    img = rgba(62, 1024, 1024, None)  # varying alpha: the fourth channel's launch transforms it
+    sub = img[600:628, 100:136].copy()
+    m, _, _ = cvm.MatchMap(img, sub)
+    t = cvm.Match(img, sub)
+    to, mo = oracle.match_u8(img, sub, 4, threads=16)
+    assert np.array_equal(bits(m), bits(mo))
+    assert same_tuple(t, to) and (t[4], t[5]) == (100, 600)
+
+
+def test_large_gray_frame_tall_template_bit_exact():
+    g = np.ascontiguousarray(image(63, 1000, 1100, 4)[..., 1])  # 1.1 Mpx; 70 rows: block sums too
+    sub = g[400:470, 700:770].copy()
+    t, m = cvm.match_u8(g, sub, 1)
+    to, mo = oracle.match_u8(g, sub, 1, threads=16)
+    assert np.array_equal(bits(m), bits(mo))
+    assert same_tuple(t, to) and same_tuple(cvm.MatchGray(g, sub), to) and (t[4], t[5]) == (700, 400)
+
+
+def test_large_frame_fast_form_tall_template_vs_fp64():
+    # fast form, a 66-row colour template: statistics above the caller's
+    # priority, the frame's rows beside k_prep; within 1e-4 of the FP64
+    # definition of the score (cvmatch_test.go:118)
+    img = rgba(61, 1024, 1024)
+    sub = img[200:266, 300:324].copy()
+    prev = cvm.SetForm(cvm.FORM_FAST)
+    try:
+        m, _, _ = cvm.MatchMap(img, sub)
+        t = cvm.Match(img, sub)
+    finally:
+        cvm.SetForm(prev)
+    m64 = oracle.ref_match_f64(img, sub, 3, threads=16)
+    assert float(np.abs(m.astype(np.float64) - m64).max()) <= 1e-4
+    assert (t[4], t[5]) == (300, 200) and t[3] >= 0.999
+
+
+@pytest.mark.parametrize("alpha", ["const", "parent"])
+def test_large_device_resident_match_bit_exact(alpha):
+    """cvm_match_device (the frame already on the device: the template
+    spectrum starts at once, the frame's rows beside k_prep) on 2^20
+    pixels, bit for bit against the oracle with cn 3 and cn 4."""
+    torch = pytest.importorskip("torch")
+    L = cvm.lib()
+    img = rgba(64, 1024, 1024)
+    if alpha == "parent":
+        img[517, 3, 3] = 7
+    t = img[400:432, 256:304].copy()
+    cn = 3 if alpha == "const" else 4
+    th, tw = t.shape[:2]
+    rw, rh = img.shape[1] - tw + 1, img.shape[0] - th + 1
+    d_img, d_tpl = torch.from_numpy(img).cuda(), torch.from_numpy(t).cuda()
+    d_map = torch.empty((rh, rw), dtype=torch.float32, device="cuda")
+    d_out = torch.zeros(6, dtype=torch.int32, device="cuda")
+    to, mo = oracle.match_u8(img, t, cn, threads=16)
+    for _ in range(2):  # the second call reuses the pooled buffers
+        rc = L.cvm_match_device(d_img.data_ptr(), img.strides[0], img.shape[1], img.shape[0], d_tpl.data_ptr(),
+                                t.strides[0], tw, th, d_map.data_ptr(), d_out.data_ptr(),
+                                torch.cuda.current_stream().cuda_stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(bits(d_map.cpu().numpy()), bits(mo))
+        o = d_out.cpu().numpy()
+        f = o.view(np.float32)
+        got = (float(f[0]), int(o[1]), int(o[2]), float(f[3]), int(o[4]), int(o[5]))
+        assert same_tuple(got, to) and (got[4], got[5]) == (256, 400)
