@@ -26,6 +26,10 @@ namespace cvm {
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static thread_local int t_pdl = 0;
+void set_pdl(int on) { t_pdl = on; }
+int pdl_on() { return t_pdl; }
+
 static thread_local std::string t_err;
 void set_error_message(const char *msg) { t_err = msg; }
 
@@ -498,7 +502,10 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
                 CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, 4, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 3,
                                          nullptr, 1.0f, fast ? off : nullptr));
     } else {
-        // every channel the device chose, one launch
+        // every channel the device chose, one launch; with late statistics
+        // it places its CTAs while k_prep finishes (programmatic dependent
+        // launch)
+        PdlScope pdl(statsLate);
         for (int c = 0; c < G->nclass; c++)
             CVM_CUDA(launch_fwd_rows(J.img, J.istride, J.step, cnS, &P->cn, G->g, G->fc[c], spec[c], cnS, st, 0,
                                      nullptr, 1.0f, fast ? off : nullptr));
@@ -520,6 +527,13 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     int colMode[2] = {1, 1};
     for (int c = 0; c < G->nclass; c++)
         if (fastSum) colMode[c] = G->fc[c].log2H <= 9 ? 4 : 3;
+    // With late statistics (their chain has slack, the template chain too)
+    // each transform launch follows a transform kernel on st and places its
+    // CTAs while that one finishes; the event waits on the side chains stay
+    // whole dependencies.  (C2 fast 92.6 -> 90.7 us; on C1, whose template
+    // chain gates the column pass, the frame transform's earlier CTAs cost
+    // that chain SMs: 68.4 -> 72.9 us, so the others launch plainly.)
+    PdlScope pdl(statsLate);
     for (int c = 0; c < G->nclass; c++)
         if (colMode[c] == 3) {
             MemberSet none;

@@ -409,6 +409,8 @@ __device__ __forceinline__ void col_passes_ch(int cn, const SmemNatCh<L, LSC> &i
 
 template <int L>
 __global__ void __launch_bounds__(256, 3) k_cols_sum_t(ColsArgs a) {
+    griddep_wait();
+    griddep_launch();
     constexpr int N = 1 << L, NP = npass(L), SC = sc4(L), LSC = ilog2k(SC);
     constexpr int M = Mid<L>::M, S = Mid<L>::S;
     extern __shared__ float2 smem[];
@@ -464,6 +466,8 @@ __global__ void __launch_bounds__(256, 3) k_cols_sum_t(ColsArgs a) {
 
 template <int MODE, int L>
 __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
+    griddep_wait();
+    griddep_launch();
     constexpr int N = 1 << L, NP = npass(L);
     constexpr int SC = N >= 1024 ? 8192 / N : 16, LSC = ilog2k(SC);
     extern __shared__ float2 smem[];
@@ -592,13 +596,13 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
 template <int MODE, int L>
 void cols_one(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     set_smem(k_cols_t<MODE, L>, smem);
-    k_cols_t<MODE, L><<<grid, kThreads, smem, st>>>(a);
+    launch_k(k_cols_t<MODE, L>, grid, dim3(kThreads), smem, st, a);
 }
 
 template <int L>
 void cols_sum_one(const ColsArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     set_smem(k_cols_sum_t<L>, smem);
-    k_cols_sum_t<L><<<grid, kThreads, smem, st>>>(a);
+    launch_k(k_cols_sum_t<L>, grid, dim3(kThreads), smem, st, a);
 }
 
 template <int MODE>

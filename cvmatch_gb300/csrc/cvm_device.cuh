@@ -19,6 +19,34 @@ int begin(const char *name, cudaStream_t st);
 void end(int idx, cudaStream_t st);
 }  // namespace prof
 
+// Programmatic dependent launch, device side.  griddep_wait: block until
+// the kernel this one may overlap (the preceding kernel of its stream) has
+// completed and its memory is visible -- a no-op when launched without
+// the attribute.  griddep_launch: this CTA no longer holds back the
+// launch of the stream's next kernel (which still waits before reading).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// A transform kernel's launch, with the programmatic-serialization
+// attribute when the calling thread asked for it (set_pdl); the kernel
+// must call griddep_wait before its first global read.
+template <typename... P, typename... A>
+inline cudaError_t launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    if (pdl_on()) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
+}
+
 // Brackets one launch with the optional per-kernel event timing.
 struct ProfScope {
     int idx;

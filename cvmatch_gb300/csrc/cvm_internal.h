@@ -236,6 +236,18 @@ cudaError_t launch_peaks(const float *map, int w, int h, float thresh, int rx, i
 // kernel-launch counter (exported by cvm_launch_count)
 void count_launches(unsigned n);
 
+// Programmatic dependent launch for the calling thread's next launches of
+// the transform kernels (rows, columns, inverse rows): each may start its
+// CTAs while the preceding kernel of its stream finishes; they wait on the
+// device (griddepcontrol.wait) before reading anything.  Only the
+// dependency on that preceding kernel is relaxed; event waits stay whole.
+void set_pdl(int on);
+int pdl_on();
+struct PdlScope {
+    explicit PdlScope(bool on) { set_pdl(on ? 1 : 0); }
+    ~PdlScope() { set_pdl(0); }
+};
+
 // sets the calling thread's message returned by cvm_last_error
 void set_error_message(const char *msg);
 

@@ -329,6 +329,7 @@ struct PrepArgs {
 // cvmatch.go:146-168), and -- in the CTA that finishes last -- the cn
 // choice and tail constants of every member.  P and F are zeroed first.
 __global__ void k_prep(PrepArgs a) {
+    griddep_launch();  // the frame's row transform may start placing CTAs
     __shared__ int isLast;
     const int tid = threadIdx.x, nt = blockDim.x;
     bool bad = false;

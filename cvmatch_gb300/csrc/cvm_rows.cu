@@ -231,6 +231,8 @@ __device__ __forceinline__ int div_cn(int line, int cn) {
 
 template <int LOG2N, bool F>
 __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
+    griddep_wait();
+    griddep_launch();
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     extern __shared__ float2 smem[];
     const FftClass &fc = a.fc;
@@ -408,6 +410,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
 // first-occurrence extrema merged by each member's last CTA.
 template <int LOG2N, bool FAST>
 __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 3) k_inv_rows_t(InvArgs a) {
+    griddep_wait();
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     constexpr int XIT = (N + kThreads - 1) / kThreads;  // result columns per thread
     extern __shared__ float2 smem[];
@@ -665,10 +668,10 @@ template <int L>
 void fwd_one(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
     if (a.fma) {
         set_smem(k_fwd_rows_t<L, true>, smem);
-        k_fwd_rows_t<L, true><<<grid, threads, smem, st>>>(a);
+        launch_k(k_fwd_rows_t<L, true>, grid, dim3(threads), smem, st, a);
     } else {
         set_smem(k_fwd_rows_t<L, false>, smem);
-        k_fwd_rows_t<L, false><<<grid, threads, smem, st>>>(a);
+        launch_k(k_fwd_rows_t<L, false>, grid, dim3(threads), smem, st, a);
     }
 }
 
@@ -676,10 +679,10 @@ template <int L>
 void inv_one(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
     if (a.ms.form) {
         set_smem(k_inv_rows_t<L, true>, smem);
-        k_inv_rows_t<L, true><<<grid, kThreads, smem, st>>>(a);
+        launch_k(k_inv_rows_t<L, true>, grid, dim3(kThreads), smem, st, a);
     } else {
         set_smem(k_inv_rows_t<L, false>, smem);
-        k_inv_rows_t<L, false><<<grid, kThreads, smem, st>>>(a);
+        launch_k(k_inv_rows_t<L, false>, grid, dim3(kThreads), smem, st, a);
     }
 }
 
