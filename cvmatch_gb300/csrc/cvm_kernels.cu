@@ -1858,6 +1858,9 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     int maxRows = g.blockH + g.thL - 1;
     if (maxRows > fc.dftH) maxRows = fc.dftH;
     const int pairs = (maxRows + 1) / 2;
+    // few rows (a small template or frame): fewer pairs per CTA until the
+    // launch has a CTA per SM, so the rows are spread over the SMs
+    while (P > 1 && (long long)((pairs + P - 1) / P) * fc.ntiles < 152) P >>= 1;
     dim3 grid((pairs + P - 1) / P, fc.ntiles);
     const size_t smem = (size_t)P * group * padded_len(fc.n) * sizeof(float2);
     // as many threads as a radix-16 pass has units (a multiple of 32 in
