@@ -69,7 +69,7 @@ def to_u8(a):
     return np.clip(np.rint(a), 0, 255).astype(np.uint8)
 
 
-def scene_c1(seed=1):
+def scene_gray_640x480(seed=1):
     """640x480 RGBA: 1/f^2 noise + 20 rectangles + N(0,2); 64x48 crop."""
     rng = np.random.default_rng(seed)
     base = pink_noise(rng, 480, 640)
@@ -84,7 +84,7 @@ def scene_c1(seed=1):
     return rgba, rgba[y:y + 48, x:x + 64].copy(), (x, y)
 
 
-def scene_c2(seed=2):
+def scene_ui_1920x1080(seed=2):
     """1920x1080 UI-like RGBA: flat panels, gradients, 1-px glyph strokes,
     three near-duplicate 96x32 buttons; the template is one button with an
     a*x+b intensity shift."""
@@ -134,7 +134,7 @@ def scene_c2(seed=2):
     return rgba, tpl, spots[0]
 
 
-def scene_c3(seed=3):
+def scene_gray_3840x2160(seed=3):
     """3840x2160 gray: 1/f^2 noise + rectangles + N(0,3); a 256x256 crop
     with N(0,4) added."""
     rng = np.random.default_rng(seed)
@@ -147,7 +147,7 @@ def scene_c3(seed=3):
     return g, tpl, (x, y)
 
 
-def scene_c4(seed=4, count=256):
+def scene_fleet_2560x1440(seed=4, count=256):
     """2560x1440 RGBA frame and `count` templates, sizes U[16,192]xU[16,128];
     70% crops with an a*x+b shift, 30% from an independent seed."""
     rng = np.random.default_rng(seed)
@@ -177,7 +177,7 @@ def scene_c4(seed=4, count=256):
     return frame, tpls, where
 
 
-def scene_c5(seed=5, frames=16, ncolor=64, ngray=8):
+def scene_stream_1920x1080(seed=5, frames=16, ncolor=64, ngray=8):
     """A 1920x1080 RGBA frame sequence: a 1/f^2 noise + rectangles scene,
     each frame the previous one with 5% of the rectangles moved and the
     sigma=2 noise redrawn; 64 colour templates of 24x24..128x96 (70% crops
@@ -336,7 +336,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle
-    frame, tpl, _ = scene_c2()
+    frame, tpl, _ = scene_ui_1920x1080()
     threads = min(16, os.cpu_count() or 1)
     for _ in range(max(1, args.warmup)):
         oracle.match_u8(frame, tpl, 3, threads=threads, want_map=False)
@@ -390,7 +390,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     L = cvm.lib()
     cvm.SetForm(FORM[args.form])
-    frame, tpl, _ = scene_c2()
+    frame, tpl, _ = scene_ui_1920x1080()
     d_frame = torch.from_numpy(frame).to(dev)
     d_tpl = torch.from_numpy(tpl).to(dev)
     d_out = torch.zeros(6, dtype=torch.int32, device=dev)
@@ -504,7 +504,7 @@ def fft_flops(n):
     return f
 
 
-def c2_models(L, form="exact"):
+def match_models(L, form="exact"):
     """Algorithmic bytes and flops per launch of each kernel on the
     benchmark workload (cn = 3 after the alpha scan; RGBA input): the HBM
     bytes each kernel must read and write by design (frame, spectra,
@@ -553,10 +553,10 @@ def c2_models(L, form="exact"):
 
 def measured_traffic(form="exact"):
     """DRAM bytes per launch per kernel from the committed ncu summary of
-    this workload in this form (profiles/match_c2_dram_traffic.txt,
-    profiles/match_c2_fast_dram_traffic.txt), or {}."""
-    path = os.path.join(ROOT, "profiles", "match_c2_fast_dram_traffic.txt" if form == "fast"
-                        else "match_c2_dram_traffic.txt")
+    this workload in this form (profiles/match_rgba_1920x1080_dram_traffic.txt,
+    profiles/match_rgba_1920x1080_fast_dram_traffic.txt), or {}."""
+    path = os.path.join(ROOT, "profiles", "match_rgba_1920x1080_fast_dram_traffic.txt" if form == "fast"
+                        else "match_rgba_1920x1080_dram_traffic.txt")
     out = {}
     if os.path.exists(path):
         for line in open(path):
@@ -615,7 +615,7 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind, form="exact"):
     """The dominant kernel's algorithmic bytes over its duration, timed live
     by the library's event instrumentation."""
     rows = profile_kernels(L, step_dev, torch)
-    models = c2_models(L, form)
+    models = match_models(L, form)
     total = sum(r[1] for r in rows)
     kernels = {}
     for nm, ms, n in rows:
@@ -633,7 +633,7 @@ def roofline(L, step_dev, torch, stream, peak, peak_kind, form="exact"):
 
 
 def run_stream(args):
-    """C5: a stream of 1920x1080 RGBA frames against 64 colour templates and
+    """A stream of 1920x1080 RGBA frames against 64 colour templates and
     8 gray matchers on each frame's gray conversion, through cvm_stream (the
     per-frame pipeline replayed as a CUDA graph, two frames in flight, host
     frames copied in and results copied out).  Reports frames/s, template
@@ -643,7 +643,7 @@ def run_stream(args):
     import ctypes as C
     import torch
     import cvmatch_gb300 as cvm
-    frames, color, gray = scene_c5()
+    frames, color, gray = scene_stream_1920x1080()
     H, W = frames[0].shape[:2]
     cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in color])
     gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in gray])
@@ -710,7 +710,7 @@ def run_gpu_secondary(args):
     sh = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     if args.workload == "fleet":
-        frame, tpls, _ = scene_c4(count=args.templates)
+        frame, tpls, _ = scene_fleet_2560x1440(count=args.templates)
         ms = [cvm.NewMatcher(t) for t in tpls]
         fleet = cvm.NewFleet(*ms)
         fleet.SetForm(FORM[args.form])
@@ -744,7 +744,7 @@ def run_gpu_secondary(args):
             return {"value": k * W * H / 1e6 / dt, "unit": "template*Mpx/s", "cores": 1, "kind": "port",
                     "sample": f"the first {k} templates of the fleet, 1 thread"}
     elif args.workload == "gray":
-        frame, tpl, _ = scene_c1()
+        frame, tpl, _ = scene_gray_640x480()
         g, gt = oracle.rgba_to_gray(frame), oracle.rgba_to_gray(tpl)
         H, W = g.shape
         th, tw = gt.shape
@@ -779,7 +779,7 @@ def run_gpu_secondary(args):
             return {"value": reps * mpx / (time.perf_counter() - t0), "unit": "template*Mpx/s", "cores": 1,
                     "kind": "port", "sample": f"{reps} MatchGray calls, 1 thread"}
     else:  # map
-        g, tpl, _ = scene_c3()
+        g, tpl, _ = scene_gray_3840x2160()
         H, W = g.shape
         th, tw = tpl.shape
         mpx = W * H / 1e6

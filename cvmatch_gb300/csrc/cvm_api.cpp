@@ -462,8 +462,11 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     // the statistics and the template chain wait for; k_prep, ready at once
     // on the caller's stream, still places its CTAs first.  (A small frame
     // or a late statistics chain loses more to the extra cross-stream
-    // waits and the side chains it exposes: C1 70.3 -> 73.4 us, C2 fast
-    // 92.8 -> 96.6 us; C2 exact 118.5 -> 113 us, C3 fast 209.6 -> 202.7 us.)
+    // waits and the side chains it exposes: a 640x480 gray match with a
+    // 64x48 template 70.3 -> 73.4 us, a 1920x1080 colour match with a 96x32
+    // template 92.8 -> 96.6 us in the fast form; the same match in the exact
+    // form 118.5 -> 113 us, a 3840x2160 gray match with a 256x256 template
+    // 209.6 -> 202.7 us in the fast form.)
     const bool split = !statsLate && (long long)J.iw * J.ih >= (1LL << 20);
     if (J.frameOnSide) CVM_CUDA(cudaStreamWaitEvent(st, ss.frame, 0));
     if (split) {
@@ -530,9 +533,11 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     // With late statistics (their chain has slack, the template chain too)
     // each transform launch follows a transform kernel on st and places its
     // CTAs while that one finishes; the event waits on the side chains stay
-    // whole dependencies.  (C2 fast 92.6 -> 90.7 us; on C1, whose template
-    // chain gates the column pass, the frame transform's earlier CTAs cost
-    // that chain SMs: 68.4 -> 72.9 us, so the others launch plainly.)
+    // whole dependencies.  (A 1920x1080 colour match with a 96x32 template:
+    // 92.6 -> 90.7 us; on a 640x480 gray match with a 64x48 template, whose
+    // template chain gates the column pass, the frame transform's earlier
+    // CTAs cost that chain SMs: 68.4 -> 72.9 us, so the others launch
+    // plainly.)
     PdlScope pdl(statsLate);
     for (int c = 0; c < G->nclass; c++)
         if (colMode[c] == 3) {

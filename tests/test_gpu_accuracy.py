@@ -39,24 +39,24 @@ def form(request):
     cvm.SetForm(prev)
 
 
-def test_c1_gray_vs_fp64(form):
+def test_gray_640x480_vs_fp64(form):
     import bench
-    rgba, tpl, _ = bench.scene_c1()
+    rgba, tpl, _ = bench.scene_gray_640x480()
     g, t = cvm.rgba_to_gray(rgba), cvm.rgba_to_gray(tpl)
     _, m = cvm.match_u8(g, t, 1)
     m64 = oracle.ref_match_f64(g, t, 1, threads=16)
-    e, gi, ri, margin = _report(f"C1 MatchGray 640x480 / 64x48 ({form})", m, m64)
+    e, gi, ri, margin = _report(f"MatchGray 640x480 / 64x48 ({form})", m, m64)
     assert e <= TOL_REF_DRIFT
     if margin > 1e-4:
         assert gi == ri
 
 
-def test_c2_rgba_vs_fp64(form):
+def test_rgba_1920x1080_vs_fp64(form):
     import bench
-    frame, tpl, _ = bench.scene_c2()
+    frame, tpl, _ = bench.scene_ui_1920x1080()
     m, _, _ = cvm.MatchMap(frame, tpl)
     m64 = oracle.ref_match_f64(frame, tpl, 3, threads=16)
-    e, gi, ri, margin = _report(f"C2 Match RGBA 1920x1080 / 96x32 ({form})", m, m64)
+    e, gi, ri, margin = _report(f"Match RGBA 1920x1080 / 96x32 ({form})", m, m64)
     assert e <= TOL_REF_DRIFT
     if margin > 1e-4:
         assert gi == ri

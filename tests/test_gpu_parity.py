@@ -507,18 +507,18 @@ def test_fleet_mixed_modes_rejected():
 # ------------------------------------------------- benchmark-sized configs
 
 
-def test_config_c1_gray_bit_exact():
+def test_gray_640x480_bit_exact():
     import bench
-    frame, tpl, (x, y) = bench.scene_c1()
+    frame, tpl, (x, y) = bench.scene_gray_640x480()
     t = cvm.MatchGray(frame, tpl)
     g, gt = oracle.rgba_to_gray(frame), oracle.rgba_to_gray(tpl)
     to, _ = oracle.match_u8(g, gt, 1, threads=8, want_map=False)
     assert same_tuple(t, to) and (t[4], t[5]) == (x, y)
 
 
-def test_config_c2_match_bit_exact():
+def test_rgba_1920x1080_bit_exact():
     import bench
-    frame, tpl, (x, y) = bench.scene_c2()
+    frame, tpl, (x, y) = bench.scene_ui_1920x1080()
     m, w, h = cvm.MatchMap(frame, tpl)
     to, mo = oracle.match_u8(frame, tpl, 3, threads=16)
     assert np.array_equal(bits(m), bits(mo))
@@ -527,9 +527,9 @@ def test_config_c2_match_bit_exact():
     assert (t[4], t[5]) == (x, y)
 
 
-def test_config_c3_map_bit_exact():
+def test_gray_3840x2160_map_bit_exact():
     import bench
-    g, tpl, (x, y) = bench.scene_c3()
+    g, tpl, (x, y) = bench.scene_gray_3840x2160()
     t, m = cvm.match_u8(g, tpl, 1)
     to, mo = oracle.match_u8(g, tpl, 1, threads=16)
     assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
