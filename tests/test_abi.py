@@ -142,3 +142,19 @@ def test_form_setters_validate_without_device_work():
     assert cvm.SetForm(cvm.FORM_EXACT) == cvm.FORM_FAST and L.cvm_get_form() == cvm.FORM_EXACT
     rc, msg = _err(L.cvm_fleet_set_form(None, cvm.FORM_FAST))
     assert rc == 3 and msg == "cvmatch: empty fleet"
+
+
+def test_no_device_fails_loudly():
+    """Without an sm_103 device every compute entry raises: there is no CPU
+    fallback behind the C ABI.  (Skipped where a device is present.)"""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    img = np.zeros((40, 60, 4), np.uint8)
+    img[5:20, 7:30] = 200
+    sub = img[5:15, 10:25].copy()
+    for call in (lambda: cvm.Match(img, sub), lambda: cvm.MatchMap(img, sub),
+                 lambda: cvm.MatchGray(img[..., 0].copy(), sub[..., 0].copy()),
+                 lambda: cvm.NewFleet(cvm.NewMatcher(sub)).FindAll(img)):
+        with pytest.raises(cvm.CvmatchError, match="no CUDA device"):
+            call()
