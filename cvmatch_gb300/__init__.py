@@ -89,6 +89,7 @@ def lib():
             L.cvm_peaks_device.argtypes = [vp, i32, i32, C.c_float, i32, i32, vp, i32, vp, vp]
             L.cvm_match_device.argtypes = img_args + [vp, vp, vp]
             L.cvm_rgba_to_gray.argtypes = [u8p, i64, i32, i32, vp]
+            L.cvm_rgba_to_gray_device.argtypes = [u8p, i64, i32, i32, vp, i64, vp]
             L.cvm_alpha_const.argtypes = [u8p, i64, i32, i32, C.POINTER(C.c_int)]
             L.cvm_matcher_new.argtypes = [u8p, i64, i32, i32, i32, C.POINTER(vp)]
             L.cvm_matcher_find.argtypes = [vp, u8p, i64, i32, i32, R]
@@ -102,6 +103,8 @@ def lib():
             L.cvm_fleet_free.restype = None
             L.cvm_fleet_set_roi.argtypes = [vp, i32, i32, i32, i32, i32]
             L.cvm_fleet_set_form.argtypes = [vp, i32]
+            L.cvm_fleet_buckets.argtypes = [vp, i32, i32, vp, i32]
+            L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
             L.cvm_get_form.argtypes = []
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
@@ -334,6 +337,25 @@ class Fleet:
         bit) or FORM_FAST (zero-mean templates, channels summed in the
         frequency domain; see cvm_fleet_set_form)."""
         _check(lib().cvm_fleet_set_form(self._h, form))
+
+    def buckets(self, pw: int, ph: int):
+        """[(tw, th, dftW, dftH, blockW, blockH, dh2, tiles, members)] per
+        bucket on a pw x ph frame (bucketize + the bucket plans)."""
+        n = lib().cvm_fleet_buckets(self._h, pw, ph, None, 0)
+        if n < 0:
+            _check(-n)
+        out = (C.c_int32 * (9 * max(n, 1)))()
+        lib().cvm_fleet_buckets(self._h, pw, ph, out, n)
+        return [tuple(out[9 * b:9 * b + 9]) for b in range(n)]
+
+    def bucket_members(self, b: int):
+        """Construction-order indices of bucket b's members."""
+        n = lib().cvm_fleet_bucket_members(self._h, b, None, 0)
+        if n < 0:
+            _check(-n)
+        out = (C.c_int32 * max(n, 1))()
+        lib().cvm_fleet_bucket_members(self._h, b, out, n)
+        return list(out[:n])
 
     def __len__(self):
         return len(self._ms)

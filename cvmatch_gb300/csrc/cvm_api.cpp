@@ -111,6 +111,16 @@ int ensure_device() {
         cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
     });
     if (d.status != CVM_OK) return fail(d.status, "%s", d.msg.c_str());
+    // The library's state (memory pool, twiddle tables, per-thread
+    // streams, Matcher and Fleet caches) lives on the device that was
+    // current at its first call; a call made with another device current
+    // would hand that state to launches on the wrong device.
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != d.device)
+        return fail(CVM_ERR_UNSUPPORTED,
+                    "cvmatch_gpu: the library is bound to CUDA device %d (current at its first call); the calling "
+                    "thread's current device is %d",
+                    d.device, cur);
     return CVM_OK;
 }
 
@@ -1446,6 +1456,17 @@ int cvm_rgba_to_gray(const uint8_t *pix, int64_t stride, int w, int h, uint8_t *
     return CVM_OK;
 }
 
+int cvm_rgba_to_gray_device(const uint8_t *d_pix, int64_t stride, int w, int h, uint8_t *d_out, int64_t ostride,
+                            void *stream) {
+    CVM_TRY(check_image(d_pix, w, h));
+    if (!d_out) return fail(CVM_ERR_NIL_IMAGE, "cvmatch: nil image");
+    if (stride < (int64_t)w * 4 || ostride < (int64_t)w)
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*4, or output stride below width");
+    CVM_TRY(ensure_device());
+    CVM_CUDA(launch_gray(d_pix, stride, w, h, d_out, ostride, static_cast<cudaStream_t>(stream)));
+    return CVM_OK;
+}
+
 int cvm_alpha_const(const uint8_t *pix, int64_t stride, int w, int h, int *out) {
     CVM_TRY(check_image(pix, w, h));
     if (stride < (int64_t)w * 4) return fail(CVM_ERR_ARGS, "cvmatch_gpu: stride below width*4");
@@ -1746,6 +1767,38 @@ int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]) {
     out[4] = shrink_dh(p, rh, th);
     out[5] = ((rw + p.blockW - 1) / p.blockW) * ((rh + p.blockH - 1) / p.blockH);
     return CVM_OK;
+}
+
+int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap) {
+    if (!f) return -fail(CVM_ERR_ARGS, "cvmatch_gpu: nil fleet");
+    const int nb = (int)f->buckets.size();
+    for (int b = 0; b < nb && b < cap && out; b++) {
+        const Bucket &bk = f->buckets[b];
+        const int rw = pw - bk.tw + 1, rh = ph - bk.th + 1;
+        int32_t *o = out + 9 * b;
+        if (rw < 1 || rh < 1) {
+            for (int k = 0; k < 9; k++) o[k] = 0;
+            continue;
+        }
+        const Plan p = make_plan(bk.tw, bk.th, rw, rh);
+        o[0] = bk.tw;
+        o[1] = bk.th;
+        o[2] = p.dftW;
+        o[3] = p.dftH;
+        o[4] = p.blockW;
+        o[5] = p.blockH;
+        o[6] = shrink_dh(p, rh, bk.th);
+        o[7] = ((rw + p.blockW - 1) / p.blockW) * ((rh + p.blockH - 1) / p.blockH);
+        o[8] = (int32_t)bk.members.size();
+    }
+    return nb;
+}
+
+int cvm_fleet_bucket_members(const cvm_fleet *f, int b, int32_t *out, int cap) {
+    if (!f || b < 0 || b >= (int)f->buckets.size()) return -fail(CVM_ERR_ARGS, "cvmatch_gpu: no such bucket");
+    const std::vector<int> &m = f->buckets[b].members;
+    for (int i = 0; i < (int)m.size() && i < cap && out; i++) out[i] = m[i];
+    return (int)m.size();
 }
 
 void *cvm_host_alloc(size_t bytes) {

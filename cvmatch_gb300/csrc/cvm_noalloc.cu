@@ -10,6 +10,11 @@
 // library holds until the process exits.  The caller still passes the
 // image, the template and the outputs.
 //
+// It computes the exact form (the reference's float32 op sequence, bit
+// for bit) whatever cvm_set_form selects: the fast form's statistics
+// kernels need per-row window sums sized by the frame, which this fixed
+// budget does not hold for the frames it accepts.
+//
 // Every call shares that array and it keeps the last call's contents;
 // everything that must start at zero is cleared by each call.  Calls whose
 // work overlaps on the GPU (several host threads, or several streams)
@@ -38,6 +43,7 @@ struct NoAllocDevice {
     unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
     size_t triOff[kMaxLog2 + 1] = {};
     size_t workOff = 0;
+    int smemOptin = 0;              // largest opt-in dynamic shared memory per block
 };
 
 std::mutex g_noalloc_mu;
@@ -66,6 +72,7 @@ int noalloc_setup(NoAllocDevice **out) {
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     if (major != 10 || minor != 3) return na_fail(CVM_ERR_NO_DEVICE, "cvmatch_gpu: built for sm_103a");
+    cudaDeviceGetAttribute(&d.smemOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -147,6 +154,17 @@ extern "C" int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride
     }
     const NormGrid ng = norm_grid(rw, rh, tw, cn);
     const int nparts = ng.ncx * ng.nby;
+    // The normalisation stages a window row of (128 + tw - 1) pixels per
+    // result row group in shared memory; a very wide template needs more
+    // than one block can have.  Refuse before anything is queued.
+    if (ng.smemBytes > (size_t)D->smemOptin) {
+        char b[220];
+        snprintf(b, sizeof b,
+                 "cvmatch_gpu: a %d-pixel-wide template needs %zu bytes of shared memory per block in the "
+                 "fixed-scratch normalisation; the device allows %d (use cvm_match_u8_device)",
+                 tw, ng.smemBytes, D->smemOptin);
+        return na_fail(CVM_ERR_UNSUPPORTED, b);
+    }
 
     // Workspace carved from the fixed array.
     size_t off = D->workOff;

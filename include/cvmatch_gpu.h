@@ -21,6 +21,12 @@
  *     (sub-images).
  *   - All entry points are safe for concurrent use from several threads.
  *     Handles serialise their own lazy geometry builds.
+ *   - One device per process: the library binds to the CUDA device that is
+ *     current on the calling thread at its first call (its memory pool,
+ *     tables, streams and every Matcher/Fleet cache live there); a later
+ *     call made with a different device current returns
+ *     CVM_ERR_UNSUPPORTED before queueing anything.  (The fixed-scratch
+ *     entry point keeps its own per-device set-up.)
  *   - The computation is the reference's op sequence: scores are
  *     bit-identical to cvmatch's Go path on the same inputs.
  */
@@ -115,7 +121,11 @@ int cvm_match_device(const uint8_t *d_parent, int64_t pstride, int pw, int ph,
  * outputs as for cvm_match_u8_device.  The first call on a device sets the
  * array up (synchronous copies of the twiddle tables); make that first call
  * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race, so serialise them. */
+ * overlaps on the GPU race, so serialise them.  It always computes the
+ * exact form (the reference's float32 op sequence, bit-identical to
+ * cvm_match_u8_device in CVM_FORM_EXACT), whatever cvm_set_form selects,
+ * and refuses templates so wide that its normalisation would need more
+ * shared memory per block than the device has (CVM_ERR_UNSUPPORTED). */
 int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride, int iw, int ih,
                                 const uint8_t *d_tpl, int64_t tstride, int tw, int th, int cn, int step,
                                 float *d_map, cvm_result *d_out, void *stream);
@@ -124,6 +134,14 @@ int cvm_match_u8_device_noalloc(const uint8_t *d_img, int64_t istride, int iw, i
 
 /* rgbToGray (cvmatch.go:222-240): out is w*h packed gray bytes. */
 int cvm_rgba_to_gray(const uint8_t *pix, int64_t stride, int w, int h, uint8_t *out);
+
+/* rgbToGray on device buffers: d_out (row stride ostride bytes) receives
+ * the gray plane of the RGBA image d_pix; queued on stream without
+ * synchronising.  MatchGray converts both of its inputs on every call
+ * (cvmatch.go:128-139, toGray cvmatch.go:201-217); a device-resident caller
+ * converts with this and then calls cvm_match_u8_device with cn = step = 1. */
+int cvm_rgba_to_gray_device(const uint8_t *d_pix, int64_t stride, int w, int h, uint8_t *d_out, int64_t ostride,
+                            void *stream);
 
 /* alphaConst (cvmatch.go:146-168): *out = 1 when every alpha byte equals
  * the first pixel's. */
@@ -260,6 +278,16 @@ void cvm_stream_free(cvm_stream *s);
  * shrinkDH, impl.go:573-582): out = {dftW, dftH, blockW, blockH, dh2,
  * tiles}, dh2 = 0 when the last band keeps dftH.  Host-only; no device. */
 int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]);
+
+/* A fleet's buckets (bucketize, fleet.go:111-171) and each bucket's plan on
+ * a pw x ph frame (buildGeom, fleet.go:356-365): returns the bucket count
+ * (negative on error) and, for the first cap buckets, 9 ints each: {tw,
+ * th, dftW, dftH, blockW, blockH, dh2, tiles, members}.  Flat members are
+ * in no bucket.  Host-only; no device. */
+int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap);
+/* Bucket b's members (construction-order indices, ascending): returns
+ * their count (negative on error) and writes the first cap of them. */
+int cvm_fleet_bucket_members(const cvm_fleet *f, int b, int32_t *out, int cap);
 
 /* Page-locked host memory for frames the caller wants copied at full
  * host-to-device bandwidth (plain pageable memory also works). */

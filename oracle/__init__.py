@@ -76,6 +76,8 @@ def lib():
                                              C.POINTER(Result), C.c_char_p]
             L.cvo_fleet_find_all_maps.argtypes = [C.POINTER(Member), i32, i32, vp, i64, i32, i32, i32,
                                                   C.POINTER(Result), vp, C.c_char_p]
+            L.cvo_fleet_find_all_sel.argtypes = [C.POINTER(Member), i32, i32, vp, i64, i32, i32, i32, vp,
+                                                 C.POINTER(Result), vp, vp, C.c_char_p]
             L.cvo_ref_match_f64.argtypes = [vp, i64, i32, i32, vp, i64, i32, i32, i32, i32, i32, vp]
             _lib = L
     return _lib
@@ -245,6 +247,43 @@ def fleet_find_all(tpls, parent: np.ndarray, threads: int = 1, want_maps: bool =
         if maps[i] is not None and np.isnan(maps[i]).all():
             maps[i] = None  # flat member: no map (impl.go:1137-1144)
     return res, maps
+
+
+def fleet_find_all_sel(tpls, parent: np.ndarray, want, threads: int = 1, want_maps: bool = False):
+    """Fleet.FindAll of the whole fleet's buckets and plans, with the member
+    tails run only for the members in `want` (indices, construction order):
+    those members' results are bit-identical to the full FindAll's.
+    Returns (results: {index: six-tuple}, maps: {index: map or None} or
+    None, (phase-1 seconds, phase-2 seconds))."""
+    ms, step = _members(tpls)
+    a, pstride, pw, ph, pstep = _view(parent)
+    if len(tpls) and pstep != step:
+        raise ValueError("parent step differs from the members'")
+    n = len(tpls)
+    mask = np.zeros(max(n, 1), np.uint8)
+    want = sorted(set(int(i) for i in want))
+    mask[want] = 1
+    out = (Result * max(n, 1))()
+    err = C.create_string_buffer(256)
+    maps, mp = None, None
+    if want_maps:
+        maps = {}
+        for i in want:
+            th, tw = np.asarray(tpls[i]).shape[:2]
+            maps[i] = np.full((ph - th + 1, pw - tw + 1), np.nan, np.float32) if tw <= pw and th <= ph else None
+        mp = (C.c_void_p * max(n, 1))(*[maps[i].ctypes.data if (i in maps and maps[i] is not None) else None
+                                        for i in range(n)])
+    phase = np.zeros(2, np.float64)
+    rc = lib().cvo_fleet_find_all_sel(ms, n, step or pstep, _ptr(a), pstride, pw, ph, threads, _ptr(mask), out,
+                                      mp, _ptr(phase), err)
+    if rc != 0:
+        raise OraclePanic(err.value.decode())
+    res = {i: out[i].tuple() for i in want}
+    if maps is not None:
+        for i in want:
+            if maps[i] is not None and np.isnan(maps[i]).all():
+                maps[i] = None  # flat member: no map (impl.go:1137-1144)
+    return res, maps, (float(phase[0]), float(phase[1]))
 
 
 def ref_match_f64(img: np.ndarray, tpl: np.ndarray, cn: int, threads: int = 8) -> np.ndarray:

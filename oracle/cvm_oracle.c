@@ -21,6 +21,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 typedef struct { float re, im; } cf;
 
@@ -938,6 +939,7 @@ typedef struct {
     int ntx, nty, lastY0;
     cvo_result *out;
     float *const *maps;  /* per member (construction order) score map out, or NULL */
+    const uint8_t *want; /* per member (construction order): run its tail; NULL = every member */
     atomic_int next;
     /* phase 1 */
     int btw, bth, rwF, rhF, cnMax, has2;
@@ -976,6 +978,7 @@ static void fl_phase2(void *vctx, int w) {
         int pos = atomic_fetch_add(&c->next, 1);
         if (pos >= c->nmem) break;
         int mi = c->mem[pos];
+        if (c->want && !c->want[mi]) continue;
         const member_t *m = &c->ms[mi];
         int cn = c->cns[mi];
         const tset_t *set = &c->sets[pos];
@@ -1006,11 +1009,28 @@ static void fl_phase2(void *vctx, int w) {
     free(z);
 }
 
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 /* Fleet.FindAll + buildGeom, fleet.go:176-390; maps (optional, per member
  * in construction order, (pw-w+1) x (ph-h+1) floats each) receive every
- * non-flat member's score map on its bucket's plan. */
-int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
-                            int pw, int ph, int threads, cvo_result *out, float *const *maps, char *err) {
+ * non-flat member's score map on its bucket's plan.  want (optional, per
+ * member in construction order) restricts the member tails (phase 2,
+ * fleet.go:265-328) and the member spectra to the members it marks: the
+ * buckets, plans and frame spectra stay those of the whole fleet, so a
+ * marked member's result is bit-identical to its result in the full
+ * FindAll, and unmarked members' results are left untouched.  phase_s
+ * (optional) receives the wall seconds of phase 1 (the frame spectra,
+ * fleet.go:240-263) and of phase 2, summed over buckets; the member
+ * spectra (buildGeom's per-geometry cache, fleet.go:366-375) are in
+ * neither. */
+int cvo_fleet_find_all_sel(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                           int pw, int ph, int threads, const uint8_t *want, cvo_result *out,
+                           float *const *maps, double *phase_s, char *err) {
+    if (phase_s) phase_s[0] = phase_s[1] = 0;
     if (n <= 0) {
         if (err) snprintf(err, 160, "cvmatch: empty fleet");
         return -3;
@@ -1059,7 +1079,7 @@ int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_
             const member_t *m = &ms[bm[j]];
             int cn = cns[bm[j]];
             cnMax = imax(cnMax, cn);
-            tset_build(m->pix, m->stride, step, cn, m->w, m->h, rhF, bth[b], &p, &sets[j]);
+            if (!want || want[bm[j]]) tset_build(m->pix, m->stride, step, cn, m->w, m->h, rhF, bth[b], &p, &sets[j]);
         }
         int ntx = (rwF + p.blockW - 1) / p.blockW;
         int nty = (rhF + p.blockH - 1) / p.blockH;
@@ -1079,14 +1099,21 @@ int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_
         c.pw = pw; c.ph = ph; c.step = step; c.p = &p; c.sets = sets; c.frame = frame; c.off = off;
         c.ntx = ntx; c.nty = nty; c.lastY0 = lastY0; c.out = out;
         c.btw = btw[b]; c.bth = bth[b]; c.rwF = rwF; c.rhF = rhF; c.cnMax = cnMax;
-        c.has2 = dh2 > 0; c.p2 = &p2; c.frame_w = frame; c.maps = maps;
+        c.has2 = dh2 > 0; c.p2 = &p2; c.frame_w = frame; c.maps = maps; c.want = want;
         atomic_init(&c.next, 0);
+        double t0 = now_s();
         run_parallel(imin(threads, ntiles), fl_phase1, &c);
+        double t1 = now_s();
         int outer = imin(threads, nm);
         c.inner = imax(threads / outer, 1);
         atomic_store(&c.next, 0);
         run_parallel(outer, fl_phase2, &c);
-        for (int j = 0; j < nm; j++) tset_free(&sets[j]);
+        if (phase_s) {
+            phase_s[0] += t1 - t0;
+            phase_s[1] += now_s() - t1;
+        }
+        for (int j = 0; j < nm; j++)
+            if (!want || want[bm[j]]) tset_free(&sets[j]);
         free(sets);
         free(off);
         free(frame);
@@ -1095,6 +1122,11 @@ int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_
     free(btw); free(bth); free(offs); free(mem);
     free(ms);
     return 0;
+}
+
+int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                            int pw, int ph, int threads, cvo_result *out, float *const *maps, char *err) {
+    return cvo_fleet_find_all_sel(cms, n, step, pp, pstride, pw, ph, threads, NULL, out, maps, NULL, err);
 }
 
 int cvo_fleet_find_all(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,

@@ -98,6 +98,13 @@ int cvo_fleet_find_all(const cvo_member *ms, int n, int step, const uint8_t *par
                        char *err);
 int cvo_fleet_find_all_maps(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
                             int pw, int ph, int threads, cvo_result *out, float *const *maps, char *err);
+/* The same restricted to the members want marks (NULL: all), on the whole
+ * fleet's buckets and plans (marked members' results are bit-identical to
+ * the full FindAll's); phase_s (nullable) gets the seconds of phase 1 and
+ * phase 2. */
+int cvo_fleet_find_all_sel(const cvo_member *cms, int n, int step, const uint8_t *pp, int64_t pstride,
+                           int pw, int ph, int threads, const uint8_t *want, cvo_result *out,
+                           float *const *maps, double *phase_s, char *err);
 
 /* Brute-force FP64 TM_CCOEFF_NORMED from the definition
  * (cvmatch_test.go:13-81); out has rw*rh doubles. */

@@ -243,3 +243,59 @@ def test_single_member_fleet_is_solo():
     t, _ = oracle.match_u8(parent, tpl, 3)
     (r,) = oracle.fleet_find_all([tpl], parent)
     assert r == t
+
+
+# ------------------------------------------- the FP64 oracle at full sizes
+
+
+@pytest.mark.parametrize("shape", REF_SHAPES)
+def test_fft_fp64_definition_equals_direct_form(shape):
+    """oracle/fp64.py (numerator by a float64 FFT, exact window sums) against
+    the direct spatial sum of refMatch (cvmatch_test.go:13-81) on the
+    reference's shapes: the same map within 1e-9."""
+    from oracle import fp64
+    iw, ih, tw, th, cn, ipad, tpad = shape
+    img = image(42 + iw, ih, iw, cn, ipad)
+    tpl = image(43 + tw, th, tw, cn, tpad)
+    direct = oracle.ref_match_f64(img, tpl, cn)
+    by_fft = fp64.ref_match_f64(img, tpl, cn)
+    assert by_fft.shape == direct.shape
+    assert np.max(np.abs(by_fft - direct)) <= 1e-9
+
+
+def test_fft_fp64_flat_template_and_planted_copy():
+    from oracle import fp64
+    img = image(501, 90, 140, 4).copy()
+    img[..., 3] = 255
+    flat = np.full((10, 12, 4), 9, np.uint8)
+    assert (fp64.ref_match_f64(img, flat, 3) == 1.0).all()
+    t = img[30:52, 40:75].copy()
+    m = fp64.ref_match_f64(img, t, 3)
+    assert fp64.first_argmax(m) == (40, 30) and abs(m[30, 40] - 1.0) < 1e-12
+
+
+def test_check_extrema_locations():
+    """The location rule: enforced only where the top-2 margin exceeds the
+    tolerance."""
+    from oracle import fp64
+    m = np.zeros((4, 5))
+    m[1, 2], m[3, 4], m[0, 0] = 0.9, 0.89995, -0.5
+    fp64.check_extrema((-0.5, 0, 0, 0.9, 2, 1), m, 1e-4)
+    fp64.check_extrema((-0.5, 0, 0, 0.89995, 4, 3), m, 1e-4)  # margin 5e-5: either place
+    m[3, 4] = 0.8
+    with pytest.raises(AssertionError):
+        fp64.check_extrema((-0.5, 0, 0, 0.8, 4, 3), m, 1e-4)
+
+
+def test_fleet_subset_equals_full_find_all():
+    """oracle.fleet_find_all_sel: the whole fleet's buckets and plans, tails
+    of the selected members only -- bit-identical results and maps."""
+    parent = image(311, 180, 260, 4).copy()
+    parent[..., 3] = 255
+    tpls = [parent[y:y + h, x:x + w].copy() for (x, y, w, h) in
+            [(10, 12, 20, 16), (40, 30, 33, 40), (100, 90, 17, 9), (150, 20, 60, 50), (5, 120, 8, 30)]]
+    full, full_maps = oracle.fleet_find_all(tpls, parent, threads=3, want_maps=True)
+    res, maps, phase = oracle.fleet_find_all_sel(tpls, parent, [1, 3], threads=3, want_maps=True)
+    assert set(res) == {1, 3} and res[1] == full[1] and res[3] == full[3]
+    assert np.array_equal(maps[1], full_maps[1]) and np.array_equal(maps[3], full_maps[3])
+    assert phase[0] >= 0 and phase[1] >= 0

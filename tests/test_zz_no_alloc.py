@@ -3,9 +3,12 @@ allocate device memory (their device memory belongs to another allocator,
 or a driver allocation's latency is not acceptable in their loop).  Its
 workspace is a fixed array inside the library, shared by every call, so
 these tests check that two different calls in a row each give exactly the
-result of the allocating entry point (cvm_match_u8_device), i.e. nothing
-from the previous call leaks into the next, and that a match too large for
-the fixed array is refused with a clear error instead of running.
+result of the allocating entry point (cvm_match_u8_device, pinned to the
+exact form, which is the form the fixed-scratch entry always computes) and
+of the oracle (the reference's float32 path restated on the CPU), i.e.
+nothing from the previous call leaks into the next, and that matches too
+large for the fixed array or too wide for its shared-memory staging are
+refused with a clear error instead of running.
 
 This file is collected last on purpose: it must pass alone in a fresh
 process (the first call performs the one-time set-up) and after every
@@ -17,6 +20,7 @@ import numpy as np
 import pytest
 
 import cvmatch_gb300 as cvm
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -72,18 +76,49 @@ def _case_gray():
     return img, tpl, 1
 
 
-def test_two_calls_in_a_row_match_the_allocating_entry_point():
+@pytest.fixture
+def exact_form():
+    """The allocating entry point reads the process-wide form: pin it to the
+    exact form (the fixed-scratch entry's) whatever earlier tests left."""
+    prev = cvm.SetForm(cvm.FORM_EXACT)
+    yield
+    cvm.SetForm(prev)
+
+
+def _tuple(out):
+    return (float(out[:1].view(np.float32)[0]), int(out[1]), int(out[2]), float(out[3:4].view(np.float32)[0]),
+            int(out[4]), int(out[5]))
+
+
+def test_two_calls_in_a_row_match_the_allocating_entry_point(exact_form):
     L = _lib()
     for img, tpl, cn in (_case_colour(), _case_gray(), _case_colour()):
-        for want_map in (True, False):
-            rc0, m0, o0 = _run(L.cvm_match_u8_device, img, tpl, cn, want_map)
+        want_t, want_map = oracle.match_u8(img, tpl, cn, threads=8)
+        for map_wanted in (True, False):
+            rc0, m0, o0 = _run(L.cvm_match_u8_device, img, tpl, cn, map_wanted)
             assert rc0 == 0, _err()
-            rc1, m1, o1 = _run(L.cvm_match_u8_device_noalloc, img, tpl, cn, want_map)
+            rc1, m1, o1 = _run(L.cvm_match_u8_device_noalloc, img, tpl, cn, map_wanted)
             assert rc1 == 0, _err()
-            # the tests' tolerance is bit identity
+            # the tests' tolerance is bit identity: with the allocating entry
+            # point and with the reference's own result (the oracle)
             assert np.array_equal(o1, o0)
-            if want_map:
+            assert _tuple(o1) == want_t
+            if map_wanted:
                 assert np.array_equal(m1.view(np.uint32), m0.view(np.uint32))
+                assert np.array_equal(m1.view(np.uint32), want_map.view(np.uint32))
+
+
+def test_fast_form_setting_does_not_change_the_fixed_scratch_result():
+    L = _lib()
+    img, tpl, cn = _case_colour()
+    want_t, _ = oracle.match_u8(img, tpl, cn, threads=8)
+    prev = cvm.SetForm(cvm.FORM_FAST)
+    try:
+        rc, _, out = _run(L.cvm_match_u8_device_noalloc, img, tpl, cn, False)
+    finally:
+        cvm.SetForm(prev)
+    assert rc == 0, _err()
+    assert _tuple(out) == want_t
 
 
 def test_oversized_match_is_refused():
@@ -94,3 +129,16 @@ def test_oversized_match_is_refused():
     rc, _, _ = _run(L.cvm_match_u8_device_noalloc, img, tpl, 1, False)
     assert rc == 11  # CVM_ERR_UNSUPPORTED
     assert "fixed device scratch" in _err()
+
+
+def test_template_too_wide_for_shared_memory_is_refused():
+    """A 6000-pixel-wide RGBA template would need ~245 KB of shared memory
+    per block in the normalisation; refused before anything is queued."""
+    L = _lib()
+    rng = np.random.default_rng(8)
+    img = rng.integers(0, 256, (200, 6000, 4), dtype=np.uint8)
+    img[..., 3] = 255
+    tpl = img[50:54, :].copy()
+    rc, _, _ = _run(L.cvm_match_u8_device_noalloc, img, tpl, 3, False)
+    assert rc == 11  # CVM_ERR_UNSUPPORTED
+    assert "shared memory" in _err()
