@@ -584,6 +584,9 @@ def roofline(L, W, torch, ms, form, sms, reps):
     parts = W.flops()
     total = sum(parts.values())
     achieved = total / (ms / 1e3) / 1e12
+    for _ in range(3):  # a form switch drops cached spectra: rebuild them outside the profile
+        W.step_dev()
+    torch.cuda.synchronize()
     rows = profile_kernels(L, W.step_dev, torch, reps=reps)
     tot_ms = sum(r[1] for r in rows) or 1.0
     kernels = {}
