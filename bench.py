@@ -365,7 +365,7 @@ def fp32_peak_tflops(sms: int):
     return sms * 128 * 2 * mhz * 1e6 / 1e12, f"derived: {sms} SMs x 128 FP32 lanes x 2 flops x {mhz:.0f} MHz ({src})"
 
 
-FORM = {"exact": 0, "fast": 1}  # CVM_FORM_EXACT, CVM_FORM_FAST
+FORM = {"exact": 0, "fast": 1, "mixed": 2}  # CVM_FORM_EXACT, CVM_FORM_FAST, CVM_FORM_MIXED
 
 
 # ------------------------------------------------ the algorithmic work model
@@ -1054,9 +1054,8 @@ def run_gpu(args):
         W = WORKLOADS[key](cvm, torch, dev, stream)
     W.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     units = _units(key, args)
-    other = "fast" if args.form == "exact" else "exact"
     r = measure(W, args.form, args, ws, dev, torch, local)
-    o = measure(W, other, args, ws, dev, torch, local)
+    others = {f: measure(W, f, args, ws, dev, torch, local) for f in FORM if f != args.form}
     W.set_form(args.form)
     value = replica_throughput(units, r["ms"], ws)
 
@@ -1080,13 +1079,14 @@ def run_gpu(args):
                                    "host_memory": "page-locked (cvm_host_alloc)"}},
                 "gpu_launches": r["launches"], "clocks": r["clocks"], "roofline": roof,
                 "result": list(res) if key != "fleet" else {"members": len(res), "first": list(res[0])},
-                # the same workload in the other arithmetic form, measured in this run
+                # the same workload in every arithmetic form, measured in this run
                 "forms": {args.form: {"value": value, "ms_per_step": r["ms"],
-                                      "e2e": replica_throughput(units, r["e2e_ms"], ws), "e2e_ms_per_step": r["e2e_ms"]},
-                          other: {"value": replica_throughput(units, o["ms"], ws), "ms_per_step": o["ms"],
-                                  "e2e": replica_throughput(units, o["e2e_ms"], ws), "e2e_ms_per_step": o["e2e_ms"],
-                                  "clocks": o["clocks"]}}}
-        line["forms"]["ratio_" + args.form + "_over_" + other] = o["ms"] / r["ms"]
+                                      "e2e": replica_throughput(units, r["e2e_ms"], ws), "e2e_ms_per_step": r["e2e_ms"]}}}
+        for f, o in others.items():
+            line["forms"][f] = {"value": replica_throughput(units, o["ms"], ws), "ms_per_step": o["ms"],
+                                "e2e": replica_throughput(units, o["e2e_ms"], ws), "e2e_ms_per_step": o["e2e_ms"],
+                                "clocks": o["clocks"]}
+            line["forms"]["ratio_" + args.form + "_over_" + f] = o["ms"] / r["ms"]
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(key, args)
         print(json.dumps(line))
@@ -1230,9 +1230,10 @@ def main():
     ap.add_argument("--templates", type=int, default=256, help="fleet size for --workload fleet")
     ap.add_argument("--ref-sample", type=int, default=16,
                     help="member tails timed per step by the fleet's reference arm (the rest scaled)")
-    ap.add_argument("--form", default="fast", choices=["exact", "fast"],
-                    help="arithmetic: fast (default; within 1e-4 of the FP64 definition) or exact (the "
-                         "reference's float32 bits; cvm_set_form / cvm_fleet_set_form)")
+    ap.add_argument("--form", default="fast", choices=["exact", "fast", "mixed"],
+                    help="arithmetic: fast (default; within 1e-4 of the FP64 definition), mixed (the fast form "
+                         "with its 1024-point inverse rows on the tensor cores) or exact (the reference's float32 "
+                         "bits; cvm_set_form / cvm_fleet_set_form); every form is measured in each run")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -107,6 +107,8 @@ def lib():
             L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
             L.cvm_get_form.argtypes = []
+            L.cvm_tc_selftest.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.cvm_device_status.argtypes = [C.POINTER(C.c_int)]
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
             L.cvm_stream_push.argtypes = [vp, u8p, i64]
             L.cvm_stream_pull.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
@@ -292,12 +294,29 @@ def NewGrayMatcher(sub) -> Matcher:
 
 FORM_EXACT = 0
 FORM_FAST = 1
+FORM_MIXED = 2
+
+
+def tc_selftest():
+    """(dft error, first-stage GEMM error) of the tensor-core DFT path on
+    this device, relative to each line's norm (cvm_tc_selftest)."""
+    a, b = C.c_double(), C.c_double()
+    _check(lib().cvm_tc_selftest(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def device_status() -> int:
+    """1 when a tensor-core kernel gave up waiting since the last call."""
+    v = C.c_int()
+    _check(lib().cvm_device_status(C.byref(v)))
+    return v.value
 
 
 def SetForm(form: int) -> int:
     """Arithmetic of one-shot matches and Matcher.Find, process-wide
-    (cvm_set_form): FORM_EXACT (default, the reference's bits) or
-    FORM_FAST.  Returns the previous form."""
+    (cvm_set_form): FORM_EXACT (default, the reference's bits), FORM_FAST,
+    or FORM_MIXED (the fast form with its 1024-point inverse row transforms
+    on the tensor cores).  Returns the previous form."""
     prev = lib().cvm_get_form()
     _check(lib().cvm_set_form(form))
     return prev
@@ -334,7 +353,8 @@ class Fleet:
 
     def SetForm(self, form: int):
         """FORM_EXACT (default: the reference's float32 arithmetic, bit for
-        bit) or FORM_FAST (zero-mean templates, channels summed in the
+        bit), FORM_MIXED (FORM_FAST with its 1024-point inverse rows on the
+        tensor cores) or FORM_FAST (zero-mean templates, channels summed in the
         frequency domain; see cvm_fleet_set_form)."""
         _check(lib().cvm_fleet_set_form(self._h, form))
 

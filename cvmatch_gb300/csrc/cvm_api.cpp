@@ -279,6 +279,19 @@ int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G) {
     return CVM_OK;
 }
 
+// The fast and mixed forms run the length-specialised kernels only
+// (transforms of 2^5 .. 2^12 points); a plan with a longer transform (a
+// template over ~4000 pixels on a side) runs the exact form's kernels
+// instead -- the reference's own arithmetic, bit for bit -- for that match
+// or fleet bucket.
+bool fast_sizes_ok(const Geom &G) {
+    for (int c = 0; c < G.nclass; c++)
+        if (G.fc[c].log2n < 5 || G.fc[c].log2n > 12 || G.fc[c].log2H < 5 || G.fc[c].log2H > 12) return false;
+    return true;
+}
+
+int effective_form(int form, const Geom &G) { return form != CVM_FORM_EXACT && !fast_sizes_ok(G) ? CVM_FORM_EXACT : form; }
+
 // Geometry that loads one template as a single tile (template spectra).
 void template_geom(const Geom &G, int tw, int th, TileGeom &tg, FftClass &tf) {
     tg = TileGeom();
@@ -373,15 +386,12 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                    Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
                    Arena::bytes((size_t)rw * rh, sizeof(float2)) + (bElems ? Arena::bytes(bElems, sizeof(unsigned int)) : 0);
-    const bool fast = J.form != CVM_FORM_EXACT;
+    // (a Matcher's cached spectra were built for the same effective form)
+    const int form = effective_form(J.form, *G);
+    const bool fast = form != CVM_FORM_EXACT;
     // one channel: the fused forward + conj-multiply + inverse column pass
     // already yields the single correlation spectrum the fast form sums to
     const bool fastSum = fast && !(J.mode == 0 && J.cnFixed == 1);
-    if (fast)
-        for (int c = 0; c < G->nclass; c++)
-            if (G->fc[c].log2n < 5 || G->fc[c].log2n > 12 || G->fc[c].log2H < 5 || G->fc[c].log2H > 12)
-                return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: fast form needs transforms of 32..4096 (%dx%d)",
-                            G->fc[c].n, G->fc[c].dftH);
     for (int c = 0; c < G->nclass; c++) {
         bytes += Arena::bytes(spec_elems(G->fc[c], cnS), sizeof(float2));
         if (fastSum) bytes += Arena::bytes(spec_elems(G->fc[c], 1), sizeof(float2));
@@ -432,7 +442,7 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     ms.map = J.map;
     ms.lanes = lanes;
     ms.lanesStride = 0;
-    ms.form = fast ? 1 : 0;
+    ms.form = form;
     // One short launch (k_prep: the template statistics, the parent's
     // alpha scan, the channel count) on st, then chains: the frame's row
     // transform (on st, or on the rows stream beside k_prep); the template
@@ -866,7 +876,7 @@ int matcher_geom(cvm_matcher *m, int rw, int rh, int form, std::shared_ptr<Match
         CVM_CUDA(cudaMalloc(&g->ts[c], tspec_elems(g->G.fc[c], cnS) * sizeof(float2)));
     cudaStream_t st = thread_stream();
     CVM_TRY(build_tspec(g->G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, cnS, nullptr, g->ts[0],
-                        g->ts[1], st, form != CVM_FORM_EXACT ? m->tsum : nullptr));
+                        g->ts[1], st, effective_form(form, g->G) != CVM_FORM_EXACT ? m->tsum : nullptr));
     CVM_CUDA(cudaStreamSynchronize(st));
     m->geom = g;
     out = g;
@@ -913,6 +923,7 @@ int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, 
 
 struct FleetBucketGeom {
     Geom G;
+    int form = CVM_FORM_EXACT;    // the fleet's form, or exact where the plan exceeds the fast kernels
     SepGrid sg;
     int nparts = 0, partOff[2] = {0, 0};
     int rwMax = 0, rhMax = 0;
@@ -1005,11 +1016,8 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         auto bg = std::make_unique<FleetBucketGeom>();
         const int rwF = pw - b.tw + 1, rhF = ph - b.th + 1;
         CVM_TRY(make_geom(b.tw, b.th, rwF, rhF, b.th, bg->G));
-        if (f->form != CVM_FORM_EXACT)
-            for (int c = 0; c < bg->G.nclass; c++)
-                if (bg->G.fc[c].log2n < 5 || bg->G.fc[c].log2n > 12 || bg->G.fc[c].log2H < 5 || bg->G.fc[c].log2H > 12)
-                    return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: fast form needs transforms of 32..4096 (%dx%d)",
-                                bg->G.fc[c].n, bg->G.fc[c].dftH);
+        bg->form = effective_form(f->form, bg->G);
+        const bool bfast = bg->form != CVM_FORM_EXACT;
         bg->cnS = f->step;
         bg->members = b.members;
         const Geom &G = bg->G;
@@ -1022,7 +1030,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         for (int c = 0; c < G.nclass; c++) {
             int P = 0;
             bg->partOff[c] = nparts;
-            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P, f->form != CVM_FORM_EXACT);
+            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P, bfast);
         }
         bg->nparts = nparts;
         std::vector<DevMember> tab(b.members.size());
@@ -1034,7 +1042,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
                 bg->ts.push_back(t[c]);
             }
             CVM_TRY(build_tspec(G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, bg->cnS, nullptr,
-                                t[0], t[1], st, f->form != CVM_FORM_EXACT ? m->tsum : nullptr));
+                                t[0], t[1], st, bfast ? m->tsum : nullptr));
             DevMember &d = tab[pos];
             memset(&d, 0, sizeof d);
             d.tspec[0] = t[0];
@@ -1054,7 +1062,7 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         CVM_CUDA(cudaMemcpy(bg->table, tab.data(), tab.size() * sizeof(DevMember), cudaMemcpyHostToDevice));
         // the fast form's member tails keep one channel-summed spectrum per tile
         for (int c = 0; c < G.nclass; c++)
-            bg->memberScratch[c] = spec_elems(G.fc[c], f->form != CVM_FORM_EXACT ? 1 : bg->cnS);
+            bg->memberScratch[c] = spec_elems(G.fc[c], bfast ? 1 : bg->cnS);
         fg->bg.push_back(std::move(bg));
     }
     CVM_CUDA(cudaStreamSynchronize(st));
@@ -1156,7 +1164,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
-        const bool fast = fg->form != CVM_FORM_EXACT;
+        const bool fast = bg.form != CVM_FORM_EXACT;
         float2 *frame[2] = {nullptr, nullptr};
         float2 *scratch[2] = {nullptr, nullptr};
         float2 *lanes = nullptr;
@@ -1190,7 +1198,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         ms.lanes = lanes;
         ms.lanesStride = (size_t)bg.rwMax * bg.rhMax;
         ms.anyRoi = !f->roi.empty();
-        ms.form = fast ? 1 : 0;
+        ms.form = bg.form;
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -1620,7 +1628,7 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
 
 int cvm_set_form(int form) {
-    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST)
+    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST && form != CVM_FORM_MIXED)
         return fail(CVM_ERR_ARGS, "cvmatch_gpu: unknown form %d", form);
     g_soloForm.store(form, std::memory_order_relaxed);
     return CVM_OK;
@@ -1628,9 +1636,26 @@ int cvm_set_form(int form) {
 
 int cvm_get_form(void) { return solo_form(); }
 
+int cvm_tc_selftest(double *dft_err, double *gemm_err) {
+    CVM_TRY(ensure_device());
+    double a = 0, b = 0;
+    CVM_CUDA(tc_selftest(&a, &b));
+    if (dft_err) *dft_err = a;
+    if (gemm_err) *gemm_err = b;
+    return CVM_OK;
+}
+
+int cvm_device_status(int *tc_timeouts) {
+    CVM_TRY(ensure_device());
+    const int v = tc_error_read_clear();
+    if (v < 0) return fail(CVM_ERR_CUDA, "cvmatch_gpu: reading the device status failed");
+    if (tc_timeouts) *tc_timeouts = v;
+    return CVM_OK;
+}
+
 int cvm_fleet_set_form(cvm_fleet *f, int form) {
     if (!f) return fail(CVM_ERR_EMPTY_FLEET, "cvmatch: empty fleet");
-    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST)
+    if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST && form != CVM_FORM_MIXED)
         return fail(CVM_ERR_ARGS, "cvmatch_gpu: unknown fleet form %d", form);
     std::lock_guard<std::mutex> lk(f->mu);
     if (f->form != form) {

@@ -111,7 +111,9 @@ struct MemberSet {
     int anyRoi;                // some member of the launch has a region of interest
     // 0: the reference's arithmetic (per-channel inverses, num = corr - t);
     // 1: the fast form (zero-mean template spectra, channels summed in the
-    // frequency domain, one inverse per tile, num = corr)
+    // frequency domain, one inverse per tile, num = corr); 2: the mixed
+    // form (the fast form with its 1024-point inverse rows on the tensor
+    // cores).  Nonzero selects the fast form's arithmetic everywhere else.
     int form;
 };
 
@@ -232,6 +234,15 @@ cudaError_t launch_shrink_gather(const float2 *src, int dftH, float2 *dst, int d
 size_t peaks_scratch_ints(int w, int h);
 cudaError_t launch_peaks(const float *map, int w, int h, float thresh, int rx, int ry, int *scratch, int32_t *xy,
                          int maxPeaks, int *count, cudaStream_t st);
+
+// The mixed form's inverse rows on the tensor cores (cvm_tc.cu): applies
+// to 1024-point rows of a fused (lanes) launch in CVM_FORM_MIXED; same grid
+// and partial records as the FP32 kernel.
+struct InvArgs;
+bool inv_rows_tc_applies(const FftClass &fc, const MemberSet &ms);
+cudaError_t launch_inv_rows_tc(const InvArgs &a, dim3 grid, cudaStream_t st);
+cudaError_t tc_selftest(double *dftErr, double *gemmErr);
+int tc_error_read_clear();
 
 // kernel-launch counter (exported by cvm_launch_count)
 void count_launches(unsigned n);

@@ -2010,6 +2010,12 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.counters = counters;
     a.out = out;
     dim3 grid(ctas, fc.ntiles, nmembers);
+    if (inv_rows_tc_applies(fc, ms)) {
+        ProfScope ps("k_inv_rows_tc", st);
+        const cudaError_t e = launch_inv_rows_tc(a, grid, st);
+        count_launches(1);
+        return e != cudaSuccess ? e : cudaGetLastError();
+    }
     const size_t smem = (size_t)P * (padded_len(fc.n) * sizeof(float2) + (wide ? 0 : 2 * fc.n * sizeof(float)));
     ProfScope ps("k_inv_rows", st);
     if (rows_fixed_length(fc.log2n)) {

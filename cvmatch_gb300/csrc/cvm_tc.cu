@@ -1,0 +1,595 @@
+// cvm_tc.cu -- the mixed form's inverse row transforms on the tensor cores.
+//
+// The fast form's member tail inverts each tile's channel-summed spectrum
+// row pair by row pair: the combine of inverseRowPair (impl.go:405-413)
+// packs two spectrum rows into one complex 1024-point line z, whose
+// inverse DFT x carries result row 2p in its real part and row 2p+1 in
+// its imaginary part (impl.go:425-443); the FP32 form runs it as the
+// radix-4 cascade (cvm_rows.cu).  Here the same inverse DFT runs as two
+// dense 32-point DFT stages on the tensor cores (the four-step
+// factorisation 1024 = 32 x 32):
+//
+//   k = 32 k1 + k2, n = n1 + 32 n2, w = e^{+2 pi i / 1024}, w32 = w^32
+//   Y[n1, k2]        = sum_k1 z[32 k1 + k2] w32^(n1 k1)        (stage 1: MMA)
+//   Y[n1, k2]       *= w^(n1 k2)                               (twiddle: FP32)
+//   x[n1 + 32 n2]    = sum_k2 Y[n1, k2] w32^(n2 k2)            (stage 2: MMA)
+//
+// Each stage is one real GEMM D[128 x 64] = A[128 x 64] B[64 x 64] per four
+// transforms: A's rows are (transform, k2) (stage 1) or (transform, n1)
+// (stage 2) with K = 32 complex inputs as (re[32], im[32]); B is the
+// 32-point DFT matrix in real block form (out re = in re cos - in im sin,
+// out im = in re sin + in im cos); D's 64 columns are the 32 complex
+// outputs as (re[32], im[32]).  tcgen05.mma kind::tf32 multiplies 19-bit
+// operands, so every operand is split as hi = rna_tf32(v), lo = v - hi and
+// the products are accumulated as Ahi Bhi + Alo Bhi + Ahi Blo in FP32 (in
+// TMEM): the representation error is ~2^-22 of each operand, the FP32
+// cascade's order.  One thread issues the MMAs; tcgen05.commit arrives on
+// an mbarrier the CTA waits on (a bounded wait: after ~2 s without the
+// arrival it records a device error, frees its TMEM and returns); D comes
+// back from TMEM with tcgen05.ld.  Operands are staged in shared memory in
+// the K-major, no-swizzle core-matrix layout (8 rows x 16 bytes per core
+// matrix), A with a 144-byte K stride so the transposed stores between the
+// stages are free of bank conflicts.
+//
+// The epilogue is the FP32 kernel's: normOne's ladder from the den lanes
+// of the statistics kernel, first-occurrence extrema, the member's result
+// from its last CTA.  Scores differ from the FP32 fast form by rounding.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "cvm_device.cuh"
+
+namespace cvm {
+namespace {
+
+constexpr int kTcThreads = 128;  // one warpgroup: warp w owns TMEM lanes 32w..32w+31
+constexpr int kTcM = 128;        // MMA rows: 4 transforms x 32
+constexpr int kTcTrans = 4;      // transforms per MMA tile
+constexpr uint32_t kTcCols = 64; // TMEM columns: D is 128 lanes x 64 fp32
+// Operand layouts (bytes).  Core matrix (row group g, K chunk c of 4 tf32)
+// at g * SBO + c * LBO; row r % 8 at +16 (r % 8), element k % 4 at +4 (k % 4).
+constexpr uint32_t A_LBO = 144, A_SBO = 16 * A_LBO, A_BYTES = (kTcM / 8) * A_SBO;   // 36864
+constexpr uint32_t B_LBO = 128, B_SBO = 16 * B_LBO, B_BYTES = (64 / 8) * B_SBO;     // 16384
+constexpr uint32_t OFF_AHI = 0, OFF_ALO = A_BYTES, OFF_BHI = 2 * A_BYTES, OFF_BLO = 2 * A_BYTES + B_BYTES;
+constexpr uint32_t OFF_TW = 2 * A_BYTES + 2 * B_BYTES;     // quarter-wave cosine table, 257 floats
+constexpr uint32_t TC_SMEM = OFF_TW + 1040;                 // + alignment slack below
+constexpr size_t kTcSmemLaunch = TC_SMEM + 1024;
+
+__device__ int g_tc_error = 0;  // a tensor-core wait that gave up (sticky until read and cleared)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint32_t a_off(int row, int k) {
+    return (uint32_t)(row >> 3) * A_SBO + (uint32_t)(k >> 2) * A_LBO + (uint32_t)(row & 7) * 16u + (uint32_t)(k & 3) * 4u;
+}
+__device__ __forceinline__ uint32_t b_off(int n, int k) {
+    return (uint32_t)(n >> 3) * B_SBO + (uint32_t)(k >> 2) * B_LBO + (uint32_t)(n & 7) * 16u + (uint32_t)(k & 3) * 4u;
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (row-group) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::tf32: D f32, A and B tf32, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ float tf32_hi(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, int accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(accum), "r"(kIdesc));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the mbarrier phase; gives up after ~2^32 cycles (about 2 s),
+// recording the failure in g_tc_error.
+__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
+    const uint32_t addr = smem_u32(bar);
+    const long long t0 = clock64();
+    for (unsigned it = 0;; it++) {
+        if (mbar_try(addr, phase)) return true;
+        if ((it & 255u) == 255u && clock64() - t0 > (1ll << 32)) {
+            atomicExch(&g_tc_error, 1);
+            return false;
+        }
+    }
+}
+
+// 64 consecutive TMEM columns of this warp's 32 lanes, one lane per
+// thread.  The load and its wait are one asm statement, so no use of the
+// registers can be scheduled before the data has arrived.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float *v) {
+    uint32_t r[64];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// cos(2 pi j / 1024) and sin(2 pi j / 1024) from the quarter-wave table
+// q[i] = cos(2 pi i / 1024), i = 0..256.
+__device__ __forceinline__ float2 tw1024(const float *q, int j) {
+    j &= 1023;
+    const int r = j & 255, qd = j >> 8;
+    const float c = q[r], s = q[256 - r];  // cos(t), sin(t) of the reduced angle
+    switch (qd) {
+        case 0: return make_float2(c, s);
+        case 1: return make_float2(-s, c);
+        case 2: return make_float2(-c, -s);
+        default: return make_float2(s, -c);
+    }
+}
+
+// The CTA's tensor-core state: TMEM columns, the MMA-completion mbarrier
+// and its phase.
+struct TcState {
+    uint32_t tmem;
+    uint32_t phase;
+    bool ok;
+};
+
+// Fills B (the 32-point inverse DFT in real block form, split hi/lo) and the
+// twiddle table; allocates TMEM (warp 0) and initialises the mbarrier.
+__device__ void tc_setup(unsigned char *sm, uint64_t *bar, uint32_t *tmemSlot, TcState &s) {
+    const int tid = threadIdx.x;
+    float *q = reinterpret_cast<float *>(sm + OFF_TW);
+    for (int i = tid; i <= 256; i += blockDim.x) {
+        float sv, cv;
+        sincospif((float)i / 512.f, &sv, &cv);
+        q[i] = cv;
+    }
+    if (tid < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)),
+                     "r"(kTcCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // B[n][k]: n = output (re 0..31, im 32..63), k = input (re 0..31, im 32..63)
+    for (int i = tid; i < 64 * 64; i += blockDim.x) {
+        const int n = i >> 6, k = i & 63, n1 = n & 31, k1 = k & 31;
+        const float2 w = tw1024(q, 32 * ((n1 * k1) & 31));  // w32^(n1 k1)
+        float v;
+        if (n < 32)
+            v = k < 32 ? w.x : -w.y;
+        else
+            v = k < 32 ? w.y : w.x;
+        const float hi = tf32_hi(v);
+        *reinterpret_cast<float *>(sm + OFF_BHI + b_off(n, k)) = hi;
+        *reinterpret_cast<float *>(sm + OFF_BLO + b_off(n, k)) = tf32_hi(v - hi);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    s.tmem = *tmemSlot;
+    s.phase = 0;
+    s.ok = true;
+}
+
+__device__ void tc_teardown(const TcState &s) {
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s.tmem), "r"(kTcCols));
+}
+
+// Stores 4 consecutive K elements (k0 % 4 == 0) of A row `row`, split.
+__device__ __forceinline__ void a_store4(unsigned char *sm, int row, int k0, float v0, float v1, float v2, float v3) {
+    const float h0 = tf32_hi(v0), h1 = tf32_hi(v1), h2 = tf32_hi(v2), h3 = tf32_hi(v3);
+    const uint32_t o = a_off(row, k0);
+    *reinterpret_cast<float4 *>(sm + OFF_AHI + o) = make_float4(h0, h1, h2, h3);
+    *reinterpret_cast<float4 *>(sm + OFF_ALO + o) =
+        make_float4(tf32_hi(v0 - h0), tf32_hi(v1 - h1), tf32_hi(v2 - h2), tf32_hi(v3 - h3));
+}
+
+__device__ __forceinline__ void a_store1(unsigned char *sm, int row, int k, float v) {
+    const float h = tf32_hi(v);
+    const uint32_t o = a_off(row, k);
+    *reinterpret_cast<float *>(sm + OFF_AHI + o) = h;
+    *reinterpret_cast<float *>(sm + OFF_ALO + o) = tf32_hi(v - h);
+}
+
+// One stage: D = Ahi Bhi + Alo Bhi + Ahi Blo over K = 64 (8 steps of 8),
+// issued by thread 0, completion on the mbarrier; every thread then waits.
+// The caller has stored A (fence.proxy.async by every writer) and
+// synchronised.
+__device__ void tc_stage(unsigned char *sm, uint64_t *bar, TcState &s) {
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t base = smem_u32(sm);
+#pragma unroll
+        for (int ks = 0; ks < 8; ks++) {
+            const uint64_t ah = sdesc(base + OFF_AHI + ks * 2 * A_LBO, A_LBO, A_SBO);
+            const uint64_t al = sdesc(base + OFF_ALO + ks * 2 * A_LBO, A_LBO, A_SBO);
+            const uint64_t bh = sdesc(base + OFF_BHI + ks * 2 * B_LBO, B_LBO, B_SBO);
+            const uint64_t bl = sdesc(base + OFF_BLO + ks * 2 * B_LBO, B_LBO, B_SBO);
+            mma_tf32(s.tmem, ah, bh, ks > 0);
+            mma_tf32(s.tmem, al, bh, 1);
+            mma_tf32(s.tmem, ah, bl, 1);
+        }
+        tc_commit(bar);
+    }
+    if (s.ok) s.ok = mbar_wait(bar, s.phase);
+    s.phase ^= 1;
+    tc_fence_after();
+}
+
+// After stage 1: thread (warp w, lane k2) reads Y[., k2] of transform w,
+// applies the twiddles w^(n1 k2) and stores the stage-2 operand: row
+// 32 w + n1, K = k2 (re) and 32 + k2 (im).
+__device__ void tc_twiddle_transpose(unsigned char *sm, const TcState &s) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float *q = reinterpret_cast<const float *>(sm + OFF_TW);
+    float y[64];
+    tmem_ld64(s.tmem + ((uint32_t)(32 * warp) << 16), y);
+#pragma unroll
+    for (int n1 = 0; n1 < 32; n1++) {
+        const float2 w = tw1024(q, n1 * lane);
+        const float yr = y[n1], yi = y[32 + n1];
+        const float tr = fmaf(yr, w.x, -yi * w.y), ti = fmaf(yr, w.y, yi * w.x);
+        a_store1(sm, 32 * warp + n1, lane, tr);
+        a_store1(sm, 32 * warp + n1, 32 + lane, ti);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+}
+
+// After stage 2: thread (warp w, lane n1) gets x[n1 + 32 n2] of transform w
+// as re[n2] = v[n2], im[n2] = v[32 + n2].
+__device__ __forceinline__ void tc_result(const TcState &s, float *v) {
+    const int warp = threadIdx.x >> 5;
+    tmem_ld64(s.tmem + ((uint32_t)(32 * warp) << 16), v);
+}
+
+// ------------------------------------------------------------ self-test
+
+// Four inverse 1024-point DFTs of z (natural order, complex) into x, and
+// the first stage's raw GEMM tile (D of stage 1) into d1 (128 x 64).
+__global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const float2 *__restrict__ z, float2 *__restrict__ x,
+                                                              float *__restrict__ d1) {
+    extern __shared__ unsigned char smraw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemSlot;
+    TcState s;
+    tc_setup(sm, &bar, &tmemSlot, s);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // stage-1 operand: row 32 w + k2, K = k1 (re), 32 + k1 (im)
+    {
+        const float2 *zt = z + warp * 1024;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            float2 e[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) e[i] = zt[32 * (4 * c + i) + lane];
+            a_store4(sm, 32 * warp + lane, 4 * c, e[0].x, e[1].x, e[2].x, e[3].x);
+            a_store4(sm, 32 * warp + lane, 32 + 4 * c, e[0].y, e[1].y, e[2].y, e[3].y);
+        }
+    }
+    fence_async_smem();
+    __syncthreads();
+    tc_stage(sm, &bar, s);
+    {
+        float v[64];
+        tc_result(s, v);
+#pragma unroll
+        for (int i = 0; i < 64; i++) d1[(32 * warp + lane) * 64 + i] = v[i];
+    }
+    tc_twiddle_transpose(sm, s);
+    tc_stage(sm, &bar, s);
+    float v[64];
+    tc_result(s, v);
+#pragma unroll
+    for (int n2 = 0; n2 < 32; n2++) x[warp * 1024 + lane + 32 * n2] = make_float2(v[n2], v[32 + n2]);
+    tc_teardown(s);
+}
+
+// --------------------------------------------------------- inverse rows
+
+// The fast form's fused inverse rows (k_inv_rows_t<10, true> with the
+// radix-4 cascade replaced): four row pairs per MMA tile, pairsPerCta row
+// pairs per CTA (the same grid and partial records as the FP32 kernel).
+__global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
+    griddep_wait();
+    constexpr int N = 1024, HALF = 512;
+    extern __shared__ unsigned char smraw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemSlot;
+    __shared__ Ext shExt[kTcThreads / 32];
+    __shared__ int isLast;
+    const FftClass &fc = a.fc;
+    const int tileLocal = blockIdx.y;
+    const int tile = fc.tileFirst + tileLocal;
+    const int slot = blockIdx.z;
+    const DevMember &m = member_of(a.ms, slot);
+    const DevParams &Pm = a.ms.params[m.pIdx];
+    const TileBox tb = tile_box(a.g, tile);
+    const int tx = tile % a.g.ntx, ty = tile / a.g.ntx;
+    const int bw = (tx == a.g.ntx - 1) ? m.rw - tb.x0 : a.g.blockW;
+    const int bh = (ty == a.g.nty - 1) ? m.rh - tb.y0 : a.g.blockH;
+    const int pair0 = blockIdx.x * a.pairsPerCta;
+    int P = 2 * pair0 < bh ? min(a.pairsPerCta, (bh - 2 * pair0 + 1) >> 1) : 0;
+    if (P > 0 && a.ms.anyRoi) {
+        const int ya = tb.y0 + 2 * pair0, yb = tb.y0 + min(2 * (pair0 + P), bh);
+        if (ya >= m.roiY1 || yb <= m.roiY0 || tb.x0 >= m.roiX1 || tb.x0 + bw <= m.roiX0) P = 0;
+    }
+    const bool flat = Pm.flat != 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int log2H = fc.log2H, hwp = fc.hwp;
+    const float2 *cb = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] +
+                       (size_t)tileLocal * a.cnS * fc.dftH * hwp;
+    const float *dens = reinterpret_cast<const float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride);
+    float *map = a.ms.map;
+    const int xlo = m.roiX0 - tb.x0, xhi = m.roiX1 - tb.x0;
+    Ext e;
+    ext_init(e);
+    if (flat) {
+        // a flat template scores 1 everywhere (impl.go:1137-1144)
+        for (int rr = 0; rr < 2 * P; rr++) {
+            const int r = 2 * pair0 + rr;
+            if (r >= bh) break;
+            const long long rowBase = (long long)(tb.y0 + r) * m.rw + tb.x0;
+            for (int x = threadIdx.x; x < bw; x += kTcThreads) {
+                if (map) map[rowBase + x] = 1.f;
+                if (x >= xlo && x < xhi) ext_add_inc(e, 1.f, rowBase + x);
+            }
+        }
+    } else if (P > 0) {
+        TcState s;
+        tc_setup(sm, &bar, &tmemSlot, s);
+        for (int t0 = 0; t0 < P; t0 += kTcTrans) {
+            // stage-1 operand from the combine (impl.go:405-413): thread
+            // (w, k2) builds row 32 w + k2 = z[32 k1 + k2], k1 = 0..31, of
+            // row pair t0 + w
+            const int p = t0 + warp;
+            const bool live = p < P;
+            const int r = 2 * (pair0 + p);
+            const float2 *u = cb + (size_t)brev_bits(r, log2H) * hwp;
+            const float2 *v = cb + (size_t)brev_bits(r + 1, log2H) * hwp;
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                float zr[4], zi[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int k = 32 * (4 * c + i) + lane;
+                    float2 U = make_float2(0.f, 0.f), V = U;
+                    if (live) {
+                        const int kk = k <= HALF ? k : N - k;
+                        U = __ldg(u + kk);
+                        V = __ldg(v + kk);
+                    }
+                    if (k <= HALF) {
+                        zr[i] = U.x - V.y;
+                        zi[i] = U.y + V.x;
+                    } else {
+                        zr[i] = U.x + V.y;
+                        zi[i] = V.x - U.y;
+                    }
+                }
+                a_store4(sm, 32 * warp + lane, 4 * c, zr[0], zr[1], zr[2], zr[3]);
+                a_store4(sm, 32 * warp + lane, 32 + 4 * c, zi[0], zi[1], zi[2], zi[3]);
+            }
+            fence_async_smem();
+            __syncthreads();
+            tc_stage(sm, &bar, s);
+            tc_twiddle_transpose(sm, s);
+            tc_stage(sm, &bar, s);
+            // den of the thread's results first (x = lane + 32 n2): their
+            // loads overlap the TMEM read
+            float den[2][32];
+            long long rowBase[2];
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                const int rr = r + half;
+                rowBase[half] = (long long)(tb.y0 + rr) * m.rw + tb.x0;
+#pragma unroll
+                for (int n2 = 0; n2 < 32; n2++) {
+                    const int x = lane + 32 * n2;
+                    den[half][n2] = (live && rr < bh && x < bw) ? __ldg(dens + rowBase[half] + x) : 0.f;
+                }
+            }
+            float xv[64];
+            tc_result(s, xv);
+            if (live && s.ok) {
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    const int rr = r + half;
+                    if (rr >= bh) break;
+                    const int yy = tb.y0 + rr;
+                    if (yy < m.roiY0 || yy >= m.roiY1) continue;
+#pragma unroll
+                    for (int n2 = 0; n2 < 32; n2++) {
+                        const int x = lane + 32 * n2;
+                        if (x < bw) {
+                            const float num = xv[32 * half + n2], dn = den[half][n2], an = fabsf(num);
+                            float score;
+                            if (an < dn)
+                                score = __fdividef(num, dn);
+                            else if (an < dn * 1.125f)
+                                score = num > 0.f ? 1.f : -1.f;
+                            else
+                                score = 0.f;
+                            if (map) map[rowBase[half] + x] = score;
+                            if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase[half] + x);
+                        }
+                    }
+                }
+            }
+            // the next tile's stores overwrite A and its MMAs D
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+        }
+        tc_teardown(s);
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (threadIdx.x == 0) {
+        Partial &o = a.partials[m.partBase + a.partOffset + tileLocal * gridDim.x + blockIdx.x];
+        o.minV = e.minV;
+        o.maxV = e.maxV;
+        o.minI = e.minI;
+        o.maxI = e.maxI;
+        __threadfence();
+        isLast = atomicAdd(&a.counters[m.pIdx], 1) == a.nparts - 1;
+    }
+    __syncthreads();
+    if (!isLast) return;
+    __threadfence();
+    ext_init(e);
+    for (int i = threadIdx.x; i < a.nparts; i += kTcThreads) {
+        const volatile Partial *pp = a.partials + m.partBase + i;
+        Ext o;
+        o.minV = pp->minV;
+        o.maxV = pp->maxV;
+        o.minI = pp->minI;
+        o.maxI = pp->maxI;
+        ext_merge(e, o);
+    }
+    __syncthreads();
+    ext_block_reduce(e, shExt);
+    if (threadIdx.x == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
+}
+
+}  // namespace
+
+bool inv_rows_tc_applies(const FftClass &fc, const MemberSet &ms) {
+    return ms.form == CVM_FORM_MIXED && fc.log2n == 10 && ms.lanes != nullptr;
+}
+
+cudaError_t launch_inv_rows_tc(const InvArgs &a, dim3 grid, cudaStream_t st) {
+    set_smem(k_inv_rows_tc, kTcSmemLaunch);
+    return launch_k(k_inv_rows_tc, grid, dim3(kTcThreads), kTcSmemLaunch, st, a);
+}
+
+int tc_error_read_clear() {
+    int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof v) != cudaSuccess) return -1;
+    if (v) cudaMemcpyToSymbol(g_tc_error, &z, sizeof z);
+    return v;
+}
+
+// Runs the self-test kernel on four pseudo-random lines and compares with
+// the DFT in double precision; returns 0 and the largest errors relative to
+// each line's norm, or a CUDA error.
+cudaError_t tc_selftest(double *dftErr, double *gemmErr) {
+    const int T = 4, N = 1024;
+    std::vector<float2> z(T * N);
+    uint32_t st = 12345u;
+    for (auto &c : z) {
+        st = st * 1664525u + 1013904223u;
+        c.x = (float)((int)(st >> 8) % 2001 - 1000) * 0.37f;
+        st = st * 1664525u + 1013904223u;
+        c.y = (float)((int)(st >> 8) % 2001 - 1000) * 0.37f;
+    }
+    float2 *dz = nullptr, *dx = nullptr;
+    float *dd = nullptr;
+    cudaError_t e = cudaMalloc(&dz, T * N * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&dx, T * N * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&dd, 128 * 64 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dz, z.data(), T * N * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)kTcSmemLaunch);
+    if (e == cudaSuccess) {
+        k_tc_selftest<<<1, kTcThreads, kTcSmemLaunch>>>(dz, dx, dd);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    std::vector<float2> x(T * N);
+    std::vector<float> d(128 * 64);
+    if (e == cudaSuccess) e = cudaMemcpy(x.data(), dx, T * N * sizeof(float2), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(d.data(), dd, 128 * 64 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dz);
+    cudaFree(dx);
+    cudaFree(dd);
+    if (e != cudaSuccess) return e;
+    const double PI2 = 6.283185307179586476925286766559;
+    double worstX = 0, worstD = 0;
+    for (int t = 0; t < T; t++) {
+        double norm = 0;
+        for (int k = 0; k < N; k++) norm += (double)z[t * N + k].x * z[t * N + k].x + (double)z[t * N + k].y * z[t * N + k].y;
+        norm = std::sqrt(norm);
+        for (int n = 0; n < N; n++) {
+            double re = 0, im = 0;
+            for (int k = 0; k < N; k++) {
+                const double th = PI2 * (double)((long long)n * k % N) / N, c = std::cos(th), s = std::sin(th);
+                re += z[t * N + k].x * c - z[t * N + k].y * s;
+                im += z[t * N + k].x * s + z[t * N + k].y * c;
+            }
+            const double err = std::hypot(x[t * N + n].x - re, x[t * N + n].y - im) / norm;
+            if (err > worstX) worstX = err;
+        }
+        // stage 1 alone: D[32 t + k2][n] for the 32-point DFTs over k1
+        for (int k2 = 0; k2 < 32; k2++) {
+            double n1norm = 0;
+            for (int k1 = 0; k1 < 32; k1++) {
+                const float2 c = z[t * N + 32 * k1 + k2];
+                n1norm += (double)c.x * c.x + (double)c.y * c.y;
+            }
+            n1norm = std::sqrt(n1norm) + 1e-30;
+            for (int n1 = 0; n1 < 32; n1++) {
+                double re = 0, im = 0;
+                for (int k1 = 0; k1 < 32; k1++) {
+                    const float2 c = z[t * N + 32 * k1 + k2];
+                    const double th = PI2 * (double)((n1 * k1) % 32) / 32, cs = std::cos(th), sn = std::sin(th);
+                    re += c.x * cs - c.y * sn;
+                    im += c.x * sn + c.y * cs;
+                }
+                const float *row = &d[(32 * t + k2) * 64];
+                const double err = std::hypot(row[n1] - re, row[32 + n1] - im) / n1norm;
+                if (err > worstD) worstD = err;
+            }
+        }
+    }
+    *dftErr = worstX;
+    *gemmErr = worstD;
+    return cudaSuccess;
+}
+
+}  // namespace cvm

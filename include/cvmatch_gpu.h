@@ -227,9 +227,11 @@ int cvm_fleet_set_roi(cvm_fleet *f, int member, int x, int y, int w, int h);
  * ladder stay those of normOne.  Scores then differ from the reference's
  * by rounding only (bounded against the FP64 definition in the tests).
  * Changing the form drops the fleet's cached spectra; not to be called
- * while a FindAll on the same fleet runs.  Transform sizes above 4096
- * are CVM_ERR_UNSUPPORTED in the fast form. */
-enum { CVM_FORM_EXACT = 0, CVM_FORM_FAST = 1 };
+ * while a FindAll on the same fleet runs.  A bucket (or one-shot match)
+ * whose plan needs transforms above 4096 points -- templates over ~4000
+ * pixels on a side -- runs the exact form's kernels instead, whatever the
+ * form: its scores are then the reference's bits. */
+enum { CVM_FORM_EXACT = 0, CVM_FORM_FAST = 1, CVM_FORM_MIXED = 2 };
 int cvm_fleet_set_form(cvm_fleet *f, int form);
 
 /* The same choice for one-shot matches (cvm_match, cvm_match_map,
@@ -244,6 +246,27 @@ int cvm_fleet_set_form(cvm_fleet *f, int form);
  * form. */
 int cvm_set_form(int form);
 int cvm_get_form(void);
+
+/* CVM_FORM_MIXED (fleets and one-shot matches alike) is the fast form with
+ * its 1024-point inverse row transforms -- the inverse DFT of inverseRowPair
+ * (impl.go:394-444) -- run on the tensor cores: two 32-point DFT stages as
+ * tcgen05 tf32 matrix products on operands split hi + lo (three products,
+ * FP32 accumulation), the twiddles between them in FP32.  Other transform
+ * widths run the fast form unchanged.  Scores differ from the fast form's
+ * by rounding only. */
+
+/* Checks the tensor-core DFT path on this device: four inverse 1024-point
+ * DFTs through the kernel's own stages against a double-precision DFT on
+ * the host.  *dft_err and *gemm_err receive the largest errors relative to
+ * each line's norm (of the whole DFT, and of the first GEMM stage alone).
+ * Diagnostic; no reference counterpart. */
+int cvm_tc_selftest(double *dft_err, double *gemm_err);
+
+/* Sticky device-side failure flags since the last call (then cleared):
+ * *tc_timeouts = 1 when a tensor-core kernel gave up waiting for its
+ * matrix products (its results are invalid).  Waits are bounded, so a
+ * failure there returns instead of hanging.  No reference counterpart. */
+int cvm_device_status(int *tc_timeouts);
 
 /* ------------------------------------------------------- frame streams */
 

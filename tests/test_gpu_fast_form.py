@@ -311,17 +311,24 @@ def test_fast_large_gray_template_mean_subtracted(fast_form):
     assert (jx, jy) == (150, 100)
 
 
-def test_fast_form_refuses_transforms_above_4096(fast_form):
-    """A 4100-px-wide template needs 8192-point row transforms: the exact
-    form runs them (generic kernels), the fast form refuses cleanly."""
+def test_fast_form_routes_transforms_above_4096_to_the_exact_kernels(fast_form):
+    """A 4100-px-wide template needs 8192-point row transforms, beyond the
+    fast form's length-specialised kernels: the match runs the exact form's
+    kernels instead, so its result is the reference's, bit for bit."""
     img = np.ascontiguousarray(scene(79, 60, 4200))
     tpl = img[11:51, 50:4150].copy()
-    with pytest.raises(cvm.CvmatchError) as e:
-        cvm.match_u8(img, tpl, 4)
-    assert e.value.code == 11 and "fast form" in str(e.value)
-    cvm.SetForm(cvm.FORM_EXACT)
-    t, _ = cvm.match_u8(img, tpl, 4, want_map=False)
+    t, m = cvm.match_u8(img, tpl, 4)
+    want, wmap = oracle.match_u8(img, tpl, 4, threads=16)
+    assert t == want and np.array_equal(m.view(np.uint32), wmap.view(np.uint32))
     assert (t[4], t[5]) == (50, 11)
+    # a fleet with such a member and an ordinary one: each bucket in its own form
+    small = img[5:25, 300:340].copy()
+    fleet = cvm.NewFleet(cvm.NewMatcher(tpl), cvm.NewMatcher(small))
+    fleet.SetForm(cvm.FORM_FAST)
+    got = fleet.FindAll(img)
+    ref = oracle.fleet_find_all([tpl, small], img, threads=16)
+    assert tuple(got[0]) == ref[0]
+    check(got[1], oracle.ref_match_f64(img, small, 4, threads=16), "ordinary bucket beside it")
 
 
 # ------------------------------------------ plan classes and buckets, fast form
