@@ -109,6 +109,14 @@ int ensure_device() {
         }
         uint64_t keep = UINT64_MAX;  // keep freed workspace cached for the next call
         cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        // the tensor-core DFT's tables (24 KB), before any call can be
+        // inside a stream capture
+        e = tc_init();
+        if (e != cudaSuccess) {
+            d.status = CVM_ERR_CUDA;
+            d.msg = std::string("cvmatch_gpu: tensor-core tables: ") + cudaGetErrorString(e);
+            return;
+        }
     });
     if (d.status != CVM_OK) return fail(d.status, "%s", d.msg.c_str());
     // The library's state (memory pool, twiddle tables, per-thread

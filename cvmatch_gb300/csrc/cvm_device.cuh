@@ -75,6 +75,7 @@ struct InvArgs {
     Partial *partials;
     int *counters;    // per member params index
     cvm_result *out;
+    const void *tcTab;  // the tensor-core kernel's tables (set by its launcher)
 };
 
 // Arguments of the column kernels (colsR4Go, mulConjGo; mode 0: forward

@@ -242,6 +242,7 @@ struct InvArgs;
 bool inv_rows_tc_applies(const FftClass &fc, const MemberSet &ms);
 cudaError_t launch_inv_rows_tc(const InvArgs &a, dim3 grid, cudaStream_t st);
 cudaError_t tc_selftest(double *dftErr, double *gemmErr);
+cudaError_t tc_init();  // the kernel's device tables, once (device set-up)
 int tc_error_read_clear();
 
 // kernel-launch counter (exported by cvm_launch_count)

@@ -34,8 +34,11 @@
 // The epilogue is the FP32 kernel's: normOne's ladder from the den lanes
 // of the statistics kernel, first-occurrence extrema, the member's result
 // from its last CTA.  Scores differ from the FP32 fast form by rounding.
+#include <cuda_fp16.h>
+
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "cvm_device.cuh"
@@ -47,24 +50,37 @@ constexpr int kTcThreads = 128;  // one warpgroup: warp w owns TMEM lanes 32w..3
 constexpr int kTcM = 128;        // MMA rows: 4 transforms x 32
 constexpr int kTcTrans = 4;      // transforms per MMA tile
 constexpr uint32_t kTcCols = 64; // TMEM columns: D is 128 lanes x 64 fp32
-// Operand layouts (bytes).  Core matrix (row group g, K chunk c of 4 tf32)
-// at g * SBO + c * LBO; row r % 8 at +16 (r % 8), element k % 4 at +4 (k % 4).
-constexpr uint32_t A_LBO = 144, A_SBO = 16 * A_LBO, A_BYTES = (kTcM / 8) * A_SBO;   // 36864
-constexpr uint32_t B_LBO = 128, B_SBO = 16 * B_LBO, B_BYTES = (64 / 8) * B_SBO;     // 16384
+// Operand layouts (bytes, fp16 elements).  Core matrix (row group g, K
+// chunk c of 8 halves) at g * SBO + c * LBO; row r % 8 at +16 (r % 8),
+// element k % 8 at +2 (k % 8).
+constexpr uint32_t A_LBO = 144, A_SBO = 8 * A_LBO, A_BYTES = (kTcM / 8) * A_SBO;   // 18432
+constexpr uint32_t B_LBO = 128, B_SBO = 8 * B_LBO, B_BYTES = (64 / 8) * B_SBO;     // 8192
 constexpr uint32_t OFF_AHI = 0, OFF_ALO = A_BYTES, OFF_BHI = 2 * A_BYTES, OFF_BLO = 2 * A_BYTES + B_BYTES;
-constexpr uint32_t OFF_TW = 2 * A_BYTES + 2 * B_BYTES;     // quarter-wave cosine table, 257 floats
-constexpr uint32_t TC_SMEM = OFF_TW + 1040;                 // + alignment slack below
-constexpr size_t kTcSmemLaunch = TC_SMEM + 1024;
+constexpr uint32_t TC_SMEM = 2 * A_BYTES + 2 * B_BYTES;    // 53248: four CTAs per SM
+constexpr size_t kTcSmemLaunch = TC_SMEM + 1024;           // + alignment slack
+// Per-transform scaling: operands are multiplied by a power of two that
+// puts the transform's largest magnitude just below 2^14 (FP16's range
+// ends at 65504; K = 64 sums of products of magnitude <= 2^14 stay in FP32).
+constexpr int kTcScaleExp = 14;
+
+// The 32-point DFT matrix in real block form (B[n][k]: out re/im n, in
+// re/im k) as the shared-memory image of its FP16 hi and lo halves, and
+// the 1024 twiddles w^j = (cos, sin)(2 pi j / 1024); built once per device
+// from double precision.
+struct TcTables {
+    unsigned char bimg[2 * B_BYTES];
+    float2 tw[1024];
+};
 
 __device__ int g_tc_error = 0;  // a tensor-core wait that gave up (sticky until read and cleared)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ uint32_t a_off(int row, int k) {
-    return (uint32_t)(row >> 3) * A_SBO + (uint32_t)(k >> 2) * A_LBO + (uint32_t)(row & 7) * 16u + (uint32_t)(k & 3) * 4u;
+__host__ __device__ __forceinline__ uint32_t a_off(int row, int k) {
+    return (uint32_t)(row >> 3) * A_SBO + (uint32_t)(k >> 3) * A_LBO + (uint32_t)(row & 7) * 16u + (uint32_t)(k & 7) * 2u;
 }
-__device__ __forceinline__ uint32_t b_off(int n, int k) {
-    return (uint32_t)(n >> 3) * B_SBO + (uint32_t)(k >> 2) * B_LBO + (uint32_t)(n & 7) * 16u + (uint32_t)(k & 3) * 4u;
+__host__ __device__ __forceinline__ uint32_t b_off(int n, int k) {
+    return (uint32_t)(n >> 3) * B_SBO + (uint32_t)(k >> 3) * B_LBO + (uint32_t)(n & 7) * 16u + (uint32_t)(k & 7) * 2u;
 }
 
 // Shared-memory matrix descriptor: start address, leading (K) and stride
@@ -74,20 +90,14 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t 
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
 }
 
-// Instruction descriptor of kind::tf32: D f32, A and B tf32, both K-major,
-// N >> 3 at bit 17, M >> 4 at bit 24.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B f16
+// (bits 7-9, 10-12 = 0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t kIdesc = (1u << 4) | ((64u >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
 
-__device__ __forceinline__ float tf32_hi(float v) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
-    return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, int accum) {
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, int accum) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n\t}\n" ::"r"(d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}\n" ::"r"(d),
         "l"(a), "l"(b), "r"(accum), "r"(kIdesc));
 }
 
@@ -124,40 +134,44 @@ __device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
     }
 }
 
-// 64 consecutive TMEM columns of this warp's 32 lanes, one lane per
-// thread.  The load and its wait are one asm statement, so no use of the
-// registers can be scheduled before the data has arrived.
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float *v) {
-    uint32_t r[64];
+// 32 consecutive TMEM columns of this warp's 32 lanes, one lane per thread.
+// The load and its wait are one asm statement, so no use of the registers
+// can be scheduled before the data has arrived.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+    uint32_t r[32];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
-          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr)
         : "memory");
 #pragma unroll
-    for (int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// cos(2 pi j / 1024) and sin(2 pi j / 1024) from the quarter-wave table
-// q[i] = cos(2 pi i / 1024), i = 0..256.
-__device__ __forceinline__ float2 tw1024(const float *q, int j) {
-    j &= 1023;
-    const int r = j & 255, qd = j >> 8;
-    const float c = q[r], s = q[256 - r];  // cos(t), sin(t) of the reduced angle
-    switch (qd) {
-        case 0: return make_float2(c, s);
-        case 1: return make_float2(-s, c);
-        case 2: return make_float2(-c, -s);
-        default: return make_float2(s, -c);
-    }
+// The power of two that scales a transform whose largest magnitude is m
+// to just below 2^kTcScaleExp (1 for an all-zero transform), and its inverse.
+__device__ __forceinline__ float2 tc_scale(float m) {
+    if (!(m > 0.f)) return make_float2(1.f, 1.f);
+    int e;
+    frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return make_float2(ldexpf(1.f, kTcScaleExp - e), ldexpf(1.f, e - kTcScaleExp));
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// hi = fp16(v), lo = fp16(v - hi): the two halves of a split operand.
+__device__ __forceinline__ void split2(float v, __half &hi, __half &lo) {
+    hi = __float2half_rn(v);
+    lo = __float2half_rn(v - __half2float(hi));
 }
 
 // The CTA's tensor-core state: TMEM columns, the MMA-completion mbarrier
@@ -168,16 +182,14 @@ struct TcState {
     bool ok;
 };
 
-// Fills B (the 32-point inverse DFT in real block form, split hi/lo) and the
-// twiddle table; allocates TMEM (warp 0) and initialises the mbarrier.
-__device__ void tc_setup(unsigned char *sm, uint64_t *bar, uint32_t *tmemSlot, TcState &s) {
+// Copies B (hi, lo) into shared memory, allocates TMEM (warp 0) and
+// initialises the mbarrier.
+__device__ void tc_setup(unsigned char *sm, const TcTables *__restrict__ tab, uint64_t *bar, uint32_t *tmemSlot,
+                         TcState &s) {
     const int tid = threadIdx.x;
-    float *q = reinterpret_cast<float *>(sm + OFF_TW);
-    for (int i = tid; i <= 256; i += blockDim.x) {
-        float sv, cv;
-        sincospif((float)i / 512.f, &sv, &cv);
-        q[i] = cv;
-    }
+    const uint4 *src = reinterpret_cast<const uint4 *>(tab->bimg);
+    uint4 *dst = reinterpret_cast<uint4 *>(sm + OFF_BHI);
+    for (int i = tid; i < (int)(2 * B_BYTES / 16); i += blockDim.x) dst[i] = __ldg(src + i);
     if (tid < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmemSlot)),
                      "r"(kTcCols));
@@ -186,20 +198,6 @@ __device__ void tc_setup(unsigned char *sm, uint64_t *bar, uint32_t *tmemSlot, T
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    // B[n][k]: n = output (re 0..31, im 32..63), k = input (re 0..31, im 32..63)
-    for (int i = tid; i < 64 * 64; i += blockDim.x) {
-        const int n = i >> 6, k = i & 63, n1 = n & 31, k1 = k & 31;
-        const float2 w = tw1024(q, 32 * ((n1 * k1) & 31));  // w32^(n1 k1)
-        float v;
-        if (n < 32)
-            v = k < 32 ? w.x : -w.y;
-        else
-            v = k < 32 ? w.y : w.x;
-        const float hi = tf32_hi(v);
-        *reinterpret_cast<float *>(sm + OFF_BHI + b_off(n, k)) = hi;
-        *reinterpret_cast<float *>(sm + OFF_BLO + b_off(n, k)) = tf32_hi(v - hi);
     }
     fence_async_smem();
     tc_fence_before();
@@ -217,39 +215,42 @@ __device__ void tc_teardown(const TcState &s) {
     if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s.tmem), "r"(kTcCols));
 }
 
-// Stores 4 consecutive K elements (k0 % 4 == 0) of A row `row`, split.
-__device__ __forceinline__ void a_store4(unsigned char *sm, int row, int k0, float v0, float v1, float v2, float v3) {
-    const float h0 = tf32_hi(v0), h1 = tf32_hi(v1), h2 = tf32_hi(v2), h3 = tf32_hi(v3);
-    const uint32_t o = a_off(row, k0);
-    *reinterpret_cast<float4 *>(sm + OFF_AHI + o) = make_float4(h0, h1, h2, h3);
-    *reinterpret_cast<float4 *>(sm + OFF_ALO + o) =
-        make_float4(tf32_hi(v0 - h0), tf32_hi(v1 - h1), tf32_hi(v2 - h2), tf32_hi(v3 - h3));
+// Stage-1 operand: this thread's row (32 warp + lane) from its 32 complex
+// inputs (re[k1], im[k1]), scaled by sc and split; one 16-byte store per
+// chunk of 8 K elements.
+__device__ __forceinline__ void a_store_row(unsigned char *sm, int row, const float *re, const float *im, float sc) {
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const float *v = half ? im : re;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            __align__(16) __half h[8], l[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) split2(v[8 * c + i] * sc, h[i], l[i]);
+            const uint32_t o = a_off(row, 32 * half + 8 * c);
+            *reinterpret_cast<uint4 *>(sm + OFF_AHI + o) = *reinterpret_cast<const uint4 *>(h);
+            *reinterpret_cast<uint4 *>(sm + OFF_ALO + o) = *reinterpret_cast<const uint4 *>(l);
+        }
+    }
 }
 
-__device__ __forceinline__ void a_store1(unsigned char *sm, int row, int k, float v) {
-    const float h = tf32_hi(v);
-    const uint32_t o = a_off(row, k);
-    *reinterpret_cast<float *>(sm + OFF_AHI + o) = h;
-    *reinterpret_cast<float *>(sm + OFF_ALO + o) = tf32_hi(v - h);
-}
-
-// One stage: D = Ahi Bhi + Alo Bhi + Ahi Blo over K = 64 (8 steps of 8),
+// One stage: D = Ahi Bhi + Alo Bhi + Ahi Blo over K = 64 (4 steps of 16),
 // issued by thread 0, completion on the mbarrier; every thread then waits.
 // The caller has stored A (fence.proxy.async by every writer) and
 // synchronised.
 __device__ void tc_stage(unsigned char *sm, uint64_t *bar, TcState &s) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && s.ok) {
         tc_fence_after();
         const uint32_t base = smem_u32(sm);
 #pragma unroll
-        for (int ks = 0; ks < 8; ks++) {
+        for (int ks = 0; ks < 4; ks++) {
             const uint64_t ah = sdesc(base + OFF_AHI + ks * 2 * A_LBO, A_LBO, A_SBO);
             const uint64_t al = sdesc(base + OFF_ALO + ks * 2 * A_LBO, A_LBO, A_SBO);
             const uint64_t bh = sdesc(base + OFF_BHI + ks * 2 * B_LBO, B_LBO, B_SBO);
             const uint64_t bl = sdesc(base + OFF_BLO + ks * 2 * B_LBO, B_LBO, B_SBO);
-            mma_tf32(s.tmem, ah, bh, ks > 0);
-            mma_tf32(s.tmem, al, bh, 1);
-            mma_tf32(s.tmem, ah, bl, 1);
+            mma_f16(s.tmem, ah, bh, ks > 0);
+            mma_f16(s.tmem, al, bh, 1);
+            mma_f16(s.tmem, ah, bl, 1);
         }
         tc_commit(bar);
     }
@@ -258,74 +259,91 @@ __device__ void tc_stage(unsigned char *sm, uint64_t *bar, TcState &s) {
     tc_fence_after();
 }
 
-// After stage 1: thread (warp w, lane k2) reads Y[., k2] of transform w,
-// applies the twiddles w^(n1 k2) and stores the stage-2 operand: row
-// 32 w + n1, K = k2 (re) and 32 + k2 (im).
-__device__ void tc_twiddle_transpose(unsigned char *sm, const TcState &s) {
+// After stage 1: thread (warp w, lane k2) reads D[., k2] of transform w
+// (= Y scaled by sc1), applies the twiddles w^(n1 k2), rescales for stage
+// 2 and stores its operand: row 32 w + n1, K = k2 (re) and 32 + k2 (im).
+// Returns the stage-2 unscale factor.
+__device__ float tc_twiddle_transpose(unsigned char *sm, const TcTables *__restrict__ tab, const TcState &s,
+                                      float inv1) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float *q = reinterpret_cast<const float *>(sm + OFF_TW);
     float y[64];
-    tmem_ld64(s.tmem + ((uint32_t)(32 * warp) << 16), y);
+    const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
+    tmem_ld32(ta, y);
+    tmem_ld32(ta + 32, y + 32);
+    float m = 0.f;
 #pragma unroll
     for (int n1 = 0; n1 < 32; n1++) {
-        const float2 w = tw1024(q, n1 * lane);
+        float2 w = __ldg(tab->tw + n1 * lane);
+        w.x *= inv1;
+        w.y *= inv1;
         const float yr = y[n1], yi = y[32 + n1];
-        const float tr = fmaf(yr, w.x, -yi * w.y), ti = fmaf(yr, w.y, yi * w.x);
-        a_store1(sm, 32 * warp + n1, lane, tr);
-        a_store1(sm, 32 * warp + n1, 32 + lane, ti);
+        y[n1] = fmaf(yr, w.x, -yi * w.y);
+        y[32 + n1] = fmaf(yr, w.y, yi * w.x);
+        m = fmaxf(m, fmaxf(fabsf(y[n1]), fabsf(y[32 + n1])));
+    }
+    const float2 sc = tc_scale(warp_max(m));
+#pragma unroll
+    for (int n1 = 0; n1 < 32; n1++) {
+        __half hr, lr, hi_, li;
+        split2(y[n1] * sc.x, hr, lr);
+        split2(y[32 + n1] * sc.x, hi_, li);
+        const int row = 32 * warp + n1;
+        *reinterpret_cast<__half *>(sm + OFF_AHI + a_off(row, lane)) = hr;
+        *reinterpret_cast<__half *>(sm + OFF_ALO + a_off(row, lane)) = lr;
+        *reinterpret_cast<__half *>(sm + OFF_AHI + a_off(row, 32 + lane)) = hi_;
+        *reinterpret_cast<__half *>(sm + OFF_ALO + a_off(row, 32 + lane)) = li;
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
-}
-
-// After stage 2: thread (warp w, lane n1) gets x[n1 + 32 n2] of transform w
-// as re[n2] = v[n2], im[n2] = v[32 + n2].
-__device__ __forceinline__ void tc_result(const TcState &s, float *v) {
-    const int warp = threadIdx.x >> 5;
-    tmem_ld64(s.tmem + ((uint32_t)(32 * warp) << 16), v);
+    return sc.y;
 }
 
 // ------------------------------------------------------------ self-test
 
 // Four inverse 1024-point DFTs of z (natural order, complex) into x, and
-// the first stage's raw GEMM tile (D of stage 1) into d1 (128 x 64).
-__global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const float2 *__restrict__ z, float2 *__restrict__ x,
+// the first stage's GEMM tile, unscaled, into d1 (128 x 64).
+__global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const TcTables *__restrict__ tab,
+                                                              const float2 *__restrict__ z, float2 *__restrict__ x,
                                                               float *__restrict__ d1) {
     extern __shared__ unsigned char smraw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmemSlot;
     TcState s;
-    tc_setup(sm, &bar, &tmemSlot, s);
+    tc_setup(sm, tab, &bar, &tmemSlot, s);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // stage-1 operand: row 32 w + k2, K = k1 (re), 32 + k1 (im)
-    {
-        const float2 *zt = z + warp * 1024;
+    float re[32], im[32], m = 0.f;
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-            float2 e[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) e[i] = zt[32 * (4 * c + i) + lane];
-            a_store4(sm, 32 * warp + lane, 4 * c, e[0].x, e[1].x, e[2].x, e[3].x);
-            a_store4(sm, 32 * warp + lane, 32 + 4 * c, e[0].y, e[1].y, e[2].y, e[3].y);
-        }
+    for (int k1 = 0; k1 < 32; k1++) {
+        const float2 e = z[warp * 1024 + 32 * k1 + lane];
+        re[k1] = e.x;
+        im[k1] = e.y;
+        m = fmaxf(m, fmaxf(fabsf(e.x), fabsf(e.y)));
     }
+    const float2 sc1 = tc_scale(warp_max(m));
+    a_store_row(sm, 32 * warp + lane, re, im, sc1.x);
     fence_async_smem();
     __syncthreads();
     tc_stage(sm, &bar, s);
     {
-        float v[64];
-        tc_result(s, v);
+        float v[32];
+        const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
+        tmem_ld32(ta, v);
 #pragma unroll
-        for (int i = 0; i < 64; i++) d1[(32 * warp + lane) * 64 + i] = v[i];
+        for (int i = 0; i < 32; i++) d1[(32 * warp + lane) * 64 + i] = v[i] * sc1.y;
+        tmem_ld32(ta + 32, v);
+#pragma unroll
+        for (int i = 0; i < 32; i++) d1[(32 * warp + lane) * 64 + 32 + i] = v[i] * sc1.y;
     }
-    tc_twiddle_transpose(sm, s);
+    const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
     tc_stage(sm, &bar, s);
-    float v[64];
-    tc_result(s, v);
+    float v[32], w[32];
+    const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
+    tmem_ld32(ta, v);
+    tmem_ld32(ta + 32, w);
 #pragma unroll
-    for (int n2 = 0; n2 < 32; n2++) x[warp * 1024 + lane + 32 * n2] = make_float2(v[n2], v[32 + n2]);
+    for (int n2 = 0; n2 < 32; n2++) x[warp * 1024 + lane + 32 * n2] = make_float2(v[n2] * inv2, w[n2] * inv2);
     tc_teardown(s);
 }
 
@@ -334,7 +352,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const float2 *__r
 // The fast form's fused inverse rows (k_inv_rows_t<10, true> with the
 // radix-4 cascade replaced): four row pairs per MMA tile, pairsPerCta row
 // pairs per CTA (the same grid and partial records as the FP32 kernel).
-__global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
     griddep_wait();
     constexpr int N = 1024, HALF = 512;
     extern __shared__ unsigned char smraw[];
@@ -343,6 +361,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
     __shared__ uint32_t tmemSlot;
     __shared__ Ext shExt[kTcThreads / 32];
     __shared__ int isLast;
+    const TcTables *tab = reinterpret_cast<const TcTables *>(a.tcTab);
     const FftClass &fc = a.fc;
     const int tileLocal = blockIdx.y;
     const int tile = fc.tileFirst + tileLocal;
@@ -382,7 +401,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
         }
     } else if (P > 0) {
         TcState s;
-        tc_setup(sm, &bar, &tmemSlot, s);
+        tc_setup(sm, tab, &bar, &tmemSlot, s);
         for (int t0 = 0; t0 < P; t0 += kTcTrans) {
             // stage-1 operand from the combine (impl.go:405-413): thread
             // (w, k2) builds row 32 w + k2 = z[32 k1 + k2], k1 = 0..31, of
@@ -390,14 +409,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
             const int p = t0 + warp;
             const bool live = p < P;
             const int r = 2 * (pair0 + p);
-            const float2 *u = cb + (size_t)brev_bits(r, log2H) * hwp;
-            const float2 *v = cb + (size_t)brev_bits(r + 1, log2H) * hwp;
+            float re[32], im[32], mx = 0.f;
+            {
+                const float2 *u = cb + (size_t)brev_bits(live ? r : 0, log2H) * hwp;
+                const float2 *v = cb + (size_t)brev_bits(live ? r + 1 : 0, log2H) * hwp;
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                float zr[4], zi[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int k = 32 * (4 * c + i) + lane;
+                for (int k1 = 0; k1 < 32; k1++) {
+                    const int k = 32 * k1 + lane;
                     float2 U = make_float2(0.f, 0.f), V = U;
                     if (live) {
                         const int kk = k <= HALF ? k : N - k;
@@ -405,49 +423,44 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
                         V = __ldg(v + kk);
                     }
                     if (k <= HALF) {
-                        zr[i] = U.x - V.y;
-                        zi[i] = U.y + V.x;
+                        re[k1] = U.x - V.y;
+                        im[k1] = U.y + V.x;
                     } else {
-                        zr[i] = U.x + V.y;
-                        zi[i] = V.x - U.y;
+                        re[k1] = U.x + V.y;
+                        im[k1] = V.x - U.y;
                     }
+                    mx = fmaxf(mx, fmaxf(fabsf(re[k1]), fabsf(im[k1])));
                 }
-                a_store4(sm, 32 * warp + lane, 4 * c, zr[0], zr[1], zr[2], zr[3]);
-                a_store4(sm, 32 * warp + lane, 32 + 4 * c, zi[0], zi[1], zi[2], zi[3]);
             }
+            const float2 sc1 = tc_scale(warp_max(mx));
+            a_store_row(sm, 32 * warp + lane, re, im, sc1.x);
             fence_async_smem();
             __syncthreads();
             tc_stage(sm, &bar, s);
-            tc_twiddle_transpose(sm, s);
+            const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
             tc_stage(sm, &bar, s);
-            // den of the thread's results first (x = lane + 32 n2): their
-            // loads overlap the TMEM read
-            float den[2][32];
-            long long rowBase[2];
-#pragma unroll
+            // x[lane + 32 n2]: columns 0..31 (re) are result row r, 32..63
+            // (im) row r + 1; den first (their loads overlap the TMEM read)
+            const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
             for (int half = 0; half < 2; half++) {
                 const int rr = r + half;
-                rowBase[half] = (long long)(tb.y0 + rr) * m.rw + tb.x0;
+                const long long rowBase = (long long)(tb.y0 + rr) * m.rw + tb.x0;
+                const bool rowOn = live && rr < bh && tb.y0 + rr >= m.roiY0 && tb.y0 + rr < m.roiY1;
+                float den[32];
 #pragma unroll
                 for (int n2 = 0; n2 < 32; n2++) {
                     const int x = lane + 32 * n2;
-                    den[half][n2] = (live && rr < bh && x < bw) ? __ldg(dens + rowBase[half] + x) : 0.f;
+                    den[n2] = (rowOn && x < bw) ? __ldg(dens + rowBase + x) : 0.f;
                 }
-            }
-            float xv[64];
-            tc_result(s, xv);
-            if (live && s.ok) {
-#pragma unroll
-                for (int half = 0; half < 2; half++) {
-                    const int rr = r + half;
-                    if (rr >= bh) break;
-                    const int yy = tb.y0 + rr;
-                    if (yy < m.roiY0 || yy >= m.roiY1) continue;
+                float xv[32];
+                tmem_ld32(ta + 32 * half, xv);
+                if (rowOn && s.ok) {
 #pragma unroll
                     for (int n2 = 0; n2 < 32; n2++) {
                         const int x = lane + 32 * n2;
                         if (x < bw) {
-                            const float num = xv[32 * half + n2], dn = den[half][n2], an = fabsf(num);
+                            const float num = xv[n2] * inv2, dn = den[n2], an = fabsf(num);
                             float score;
                             if (an < dn)
                                 score = __fdividef(num, dn);
@@ -455,8 +468,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
                                 score = num > 0.f ? 1.f : -1.f;
                             else
                                 score = 0.f;
-                            if (map) map[rowBase[half] + x] = score;
-                            if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase[half] + x);
+                            if (map) map[rowBase + x] = score;
+                            if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase + x);
                         }
                     }
                 }
@@ -497,15 +510,50 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_inv_rows_tc(InvArgs a) {
     if (threadIdx.x == 0) ext_store_result(e, m.rw, a.out + m.outIdx);
 }
 
+TcTables *g_tab = nullptr;  // device copy, built by tc_init
+
 }  // namespace
 
+// Builds the device tables once (called from the library's device set-up).
+cudaError_t tc_init() {
+    if (g_tab) return cudaSuccess;
+    std::vector<unsigned char> img(sizeof(TcTables), 0);
+    TcTables *h = reinterpret_cast<TcTables *>(img.data());
+    const double PI2 = 6.283185307179586476925286766559;
+    for (int n = 0; n < 64; n++)
+        for (int k = 0; k < 64; k++) {
+            const int n1 = n & 31, k1 = k & 31;
+            const double th = PI2 * (double)((n1 * k1) & 31) / 32.0, c = std::cos(th), sn = std::sin(th);
+            const double v = n < 32 ? (k < 32 ? c : -sn) : (k < 32 ? sn : c);
+            const float vf = (float)v;
+            const __half hi = __float2half_rn(vf), lo = __float2half_rn(vf - __half2float(hi));
+            *reinterpret_cast<__half *>(h->bimg + b_off(n, k)) = hi;
+            *reinterpret_cast<__half *>(h->bimg + B_BYTES + b_off(n, k)) = lo;
+        }
+    for (int j = 0; j < 1024; j++) {
+        const double th = PI2 * j / 1024.0;
+        h->tw[j] = make_float2((float)std::cos(th), (float)std::sin(th));
+    }
+    TcTables *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(TcTables));
+    if (e == cudaSuccess) e = cudaMemcpy(d, img.data(), sizeof(TcTables), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (d) cudaFree(d);
+        return e;
+    }
+    g_tab = d;
+    return cudaSuccess;
+}
+
 bool inv_rows_tc_applies(const FftClass &fc, const MemberSet &ms) {
-    return ms.form == CVM_FORM_MIXED && fc.log2n == 10 && ms.lanes != nullptr;
+    return ms.form == CVM_FORM_MIXED && fc.log2n == 10 && ms.lanes != nullptr && g_tab != nullptr;
 }
 
 cudaError_t launch_inv_rows_tc(const InvArgs &a, dim3 grid, cudaStream_t st) {
+    InvArgs b = a;
+    b.tcTab = g_tab;
     set_smem(k_inv_rows_tc, kTcSmemLaunch);
-    return launch_k(k_inv_rows_tc, grid, dim3(kTcThreads), kTcSmemLaunch, st, a);
+    return launch_k(k_inv_rows_tc, grid, dim3(kTcThreads), kTcSmemLaunch, st, b);
 }
 
 int tc_error_read_clear() {
@@ -516,9 +564,11 @@ int tc_error_read_clear() {
 }
 
 // Runs the self-test kernel on four pseudo-random lines and compares with
-// the DFT in double precision; returns 0 and the largest errors relative to
-// each line's norm, or a CUDA error.
+// the DFT in double precision; returns the largest errors relative to each
+// line's norm (whole DFT; first stage alone), or a CUDA error.
 cudaError_t tc_selftest(double *dftErr, double *gemmErr) {
+    cudaError_t e = tc_init();
+    if (e != cudaSuccess) return e;
     const int T = 4, N = 1024;
     std::vector<float2> z(T * N);
     uint32_t st = 12345u;
@@ -530,14 +580,14 @@ cudaError_t tc_selftest(double *dftErr, double *gemmErr) {
     }
     float2 *dz = nullptr, *dx = nullptr;
     float *dd = nullptr;
-    cudaError_t e = cudaMalloc(&dz, T * N * sizeof(float2));
+    e = cudaMalloc(&dz, T * N * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&dx, T * N * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&dd, 128 * 64 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemcpy(dz, z.data(), T * N * sizeof(float2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)kTcSmemLaunch);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemLaunch);
     if (e == cudaSuccess) {
-        k_tc_selftest<<<1, kTcThreads, kTcSmemLaunch>>>(dz, dx, dd);
+        k_tc_selftest<<<1, kTcThreads, kTcSmemLaunch>>>(g_tab, dz, dx, dd);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
