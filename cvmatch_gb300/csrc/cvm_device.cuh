@@ -210,6 +210,32 @@ __device__ __forceinline__ void bfly4_one(float2 *pa, float2 *pc, float2 *pb, fl
     *pd = make_float2(s1x - rr, s1y - ri);
 }
 
+// normOne's score ladder (impl.go:825-849): |num| < den -> num / den,
+// |num| < 1.125 den -> +-1, else 0.  The exact form divides correctly
+// rounded, as the reference does.
+__device__ __forceinline__ float score_exact(float num, float den) {
+    const float an = fabsf(num);
+    if (an < den) return __fdiv_rn(num, den);
+    if (an < __fmul_rn(den, 1.125f)) return num > 0.f ? 1.f : -1.f;
+    return 0.f;
+}
+
+// The fast form's ladder: the hardware division (within 2 ulp), except on
+// near-flat windows (the statistics kernel stores their double-precision
+// denominator negated), whose quotient is formed in double precision.
+__device__ __forceinline__ float score_fast(float num, float den) {
+    const float an = fabsf(num);
+    if (den < 0.f) {
+        const double d = -(double)den, n = (double)num;
+        if (fabs(n) < d) return __double2float_rn(__ddiv_rn(n, d));
+        if (fabs(n) < d * 1.125) return num > 0.f ? 1.f : -1.f;
+        return 0.f;
+    }
+    if (an < den) return __fdividef(num, den);
+    if (an < den * 1.125f) return num > 0.f ? 1.f : -1.f;
+    return 0.f;
+}
+
 // Padded shared-memory line layout: one spare slot every 16 elements keeps
 // the strided pass accesses free of bank conflicts.
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }

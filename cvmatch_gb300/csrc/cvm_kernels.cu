@@ -302,8 +302,10 @@ __device__ void finalize_params(DevParams &p, const DevFrame &F, int *cnMax) {
     p.varSum = vs;
     p.flat = vs == 0;
     const double ad = __dmul_rn((double)p.tw, (double)p.th);
-    p.templNorm = __double2float_rn(__dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad)));
-    p.varScale = __double2float_rn(__ddiv_rn(1.0, ad));
+    p.templNormD = __dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad));
+    p.varScaleD = __ddiv_rn(1.0, ad);
+    p.templNorm = __double2float_rn(p.templNormD);
+    p.varScale = __double2float_rn(p.varScaleD);
     p.numScale = cn == 1 ? __double2float_rn(__ddiv_rn(__ll2double_rn((long long)p.tsum[0]), ad)) : p.varScale;
     if (!p.flat) atomicMax(cnMax, cn);
 }
@@ -1696,8 +1698,16 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             // FAST: the square root from the hardware reciprocal square root
             // (within 2 ulp) instead of the correctly rounded sequence
             const float sd = FAST ? __fmul_rn(diff2, rsqrtf(diff2)) : __fsqrt_rn(diff2);
-            const float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
+            float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
             if (FAST) {
+                // A near-flat window (variance below 2^-14 of the window's
+                // mean square, decided on the exact integers) takes its
+                // denominator sqrt(varW varT) in double precision and is
+                // marked by the sign: the inverse rows then form its
+                // quotient in double precision too.
+                if (den > 0.f && (idv << 14) < area * q)
+                    den = -__double2float_rn(__dmul_rn(__dsqrt_rn(__dmul_rn(__ull2double_rn(idv), Pm.varScaleD)),
+                                                       Pm.templNormD));
                 dens[(size_t)y * m.rw] = den;
             } else {
                 const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);

@@ -572,14 +572,8 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
                             if (cnSum > 1) num = __fadd_rn(acc[(size_t)(2 * line + half) * N + x], num);
                             num = __fsub_rn(num, dv[half][i].x);
                         }
-                        const float den = dv[half][i].y, an = fabsf(num);
-                        float score;
-                        if (an < den)
-                            score = FAST ? __fdividef(num, den) : __fdiv_rn(num, den);
-                        else if (an < __fmul_rn(den, 1.125f))
-                            score = num > 0.f ? 1.f : -1.f;
-                        else
-                            score = 0.f;
+                        const float den = dv[half][i].y;
+                        const float score = FAST ? score_fast(num, den) : score_exact(num, den);
                         if (map) map[rowBase[half] + x] = score;
                         if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase[half] + x);
                     }
@@ -620,13 +614,8 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
                         } else {
                             num = __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
                         }
-                        const float den = td[q].y, an = fabsf(num);
-                        if (an < den)
-                            score = fast ? __fdividef(num, den) : __fdiv_rn(num, den);
-                        else if (an < __fmul_rn(den, 1.125f))
-                            score = num > 0.f ? 1.f : -1.f;
-                        else
-                            score = 0.f;
+                        const float den = td[q].y;
+                        score = fast ? score_fast(num, den) : score_exact(num, den);
                     }
                     if (map) map[rowBase + x] = score;
                     // rows ascend, and x ascends within a row: increasing indices

@@ -460,14 +460,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
                     for (int n2 = 0; n2 < 32; n2++) {
                         const int x = lane + 32 * n2;
                         if (x < bw) {
-                            const float num = xv[n2] * inv2, dn = den[n2], an = fabsf(num);
-                            float score;
-                            if (an < dn)
-                                score = __fdividef(num, dn);
-                            else if (an < dn * 1.125f)
-                                score = num > 0.f ? 1.f : -1.f;
-                            else
-                                score = 0.f;
+                            const float score = score_fast(xv[n2] * inv2, den[n2]);
                             if (map) map[rowBase + x] = score;
                             if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase + x);
                         }

@@ -403,3 +403,27 @@ def test_fast_device_resident_colour_match(fast_form, alpha):
                   ref_map=ref(img, t, cn))
         jy, jx = np.unravel_index(int(np.argmax(m)), m.shape)
         assert (jx, jy) == (120, 60)
+
+
+@pytest.mark.parametrize("form", ["fast", "mixed"])
+def test_near_flat_windows_vs_fp64(form):
+    """A low-contrast frame (200 +- ~1 grey levels): every window is
+    near-flat (variance below 2^-14 of its mean square), so every
+    denominator and quotient takes the double-precision path; the scores
+    still meet the 1e-4 bar against FP64 and the peak is where the
+    template was cut.  1024-wide tiles, so the mixed form runs its
+    tensor-core rows here."""
+    rng = np.random.default_rng(101)
+    img = np.empty((300, 1100, 4), np.uint8)
+    img[..., :3] = np.clip(np.rint(200 + rng.standard_normal((300, 1100, 3)) * 0.8), 0, 255)
+    img[..., 3] = 255
+    t = img[120:152, 400:496].copy()
+    assert oracle.plan(96, 32, 1100 - 95, 300 - 31).dft_w == 1024
+    prev = cvm.SetForm(cvm.FORM_FAST if form == "fast" else cvm.FORM_MIXED)
+    try:
+        m, _, _ = cvm.MatchMap(img, t)
+    finally:
+        cvm.SetForm(prev)
+    assert cvm.device_status() == 0
+    map_check(m, fp64.ref_match_f64(img, t, 3), f"near-flat windows ({form})", ref_map=ref(img, t, 3))
+    assert fp64.first_argmax(m) == (400, 120)
