@@ -1087,6 +1087,11 @@ def run_gpu(args):
                                 "e2e": replica_throughput(units, o["e2e_ms"], ws), "e2e_ms_per_step": o["e2e_ms"],
                                 "clocks": o["clocks"]}
             line["forms"]["ratio_" + args.form + "_over_" + f] = o["ms"] / r["ms"]
+        # the fast forms' tile plans the autotuner chose for this workload's shapes
+        try:
+            line["autotune"] = cvm.autotune_report()
+        except Exception:  # an older library without the tuner
+            line["autotune"] = None
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(key, args)
         print(json.dumps(line))

@@ -107,6 +107,9 @@ def lib():
             L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
             L.cvm_get_form.argtypes = []
+            L.cvm_set_autotune.argtypes = [i32]
+            L.cvm_autotune_report.argtypes = [C.c_char_p, C.c_size_t]
+            L.cvm_autotune_report.restype = C.c_size_t
             L.cvm_tc_selftest.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.cvm_device_status.argtypes = [C.POINTER(C.c_int)]
             L.cvm_stream_new.argtypes = [vp, vp, i32, i32, C.POINTER(vp)]
@@ -295,6 +298,21 @@ def NewGrayMatcher(sub) -> Matcher:
 FORM_EXACT = 0
 FORM_FAST = 1
 FORM_MIXED = 2
+
+
+def SetAutotune(on: bool) -> bool:
+    """The fast forms' tile-plan autotuner on or off (cvm_set_autotune);
+    returns the previous setting."""
+    return bool(lib().cvm_set_autotune(1 if on else 0))
+
+
+def autotune_report():
+    """The tuned shapes and their measured candidate plans (list of dicts)."""
+    import json
+    n = lib().cvm_autotune_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib().cvm_autotune_report(buf, n + 1)
+    return json.loads(buf.value.decode())
 
 
 def tc_selftest():

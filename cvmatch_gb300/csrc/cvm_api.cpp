@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 #include <atomic>
+#include <tuple>
 
 #include "cvm_internal.h"
 #include "cvm_plan.h"
@@ -241,8 +242,8 @@ struct Geom {
     FftClass fc[2];
 };
 
-int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G) {
-    G.p = make_plan(tw, th, rw, rh);
+int make_geom(int tw, int th, int rw, int rh, int shrinkTH, Geom &G, const Plan *forced = nullptr) {
+    G.p = forced ? *forced : make_plan(tw, th, rw, rh);
     if (G.p.dftW > kMaxDftW || G.p.dftH > kMaxDftH)
         return fail(CVM_ERR_UNSUPPORTED, "cvmatch_gpu: tile transform %dx%d exceeds the supported %dx%d",
                     G.p.dftW, G.p.dftH, kMaxDftW, kMaxDftH);
@@ -368,15 +369,109 @@ struct SoloJob {
     float *map;
     cvm_result *out;
     int frameOnSide;  // the frame arrives on the second side stream (its frame event)
-    int form;         // CVM_FORM_EXACT or CVM_FORM_FAST (cached spectra must be of this form)
+    int form;         // CVM_FORM_EXACT, _FAST or _MIXED (cached spectra must be of this form)
+    const Plan *plan; // the tile plan (one-shot; nullptr: the tuned plan, or newGoPlan)
 };
+
+int run_solo(const SoloJob &J, cudaStream_t st);
+
+// ------------------------------------------------------------ autotuner
+//
+// The fast and mixed forms may run any tile plan (the exact form keeps
+// newGoPlan, impl.go:246-295: its bits depend on the plan).  The first
+// fast-form call of a shape times up to four candidate plans
+// (plan_candidates: newGoPlan's choice and the best of a GPU cost proxy)
+// on the call's own inputs -- each run once to warm up, then twice between
+// CUDA events on the call's stream -- and keeps the fastest if it beats
+// newGoPlan's by more than 3 %; the choice is cached per (frame size,
+// template size, channel mode, form) for the life of the process, so every
+// later call of the shape (one-shot calls and Matchers alike) runs the same
+// plan and gives the same results.  A call made while its stream is being
+// captured into a graph runs newGoPlan's plan and tunes nothing.
+struct TuneKey {
+    int iw, ih, tw, th, mode, cn, step, form;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(iw, ih, tw, th, mode, cn, step, form) <
+               std::tie(o.iw, o.ih, o.tw, o.th, o.mode, o.cn, o.step, o.form);
+    }
+};
+struct TuneEntry {
+    Plan plan;
+    int n = 0;
+    Plan cand[4];
+    float ms[4] = {0, 0, 0, 0};
+};
+std::mutex g_tuneMu;
+std::map<TuneKey, TuneEntry> g_tune;
+std::atomic<int> g_autotune{1};
+
+// The plan a fast-form one-shot match of J's shape runs (tuning it first
+// when needed); *out = newGoPlan's plan when tuning is off or not possible.
+int solo_plan(const SoloJob &J, cudaStream_t st, Plan *out) {
+    const int rw = J.iw - J.tw + 1, rh = J.ih - J.th + 1;
+    *out = make_plan(J.tw, J.th, rw, rh);
+    if (J.form == CVM_FORM_EXACT || !g_autotune.load()) return CVM_OK;
+    const TuneKey key{J.iw, J.ih, J.tw, J.th, J.mode, J.mode == 1 ? 0 : J.cnFixed, J.step, J.form};
+    {
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            *out = it->second.plan;
+            return CVM_OK;
+        }
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return CVM_OK;
+    }
+    std::vector<Plan> cands = plan_candidates(J.tw, J.th, rw, rh, 4);
+    TuneEntry ent;
+    ent.plan = *out;
+    if (cands.size() > 1) {
+        thread_local cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (!e0) {
+            CVM_CUDA(cudaEventCreate(&e0));
+            CVM_CUDA(cudaEventCreate(&e1));
+        }
+        int best = 0;
+        for (size_t i = 0; i < cands.size(); i++) {
+            SoloJob T = J;
+            T.plan = &cands[i];
+            CVM_TRY(run_solo(T, st));
+            CVM_CUDA(cudaEventRecord(e0, st));
+            CVM_TRY(run_solo(T, st));
+            CVM_TRY(run_solo(T, st));
+            CVM_CUDA(cudaEventRecord(e1, st));
+            CVM_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            CVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            ent.cand[ent.n] = cands[i];
+            ent.ms[ent.n] = ms / 2;
+            ent.n++;
+            if (ms / 2 < ent.ms[best]) best = (int)i;
+        }
+        // cands[0] is newGoPlan's choice whenever it qualifies
+        const bool baseFirst = cands[0].dftW == out->dftW && cands[0].dftH == out->dftH;
+        if (!baseFirst || ent.ms[best] < 0.97f * ent.ms[0]) ent.plan = cands[best];
+    }
+    std::lock_guard<std::mutex> lk(g_tuneMu);
+    auto ins = g_tune.emplace(key, ent);  // another thread may have tuned the shape meanwhile
+    *out = ins.first->second.plan;
+    return CVM_OK;
+}
 
 int run_solo(const SoloJob &J, cudaStream_t st) {
     const int rw = J.iw - J.tw + 1, rh = J.ih - J.th + 1;
     Geom local;
     const Geom *G = J.G;
     if (!G) {
-        CVM_TRY(make_geom(J.tw, J.th, rw, rh, J.th, local));
+        Plan p;
+        if (J.plan)
+            p = *J.plan;
+        else
+            CVM_TRY(solo_plan(J, st, &p));
+        CVM_TRY(make_geom(J.tw, J.th, rw, rh, J.th, local, &p));
         G = &local;
     }
     const int cnS = J.mode == 1 ? 4 : J.cnFixed;
@@ -868,7 +963,9 @@ namespace {
 
 // The Matcher's cached plan and spectra for one result size, built once
 // under the handle's lock (the double-checked cache of matcher.go:114-126).
-int matcher_geom(cvm_matcher *m, int rw, int rh, int form, std::shared_ptr<MatcherGeom> &out) {
+int matcher_geom(cvm_matcher *m, const uint8_t *dParent, long long pstride, int pw, int ph, int form, cudaStream_t st,
+                 cvm_result *dOut, std::shared_ptr<MatcherGeom> &out) {
+    const int rw = pw - m->w + 1, rh = ph - m->h + 1;
     std::lock_guard<std::mutex> lk(m->mu);
     if (m->geom && m->geom->rw == rw && m->geom->rh == rh && m->geom->form == form) {
         out = m->geom;
@@ -878,14 +975,35 @@ int matcher_geom(cvm_matcher *m, int rw, int rh, int form, std::shared_ptr<Match
     g->rw = rw;
     g->rh = rh;
     g->form = form;
-    CVM_TRY(make_geom(m->w, m->h, rw, rh, m->h, g->G));
+    // the plan a one-shot match of this shape runs (tuned on this frame in
+    // the fast forms), so Find and Match stay identical
+    Plan plan;
+    {
+        SoloJob T;
+        memset(&T, 0, sizeof T);
+        T.form = form;
+        T.img = dParent;
+        T.istride = pstride;
+        T.iw = pw;
+        T.ih = ph;
+        T.step = m->step;
+        T.mode = m->step == 4 ? 1 : 0;
+        T.cnFixed = m->step == 4 ? 4 : 1;
+        T.tpl = m->dPix;
+        T.tstride = (long long)m->w * m->step;
+        T.tw = m->w;
+        T.th = m->h;
+        T.out = dOut;  // the tuning runs' results are overwritten by the call's own
+        CVM_TRY(solo_plan(T, st, &plan));
+    }
+    CVM_TRY(make_geom(m->w, m->h, rw, rh, m->h, g->G, &plan));
     const int cnS = m->step;  // colour: all four channels (cn is decided per frame)
     for (int c = 0; c < g->G.nclass; c++)
         CVM_CUDA(cudaMalloc(&g->ts[c], tspec_elems(g->G.fc[c], cnS) * sizeof(float2)));
-    cudaStream_t st = thread_stream();
+    cudaStream_t bst = thread_stream();
     CVM_TRY(build_tspec(g->G, m->dPix, (long long)m->w * m->step, m->step, m->w, m->h, cnS, nullptr, g->ts[0],
-                        g->ts[1], st, effective_form(form, g->G) != CVM_FORM_EXACT ? m->tsum : nullptr));
-    CVM_CUDA(cudaStreamSynchronize(st));
+                        g->ts[1], bst, effective_form(form, g->G) != CVM_FORM_EXACT ? m->tsum : nullptr));
+    CVM_CUDA(cudaStreamSynchronize(bst));
     m->geom = g;
     out = g;
     return CVM_OK;
@@ -901,10 +1019,9 @@ int matcher_find_dev(cvm_matcher *m, const uint8_t *dParent, long long pstride, 
         CVM_CUDA(upload_bytes(dOut, &kFlatResult, sizeof kFlatResult, st));
         return CVM_OK;
     }
-    const int rw = pw - m->w + 1, rh = ph - m->h + 1;
     const int form = solo_form();
     std::shared_ptr<MatcherGeom> g;
-    CVM_TRY(matcher_geom(m, rw, rh, form, g));
+    CVM_TRY(matcher_geom(m, dParent, pstride, pw, ph, form, st, dOut, g));
     SoloJob J;
     memset(&J, 0, sizeof J);
     J.form = form;
@@ -1038,7 +1155,8 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
         for (int c = 0; c < G.nclass; c++) {
             int P = 0;
             bg->partOff[c] = nparts;
-            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P, bfast);
+            nparts += G.fc[c].ntiles * inv_rows_ctas_per_tile(G.fc[c], G.fc[c].dftH, &P, bfast,
+                                                              bg->form == CVM_FORM_MIXED && G.fc[c].log2n == 10);
         }
         bg->nparts = nparts;
         std::vector<DevMember> tab(b.members.size());
@@ -1634,6 +1752,40 @@ int cvm_fleet_find_all_device(cvm_fleet *f, const uint8_t *d_parent, int64_t pst
 }
 
 void cvm_fleet_free(cvm_fleet *f) { delete f; }
+
+int cvm_set_autotune(int on) { return g_autotune.exchange(on ? 1 : 0); }
+
+size_t cvm_autotune_report(char *buf, size_t len) {
+    std::string j = "[";
+    {
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        bool first = true;
+        for (const auto &kv : g_tune) {
+            const TuneKey &k = kv.first;
+            const TuneEntry &e = kv.second;
+            char b[256];
+            snprintf(b, sizeof b,
+                     "%s{\"frame\":[%d,%d],\"template\":[%d,%d],\"mode\":%d,\"cn\":%d,\"step\":%d,\"form\":%d,"
+                     "\"plan\":[%d,%d],\"candidates\":[",
+                     first ? "" : ",", k.iw, k.ih, k.tw, k.th, k.mode, k.cn, k.step, k.form, e.plan.dftW, e.plan.dftH);
+            j += b;
+            for (int i = 0; i < e.n; i++) {
+                snprintf(b, sizeof b, "%s{\"plan\":[%d,%d],\"ms\":%.5f}", i ? "," : "", e.cand[i].dftW, e.cand[i].dftH,
+                         (double)e.ms[i]);
+                j += b;
+            }
+            j += "]}";
+            first = false;
+        }
+    }
+    j += "]";
+    if (buf && len) {
+        const size_t n = j.size() < len - 1 ? j.size() : len - 1;
+        memcpy(buf, j.data(), n);
+        buf[n] = 0;
+    }
+    return j.size();
+}
 
 int cvm_set_form(int form) {
     if (form != CVM_FORM_EXACT && form != CVM_FORM_FAST && form != CVM_FORM_MIXED)

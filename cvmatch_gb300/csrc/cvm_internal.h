@@ -171,7 +171,9 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
 cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int cnS, const MemberSet &ms,
                             int nmembers, int rowsMax, int partOffset, int nparts, Partial *partials, int *counters,
                             cvm_result *out, cudaStream_t st, int wide = 0);
-int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide = 0);
+// tc: the launch runs the tensor-core kernel (CVM_FORM_MIXED, 1024-point
+// rows), which takes 32 row pairs per CTA in a fleet (wide)
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide = 0, int tc = 0);
 // Normalisation + first-occurrence extrema: CW x B results per CTA, ncx x
 // nby CTAs per member, result rows in groups of G; the member's last CTA
 // writes its result to out[outIdx].  counters (one int per member of the

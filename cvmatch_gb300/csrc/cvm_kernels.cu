@@ -1984,12 +1984,14 @@ cudaError_t launch_cols(int mode, const float2 *in, float2 *out, int cnS, const 
     return cudaGetLastError();
 }
 
-int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide) {
+int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, int wide, int tc) {
     // 4096 elements per CTA: the radix-16 passes (n/16 units per line) keep
     // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM);
     // wide: 8192 elements (two units per thread per pass), ~70 KB without
-    // the accumulator
+    // the accumulator; the tensor-core kernel in a fleet: 32 row pairs (its
+    // per-CTA set-up -- TMEM, the DFT matrix copy -- spread over 8 MMA tiles)
     int P = (wide ? 8192 : 4096) / fc.n;
+    if (tc && wide) P = 32;
     if (P < 1) P = 1;
     // A tile emits at most rowsMax rows, and never more than dftH (a fleet
     // member's last band extends to its own result edge, still inside the
@@ -2012,7 +2014,8 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.ms = ms;
     int P = 0;
     if (wide && (!ms.form || !rows_fixed_length(fc.log2n))) return cudaErrorInvalidValue;
-    const int ctas = inv_rows_ctas_per_tile(fc, rowsMax, &P, wide);
+    const bool tc = inv_rows_tc_applies(fc, ms);
+    const int ctas = inv_rows_ctas_per_tile(fc, rowsMax, &P, wide, tc);
     a.pairsPerCta = P;
     a.partOffset = partOffset;
     a.nparts = nparts;
@@ -2020,7 +2023,7 @@ cudaError_t launch_inv_rows(const TileGeom &g, const FftClass &fc, int cls, int 
     a.counters = counters;
     a.out = out;
     dim3 grid(ctas, fc.ntiles, nmembers);
-    if (inv_rows_tc_applies(fc, ms)) {
+    if (tc) {
         ProfScope ps("k_inv_rows_tc", st);
         const cudaError_t e = launch_inv_rows_tc(a, grid, st);
         count_launches(1);

@@ -71,6 +71,47 @@ Plan make_plan(int tw, int th, int rw, int rh) {
     return p;
 }
 
+Plan plan_with(int W, int H, int tw, int th, int rw, int rh) {
+    Plan p;
+    p.dftW = W;
+    p.dftH = H;
+    p.hw = W / 2 + 1;
+    p.blockW = std::min(W - tw + 1, rw);
+    p.blockH = std::min(H - th + 1, rh);
+    const int64_t ntx = (rw + p.blockW - 1) / p.blockW, nty = (rh + p.blockH - 1) / p.blockH;
+    p.cost = ntx * nty * int64_t(W) * H * (ilog2(W) + ilog2(H) + 6);
+    return p;
+}
+
+// Tile plans the autotuner times for the fast forms (the exact form keeps
+// newGoPlan: its bits depend on the plan).  Power-of-two transforms of
+// 32 .. 4096 points (the length-specialised kernels) whose blocks hold at
+// least 16 results a side, ranked by a GPU cost proxy -- transform points
+// x (log2 of the tile size + a per-point memory term) over the tile grid
+// -- with newGoPlan's own choice first when it qualifies; at most `count`.
+std::vector<Plan> plan_candidates(int tw, int th, int rw, int rh, int count) {
+    std::vector<Plan> out;
+    const Plan base = make_plan(tw, th, rw, rh);
+    auto ok = [&](int W, int H) {
+        return W >= 32 && W <= 4096 && H >= 32 && H <= 4096 && int64_t(W) * H <= (int64_t(1) << 22) &&
+               std::min(W - tw + 1, rw) >= std::min(16, rw) && std::min(H - th + 1, rh) >= std::min(16, rh) &&
+               W - tw + 1 >= 1 && H - th + 1 >= 1;
+    };
+    if (ok(base.dftW, base.dftH)) out.push_back(plan_with(base.dftW, base.dftH, tw, th, rw, rh));
+    std::vector<Plan> all;
+    for (int W = 32; W <= 4096; W <<= 1)
+        for (int H = 32; H <= 4096; H <<= 1)
+            if (ok(W, H) && !(W == base.dftW && H == base.dftH)) all.push_back(plan_with(W, H, tw, th, rw, rh));
+    std::stable_sort(all.begin(), all.end(), [](const Plan &a, const Plan &b) {
+        return a.cost < b.cost || (a.cost == b.cost && int64_t(a.dftW) * a.dftH < int64_t(b.dftW) * b.dftH);
+    });
+    for (const Plan &p : all) {
+        if ((int)out.size() >= count) break;
+        out.push_back(p);
+    }
+    return out;
+}
+
 // The last-band transform height (shrinkDH, impl.go:573-582): 0 when the
 // band keeps dftH.
 int shrink_dh(const Plan &p, int rh, int th) {

@@ -16,20 +16,24 @@
 //
 // Each stage is one real GEMM D[128 x 64] = A[128 x 64] B[64 x 64] per four
 // transforms: A's rows are (transform, k2) (stage 1) or (transform, n1)
-// (stage 2) with K = 32 complex inputs as (re[32], im[32]); B is the
-// 32-point DFT matrix in real block form (out re = in re cos - in im sin,
-// out im = in re sin + in im cos); D's 64 columns are the 32 complex
-// outputs as (re[32], im[32]).  tcgen05.mma kind::tf32 multiplies 19-bit
-// operands, so every operand is split as hi = rna_tf32(v), lo = v - hi and
-// the products are accumulated as Ahi Bhi + Alo Bhi + Ahi Blo in FP32 (in
-// TMEM): the representation error is ~2^-22 of each operand, the FP32
-// cascade's order.  One thread issues the MMAs; tcgen05.commit arrives on
-// an mbarrier the CTA waits on (a bounded wait: after ~2 s without the
-// arrival it records a device error, frees its TMEM and returns); D comes
-// back from TMEM with tcgen05.ld.  Operands are staged in shared memory in
-// the K-major, no-swizzle core-matrix layout (8 rows x 16 bytes per core
-// matrix), A with a 144-byte K stride so the transposed stores between the
-// stages are free of bank conflicts.
+// (stage 2) with K = 32 complex inputs as interleaved (re, im) pairs; B is
+// the 32-point DFT matrix in real block form (out re = in re cos - in im
+// sin, out im = in re sin + in im cos); D's 64 columns are the 32 complex
+// outputs, interleaved the same way.  The products run as tcgen05.mma
+// kind::f16 (FP16 operands, FP32 accumulation in TMEM) on split operands:
+// each transform is first scaled by the power of two that brings its
+// largest magnitude just below 2^14 (FP16's range), then every operand is
+// split as hi = fp16(v), lo = fp16(v - hi), and the products are
+// accumulated as Ahi Bhi + Alo Bhi + Ahi Blo: ~22 significant bits per
+// operand, the FP32 cascade's order of error.  The scale is undone (exactly,
+// a power of two) when D is read back.  One thread issues the MMAs;
+// tcgen05.commit arrives on an mbarrier the CTA waits on (a bounded wait:
+// after ~2 s without the arrival it records a device error, frees its TMEM
+// and returns); D comes back from TMEM with tcgen05.ld.  Operands are staged
+// in shared memory in the K-major, no-swizzle core-matrix layout (8 rows x
+// 16 bytes per core matrix), A with a 144-byte K stride so the transposed
+// stores between the stages are free of bank conflicts; the DFT matrix and
+// the twiddles are built once per device in double precision.
 //
 // The epilogue is the FP32 kernel's: normOne's ladder from the den lanes
 // of the statistics kernel, first-occurrence extrema, the member's result
@@ -215,22 +219,25 @@ __device__ void tc_teardown(const TcState &s) {
     if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s.tmem), "r"(kTcCols));
 }
 
+// hi/lo halves of two values at once (packed conversions).
+__device__ __forceinline__ void split_pair(float a, float b, __half2 &hi, __half2 &lo) {
+    hi = __floats2half2_rn(a, b);
+    const float2 h = __half22float2(hi);
+    lo = __floats2half2_rn(a - h.x, b - h.y);
+}
+
 // Stage-1 operand: this thread's row (32 warp + lane) from its 32 complex
-// inputs (re[k1], im[k1]), scaled by sc and split; one 16-byte store per
-// chunk of 8 K elements.
+// inputs z[k1] = (re[k1], im[k1]) at K = 2 k1 (re), 2 k1 + 1 (im), scaled
+// by sc and split; one 16-byte store per chunk of 4 complex values.
 __device__ __forceinline__ void a_store_row(unsigned char *sm, int row, const float *re, const float *im, float sc) {
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
-        const float *v = half ? im : re;
+    for (int c = 0; c < 8; c++) {
+        __align__(16) __half2 h[4], l[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            __align__(16) __half h[8], l[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) split2(v[8 * c + i] * sc, h[i], l[i]);
-            const uint32_t o = a_off(row, 32 * half + 8 * c);
-            *reinterpret_cast<uint4 *>(sm + OFF_AHI + o) = *reinterpret_cast<const uint4 *>(h);
-            *reinterpret_cast<uint4 *>(sm + OFF_ALO + o) = *reinterpret_cast<const uint4 *>(l);
-        }
+        for (int i = 0; i < 4; i++) split_pair(re[4 * c + i] * sc, im[4 * c + i] * sc, h[i], l[i]);
+        const uint32_t o = a_off(row, 8 * c);
+        *reinterpret_cast<uint4 *>(sm + OFF_AHI + o) = *reinterpret_cast<const uint4 *>(h);
+        *reinterpret_cast<uint4 *>(sm + OFF_ALO + o) = *reinterpret_cast<const uint4 *>(l);
     }
 }
 
@@ -260,9 +267,10 @@ __device__ void tc_stage(unsigned char *sm, uint64_t *bar, TcState &s) {
 }
 
 // After stage 1: thread (warp w, lane k2) reads D[., k2] of transform w
-// (= Y scaled by sc1), applies the twiddles w^(n1 k2), rescales for stage
-// 2 and stores its operand: row 32 w + n1, K = k2 (re) and 32 + k2 (im).
-// Returns the stage-2 unscale factor.
+// (= Y scaled by sc1, columns (re, im) of n1 at 2 n1, 2 n1 + 1), applies
+// the twiddles w^(n1 k2), rescales for stage 2 and stores its operand:
+// row 32 w + n1, K = 2 k2 (re) and 2 k2 + 1 (im), one 4-byte store each
+// for hi and lo.  Returns the stage-2 unscale factor.
 __device__ float tc_twiddle_transpose(unsigned char *sm, const TcTables *__restrict__ tab, const TcState &s,
                                       float inv1) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -276,22 +284,19 @@ __device__ float tc_twiddle_transpose(unsigned char *sm, const TcTables *__restr
         float2 w = __ldg(tab->tw + n1 * lane);
         w.x *= inv1;
         w.y *= inv1;
-        const float yr = y[n1], yi = y[32 + n1];
-        y[n1] = fmaf(yr, w.x, -yi * w.y);
-        y[32 + n1] = fmaf(yr, w.y, yi * w.x);
-        m = fmaxf(m, fmaxf(fabsf(y[n1]), fabsf(y[32 + n1])));
+        const float yr = y[2 * n1], yi = y[2 * n1 + 1];
+        y[2 * n1] = fmaf(yr, w.x, -yi * w.y);
+        y[2 * n1 + 1] = fmaf(yr, w.y, yi * w.x);
+        m = fmaxf(m, fmaxf(fabsf(y[2 * n1]), fabsf(y[2 * n1 + 1])));
     }
     const float2 sc = tc_scale(warp_max(m));
 #pragma unroll
     for (int n1 = 0; n1 < 32; n1++) {
-        __half hr, lr, hi_, li;
-        split2(y[n1] * sc.x, hr, lr);
-        split2(y[32 + n1] * sc.x, hi_, li);
-        const int row = 32 * warp + n1;
-        *reinterpret_cast<__half *>(sm + OFF_AHI + a_off(row, lane)) = hr;
-        *reinterpret_cast<__half *>(sm + OFF_ALO + a_off(row, lane)) = lr;
-        *reinterpret_cast<__half *>(sm + OFF_AHI + a_off(row, 32 + lane)) = hi_;
-        *reinterpret_cast<__half *>(sm + OFF_ALO + a_off(row, 32 + lane)) = li;
+        __half2 h, l;
+        split_pair(y[2 * n1] * sc.x, y[2 * n1 + 1] * sc.x, h, l);
+        const uint32_t o = a_off(32 * warp + n1, 2 * lane);
+        *reinterpret_cast<__half2 *>(sm + OFF_AHI + o) = h;
+        *reinterpret_cast<__half2 *>(sm + OFF_ALO + o) = l;
     }
     fence_async_smem();
     tc_fence_before();
@@ -327,23 +332,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const TcTables *_
     __syncthreads();
     tc_stage(sm, &bar, s);
     {
+        // stored as (re[32], im[32]) per row
         float v[32];
         const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
         tmem_ld32(ta, v);
 #pragma unroll
-        for (int i = 0; i < 32; i++) d1[(32 * warp + lane) * 64 + i] = v[i] * sc1.y;
+        for (int i = 0; i < 16; i++) {
+            d1[(32 * warp + lane) * 64 + i] = v[2 * i] * sc1.y;
+            d1[(32 * warp + lane) * 64 + 32 + i] = v[2 * i + 1] * sc1.y;
+        }
         tmem_ld32(ta + 32, v);
 #pragma unroll
-        for (int i = 0; i < 32; i++) d1[(32 * warp + lane) * 64 + 32 + i] = v[i] * sc1.y;
+        for (int i = 0; i < 16; i++) {
+            d1[(32 * warp + lane) * 64 + 16 + i] = v[2 * i] * sc1.y;
+            d1[(32 * warp + lane) * 64 + 48 + i] = v[2 * i + 1] * sc1.y;
+        }
     }
     const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
     tc_stage(sm, &bar, s);
-    float v[32], w[32];
+    float v[32];
     const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
-    tmem_ld32(ta, v);
-    tmem_ld32(ta + 32, w);
 #pragma unroll
-    for (int n2 = 0; n2 < 32; n2++) x[warp * 1024 + lane + 32 * n2] = make_float2(v[n2] * inv2, w[n2] * inv2);
+    for (int hf = 0; hf < 2; hf++) {
+        tmem_ld32(ta + 32 * hf, v);
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            x[warp * 1024 + lane + 32 * (16 * hf + i)] = make_float2(v[2 * i] * inv2, v[2 * i + 1] * inv2);
+    }
     tc_teardown(s);
 }
 
@@ -439,30 +454,42 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
             tc_stage(sm, &bar, s);
             const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
             tc_stage(sm, &bar, s);
-            // x[lane + 32 n2]: columns 0..31 (re) are result row r, 32..63
-            // (im) row r + 1; den first (their loads overlap the TMEM read)
+            // x[lane + 32 n2] = (re, im) at columns 2 n2, 2 n2 + 1: re is
+            // result row r, im row r + 1; 16 values of n2 per TMEM read, den
+            // first (their loads overlap the TMEM read).  The two rows'
+            // results interleave, so the extrema break ties by index
+            // explicitly (ext_add).
             const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
+            const long long rowBase0 = (long long)(tb.y0 + r) * m.rw + tb.x0, rowBase1 = rowBase0 + m.rw;
+            const bool on0 = live && r < bh && tb.y0 + r >= m.roiY0 && tb.y0 + r < m.roiY1;
+            const bool on1 = live && r + 1 < bh && tb.y0 + r + 1 >= m.roiY0 && tb.y0 + r + 1 < m.roiY1;
 #pragma unroll 1
-            for (int half = 0; half < 2; half++) {
-                const int rr = r + half;
-                const long long rowBase = (long long)(tb.y0 + rr) * m.rw + tb.x0;
-                const bool rowOn = live && rr < bh && tb.y0 + rr >= m.roiY0 && tb.y0 + rr < m.roiY1;
-                float den[32];
+            for (int hf = 0; hf < 2; hf++) {
+                float d0[16], d1[16];
 #pragma unroll
-                for (int n2 = 0; n2 < 32; n2++) {
-                    const int x = lane + 32 * n2;
-                    den[n2] = (rowOn && x < bw) ? __ldg(dens + rowBase + x) : 0.f;
+                for (int i = 0; i < 16; i++) {
+                    const int x = lane + 32 * (16 * hf + i);
+                    d0[i] = (on0 && x < bw) ? __ldg(dens + rowBase0 + x) : 0.f;
+                    d1[i] = (on1 && x < bw) ? __ldg(dens + rowBase1 + x) : 0.f;
                 }
                 float xv[32];
-                tmem_ld32(ta + 32 * half, xv);
-                if (rowOn && s.ok) {
+                tmem_ld32(ta + 32 * hf, xv);
+                if (s.ok) {
 #pragma unroll
-                    for (int n2 = 0; n2 < 32; n2++) {
-                        const int x = lane + 32 * n2;
+                    for (int i = 0; i < 16; i++) {
+                        const int x = lane + 32 * (16 * hf + i);
                         if (x < bw) {
-                            const float score = score_fast(xv[n2] * inv2, den[n2]);
-                            if (map) map[rowBase + x] = score;
-                            if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase + x);
+                            const bool inx = x >= xlo && x < xhi;
+                            if (on0) {
+                                const float score = score_fast(xv[2 * i] * inv2, d0[i]);
+                                if (map) map[rowBase0 + x] = score;
+                                if (inx) ext_add(e, score, rowBase0 + x);
+                            }
+                            if (on1) {
+                                const float score = score_fast(xv[2 * i + 1] * inv2, d1[i]);
+                                if (map) map[rowBase1 + x] = score;
+                                if (inx) ext_add(e, score, rowBase1 + x);
+                            }
                         }
                     }
                 }
@@ -513,11 +540,12 @@ cudaError_t tc_init() {
     std::vector<unsigned char> img(sizeof(TcTables), 0);
     TcTables *h = reinterpret_cast<TcTables *>(img.data());
     const double PI2 = 6.283185307179586476925286766559;
+    // B[n][k]: output n = 2 n1 + (0 re, 1 im), input k = 2 k1 + (0 re, 1 im)
     for (int n = 0; n < 64; n++)
         for (int k = 0; k < 64; k++) {
-            const int n1 = n & 31, k1 = k & 31;
+            const int n1 = n >> 1, k1 = k >> 1, on = n & 1, ik = k & 1;
             const double th = PI2 * (double)((n1 * k1) & 31) / 32.0, c = std::cos(th), sn = std::sin(th);
-            const double v = n < 32 ? (k < 32 ? c : -sn) : (k < 32 ? sn : c);
+            const double v = on == 0 ? (ik == 0 ? c : -sn) : (ik == 0 ? sn : c);
             const float vf = (float)v;
             const __half hi = __float2half_rn(vf), lo = __float2half_rn(vf - __half2float(hi));
             *reinterpret_cast<__half *>(h->bimg + b_off(n, k)) = hi;

@@ -250,10 +250,28 @@ int cvm_get_form(void);
 /* CVM_FORM_MIXED (fleets and one-shot matches alike) is the fast form with
  * its 1024-point inverse row transforms -- the inverse DFT of inverseRowPair
  * (impl.go:394-444) -- run on the tensor cores: two 32-point DFT stages as
- * tcgen05 tf32 matrix products on operands split hi + lo (three products,
- * FP32 accumulation), the twiddles between them in FP32.  Other transform
+ * tcgen05 kind::f16 matrix products on operands scaled per transform by a
+ * power of two and split into FP16 hi + lo halves (three products, FP32
+ * accumulation), the twiddles between them in FP32.  Other transform
  * widths run the fast form unchanged.  Scores differ from the fast form's
  * by rounding only. */
+
+/* The tile-plan autotuner of the fast and mixed forms (on by default; the
+ * exact form always runs newGoPlan's plan, impl.go:246-295, since its bits
+ * depend on it).  The first fast-form one-shot match or Matcher.Find of a
+ * shape (frame size, template size, channel mode, form) times up to four
+ * power-of-two tile plans on its own inputs -- newGoPlan's choice and the
+ * best of a GPU cost proxy -- and keeps the fastest if it beats newGoPlan's
+ * by more than 3 %; every later call of that shape in the process runs the
+ * cached plan (so results repeat exactly).  Calls made while their stream
+ * is being captured do not tune.  cvm_set_autotune returns the previous
+ * setting.  No reference counterpart (the reference always plans with
+ * newGoPlan). */
+int cvm_set_autotune(int on);
+/* The tuned shapes as a JSON array (frame, template, mode, cn, step, form,
+ * the chosen plan and each candidate's measured ms); returns the full
+ * length, writes at most len - 1 characters and a terminating NUL. */
+size_t cvm_autotune_report(char *buf, size_t len);
 
 /* Checks the tensor-core DFT path on this device: four inverse 1024-point
  * DFTs through the kernel's own stages against a double-precision DFT on

@@ -414,16 +414,18 @@ def test_near_flat_windows_vs_fp64(form):
     template was cut.  1024-wide tiles, so the mixed form runs its
     tensor-core rows here."""
     rng = np.random.default_rng(101)
-    img = np.empty((300, 1100, 4), np.uint8)
-    img[..., :3] = np.clip(np.rint(200 + rng.standard_normal((300, 1100, 3)) * 0.8), 0, 255)
+    img = np.empty((300, 1920, 4), np.uint8)
+    img[..., :3] = np.clip(np.rint(200 + rng.standard_normal((300, 1920, 3)) * 0.8), 0, 255)
     img[..., 3] = 255
     t = img[120:152, 400:496].copy()
-    assert oracle.plan(96, 32, 1100 - 95, 300 - 31).dft_w == 1024
+    assert oracle.plan(96, 32, 1920 - 95, 300 - 31).dft_w == 1024
     prev = cvm.SetForm(cvm.FORM_FAST if form == "fast" else cvm.FORM_MIXED)
+    prev_t = cvm.SetAutotune(False)  # newGoPlan's 1024-wide tiles
     try:
         m, _, _ = cvm.MatchMap(img, t)
     finally:
         cvm.SetForm(prev)
+        cvm.SetAutotune(prev_t)
     assert cvm.device_status() == 0
     map_check(m, fp64.ref_match_f64(img, t, 3), f"near-flat windows ({form})", ref_map=ref(img, t, 3))
     assert fp64.first_argmax(m) == (400, 120)

@@ -1,8 +1,8 @@
 """The mixed form (CVM_FORM_MIXED): the fast form with its 1024-point
 inverse row transforms -- the inverse DFT of inverseRowPair,
 impl.go:394-444 -- run as two 32-point DFT stages on the tensor cores
-(tcgen05 tf32 matrix products on hi + lo split operands, FP32
-accumulation).
+(tcgen05 kind::f16 matrix products on hi + lo split FP16 operands with
+per-transform power-of-two scaling, FP32 accumulation).
 
 First the path's own check (cvm_tc_selftest: the kernel's stages against a
 double-precision DFT on the host); then the form held to the metric's bar
@@ -64,12 +64,14 @@ def test_mixed_equals_fast_where_rows_are_not_1024():
     p = oracle.plan(64, 40, 420 - 63, 300 - 39)
     assert p.dft_w != 1024
     prev = cvm.SetForm(cvm.FORM_FAST)
+    prev_t = cvm.SetAutotune(False)  # both forms on newGoPlan's plan
     try:
         fast, _, _ = cvm.MatchMap(img, t)
         cvm.SetForm(cvm.FORM_MIXED)
         mixed, _, _ = cvm.MatchMap(img, t)
     finally:
         cvm.SetForm(prev)
+        cvm.SetAutotune(prev_t)
     assert np.array_equal(fast.view(np.uint32), mixed.view(np.uint32))
 
 
