@@ -452,9 +452,9 @@ def fleet_flops(buckets, members, tpl_shapes, pw, ph, cns):
 
 
 # which live-profiled kernels do which part of the counted work
-KERNEL_PART = {"k_fwd_rows": "fwd_rows", "k_cols_fwd": "fwd_cols", "k_cols_fwd_mul_inv": "fwd_cols+mul_inv_cols",
+KERNEL_PART = {"k_fwd_rows": "fwd_rows", "k_fwd_rows_tma": "fwd_rows", "k_cols_fwd": "fwd_cols", "k_cols_fwd_mul_inv": "fwd_cols+mul_inv_cols",
                "k_cols_fwd_sum_inv": "fwd_cols+mul_inv_cols", "k_cols_mul_inv": "mul_inv_cols",
-               "k_cols_sum_inv": "mul_inv_cols", "k_inv_rows": "inv_rows"}
+               "k_cols_sum_inv": "mul_inv_cols", "k_inv_rows": "inv_rows", "k_inv_rows_tc": "inv_rows"}
 
 
 def kernel_flops(parts, name):

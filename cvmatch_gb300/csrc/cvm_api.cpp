@@ -66,6 +66,7 @@ struct DeviceState {
     int status = CVM_OK;
     std::string msg;
     int device = 0;
+    int pageable = 0;  // the device reads pageable host memory coherently (cudaDevAttrPageableMemoryAccess)
     cudaMemPool_t pool = nullptr;
     std::mutex triMu;
     std::map<int, float2 *> tri;  // log2 n -> device twiddle table
@@ -97,6 +98,7 @@ int ensure_device() {
             d.msg = b;
             return;
         }
+        cudaDeviceGetAttribute(&d.pageable, cudaDevAttrPageableMemoryAccess, d.device);
         cudaMemPoolProps props;
         memset(&props, 0, sizeof props);
         props.allocType = cudaMemAllocationTypePinned;
@@ -381,8 +383,9 @@ int run_solo(const SoloJob &J, cudaStream_t st);
 // newGoPlan, impl.go:246-295: its bits depend on the plan).  The first
 // fast-form call of a shape times up to four candidate plans
 // (plan_candidates: newGoPlan's choice and the best of a GPU cost proxy)
-// on the call's own inputs -- each run once to warm up, then twice between
-// CUDA events on the call's stream -- and keeps the fastest if it beats
+// on the call's own inputs -- each run once to warm up, then twice from a
+// cold L2 between CUDA events on the call's stream, the faster of the two
+// counting -- and keeps the fastest if it beats
 // newGoPlan's by more than 3 %; the choice is cached per (frame size,
 // template size, channel mode, form) for the life of the process, so every
 // later call of the shape (one-shot calls and Matchers alike) runs the same
@@ -434,23 +437,40 @@ int solo_plan(const SoloJob &J, cudaStream_t st, Plan *out) {
             CVM_CUDA(cudaEventCreate(&e0));
             CVM_CUDA(cudaEventCreate(&e1));
         }
+        // Each timed run starts from a cold L2 (a transient buffer twice the
+        // L2's size cleared before it), as a frame that just arrived does.
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev().device);
+        void *flush = nullptr;
+        const size_t flushBytes = (size_t)2 * (l2 > 0 ? l2 : (64 << 20));
+        if (cudaMalloc(&flush, flushBytes) != cudaSuccess) {
+            cudaGetLastError();
+            flush = nullptr;
+        }
         int best = 0;
-        for (size_t i = 0; i < cands.size(); i++) {
+        int rc = CVM_OK;
+        for (size_t i = 0; i < cands.size() && rc == CVM_OK; i++) {
             SoloJob T = J;
             T.plan = &cands[i];
-            CVM_TRY(run_solo(T, st));
-            CVM_CUDA(cudaEventRecord(e0, st));
-            CVM_TRY(run_solo(T, st));
-            CVM_TRY(run_solo(T, st));
-            CVM_CUDA(cudaEventRecord(e1, st));
-            CVM_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            CVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            rc = run_solo(T, st);  // warm-up (workspace, twiddle tables)
+            float msBest = 0;
+            for (int r = 0; r < 2 && rc == CVM_OK; r++) {
+                if (flush) cudaMemsetAsync(flush, 0, flushBytes, st);
+                cudaEventRecord(e0, st);
+                rc = run_solo(T, st);
+                cudaEventRecord(e1, st);
+                if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(CVM_ERR_CUDA, "cvmatch_gpu: autotune timing failed");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (r == 0 || ms < msBest) msBest = ms;
+            }
             ent.cand[ent.n] = cands[i];
-            ent.ms[ent.n] = ms / 2;
+            ent.ms[ent.n] = msBest;
             ent.n++;
-            if (ms / 2 < ent.ms[best]) best = (int)i;
+            if (msBest < ent.ms[best]) best = (int)i;
         }
+        if (flush) cudaFree(flush);
+        if (rc != CVM_OK) return rc;
         // cands[0] is newGoPlan's choice whenever it qualifies
         const bool baseFirst = cands[0].dftW == out->dftW && cands[0].dftH == out->dftH;
         if (!baseFirst || ent.ms[best] < 0.97f * ent.ms[0]) ent.plan = cands[best];
@@ -784,6 +804,16 @@ int upload_image(PoolBuf &b, const uint8_t *src, long long stride, int w, int h,
         return CVM_OK;
     }
     cudaGetLastError();  // an unregistered pointer's query leaves no error behind
+    // A device that reads pageable host memory coherently (a Grace host's
+    // NVLink-C2C address translation) takes the caller's ordinary memory the
+    // same way: no synchronous staged copy by the driver, so the transfer
+    // overlaps the call's queued launches as a page-locked frame's does.
+    // The caller's buffer stays valid until the call returns (it
+    // synchronises before returning).
+    if (dev().pageable && (size_t)row * h >= (size_t(64) << 10)) {
+        CVM_CUDA(launch_ingest(b.p, (size_t)*pitch, src, (size_t)stride, row, h, st));
+        return CVM_OK;
+    }
     if (row * h <= (size_t(4) << 20)) {
         Staging *sg = staging(row * h, stageSlot);
         if (sg) {
@@ -1807,9 +1837,9 @@ int cvm_tc_selftest(double *dft_err, double *gemm_err) {
 
 int cvm_device_status(int *tc_timeouts) {
     CVM_TRY(ensure_device());
-    const int v = tc_error_read_clear();
-    if (v < 0) return fail(CVM_ERR_CUDA, "cvmatch_gpu: reading the device status failed");
-    if (tc_timeouts) *tc_timeouts = v;
+    const int v = tc_error_read_clear(), w = rows_error_read_clear();
+    if (v < 0 || w < 0) return fail(CVM_ERR_CUDA, "cvmatch_gpu: reading the device status failed");
+    if (tc_timeouts) *tc_timeouts = v | w;
     return CVM_OK;
 }
 

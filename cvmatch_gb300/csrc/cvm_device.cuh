@@ -10,6 +10,8 @@
 #include <climits>
 #include <cstdint>
 
+#include <cuda.h>
+
 #include "cvm_internal.h"
 
 namespace cvm {
@@ -125,11 +127,26 @@ struct FwdRowsArgs {
     // every CTA sums the template (this launch's one tile) itself, and
     // sub[k] = sum_k / subDiv
     int selfSums;
+    // TMA staging of the CTA's frame rows (the tensor map passed beside the
+    // arguments): boxes of 256 bytes x 2 pairsPerCta rows land at byte
+    // offset tmaSmemOff of the dynamic shared memory, box i at
+    // i * 256 * 2 pairsPerCta; 0 = plain loads
+    int tma;
+    unsigned int tmaSmemOff;
 };
 
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).
+// map: the frame's tensor map when a.tma (ignored otherwise).
 bool rows_fixed_length(int log2n);
-void launch_fwd_rows_fixed(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st);
+void launch_fwd_rows_fixed(const FwdRowsArgs &a, const CUtensorMap &map, dim3 grid, int threads, size_t smem,
+                           cudaStream_t st);
+// Encodes a 2-D tensor map over w x h bytes at img (row stride istride)
+// with boxes of 256 bytes x boxRows rows; false when the driver entry point
+// or the encoding is unavailable.
+bool encode_frame_map(CUtensorMap *map, const void *img, long long istride, long long wBytes, int h, int boxRows);
+// Sticky device flag of a TMA wait in the forward rows that gave up (read
+// and cleared).
+int rows_error_read_clear();
 void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st);
 // The column kernels specialised on dftH = 2^5 .. 2^12 (cvm_cols.cu).
 bool cols_fixed_length(int log2H);

@@ -249,6 +249,7 @@ cudaError_t launch_inv_rows_tc(const InvArgs &a, dim3 grid, cudaStream_t st);
 cudaError_t tc_selftest(double *dftErr, double *gemmErr);
 cudaError_t tc_init();  // the kernel's device tables, once (device set-up)
 int tc_error_read_clear();
+int rows_error_read_clear();  // the forward rows' TMA waits (cvm_rows.cu)
 
 // kernel-launch counter (exported by cvm_launch_count)
 void count_launches(unsigned n);

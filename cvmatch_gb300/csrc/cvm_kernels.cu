@@ -35,6 +35,9 @@
 #include <string>
 #include <vector>
 
+#include <algorithm>
+#include <cstring>
+
 #include "cvm_device.cuh"
 
 namespace cvm {
@@ -1701,11 +1704,12 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
             if (FAST) {
                 // A near-flat window (variance below 2^-14 of the window's
-                // mean square, decided on the exact integers) takes its
-                // denominator sqrt(varW varT) in double precision and is
-                // marked by the sign: the inverse rows then form its
-                // quotient in double precision too.
-                if (den > 0.f && (idv << 14) < area * q)
+                // mean square: diff2 = idiff / area against the squared sum
+                // q, both from the exact integers) takes its denominator
+                // sqrt(varW varT) in double precision and is marked by the
+                // sign: the inverse rows then form its quotient in double
+                // precision too.
+                if (den > 0.f && diff2 < __ull2float_rn(q) * 6.103515625e-05f)
                     den = -__double2float_rn(__dmul_rn(__dsqrt_rn(__dmul_rn(__ull2double_rn(idv), Pm.varScaleD)),
                                                        Pm.templNormD));
                 dens[(size_t)y * m.rw] = den;
@@ -1879,7 +1883,6 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
     const int groupLikely = (cnDev && chanCount == 4 && group == 4) ? 3 : group;
     int threads = P * groupLikely * (fc.n >= 16 ? fc.n / 16 : 1);
     threads = threads < 64 ? 64 : (threads > kThreads ? kThreads : (threads + 31) / 32 * 32);
-    ProfScope ps(label ? label : "k_fwd_rows", st);
     if (rows_fixed_length(fc.log2n)) {
         FwdRowsArgs a;
         a.img = img;
@@ -1902,13 +1905,39 @@ cudaError_t launch_fwd_rows(const uint8_t *img, long long istride, int step, int
         // a sample transform marks the fast form (the exact form packs the
         // reference's samples untouched): its butterflies may fuse
         a.fma = (mul != 1.0f || sub || subSums || selfSums) ? 1 : 0;
+        // Frames of 4-byte or gray pixels at 16-byte aligned addresses and
+        // pitches are staged by TMA: each CTA's rows in boxes of 256 bytes
+        // after the line buffers (the widest tile's span + the 16-byte
+        // rounding, per box row).  Frame extent: the tiles' loads lie inside
+        // the rows/columns the geometry covers (x0 + loadW <= rwT + twL - 1).
+        CUtensorMap map;
+        memset(&map, 0, sizeof map);
+        a.tma = 0;
+        a.tmaSmemOff = 0;
+        size_t smemT = smem;
+        const int maxLoadW = std::min(fc.n, g.blockW + g.twL - 1);
+        const long long wBytes = (long long)(g.rwT + g.twL - 1) * step;
+        const int hRows = g.rhT + g.thL - 1;
+        if (!selfSums && (step == 4 ? a.pix32 : step == 1) && (reinterpret_cast<uintptr_t>(img) & 15) == 0 &&
+            (istride & 15) == 0 && 2 * P <= 256 && fc.n >= 256) {
+            const int nbMax = (15 + maxLoadW * step + 255) / 256;
+            const size_t off = (smem + 127) / 128 * 128;
+            const size_t need = off + 128 + (size_t)nbMax * 256 * 2 * P;  // + the kernel's runtime alignment
+            if (need <= 200 * 1024 && encode_frame_map(&map, img, istride, wBytes, hRows, 2 * P)) {
+                a.tma = 1;
+                a.tmaSmemOff = (unsigned)off;
+                smemT = need;
+            }
+        }
+        ProfScope ps(label ? label : (a.tma ? "k_fwd_rows_tma" : "k_fwd_rows"), st);
         for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
             a.chanFirst = c0;
-            launch_fwd_rows_fixed(a, grid, threads, smem, st);
+            launch_fwd_rows_fixed(a, map, grid, threads, smemT, st);
             count_launches(1);
         }
         return cudaGetLastError();
     }
+    ProfScope ps(label ? label : "k_fwd_rows", st);
     if (mul != 1.0f || sub || subSums || selfSums) return cudaErrorInvalidValue;  // sample transform: fixed lengths only
     set_smem(k_fwd_rows, smem);
     for (int c0 = chanFirst; c0 < chanCount; c0 += group) {
@@ -1988,10 +2017,9 @@ int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, in
     // 4096 elements per CTA: the radix-16 passes (n/16 units per line) keep
     // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM);
     // wide: 8192 elements (two units per thread per pass), ~70 KB without
-    // the accumulator; the tensor-core kernel in a fleet: 32 row pairs (its
-    // per-CTA set-up -- TMEM, the DFT matrix copy -- spread over 8 MMA tiles)
+    // the accumulator; the tensor-core kernel takes the same
     int P = (wide ? 8192 : 4096) / fc.n;
-    if (tc && wide) P = 32;
+    (void)tc;  // (32 pairs per CTA measured slower for it: 6.25 against 5.14 ms per 256-member frame)
     if (P < 1) P = 1;
     // A tile emits at most rowsMax rows, and never more than dftH (a fleet
     // member's last band extends to its own result edge, still inside the

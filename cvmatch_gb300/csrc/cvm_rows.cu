@@ -9,6 +9,8 @@
 // at a constant offset from the unit's first element in the padded
 // shared-memory line, so a unit costs one address computation instead of
 // one per element.  Other lengths run the generic kernels.
+#include <cudaTypedefs.h>
+
 #include "cvm_device.cuh"
 
 namespace cvm {
@@ -229,8 +231,53 @@ __device__ __forceinline__ int div_cn(int line, int cn) {
 
 // ------------------------------------------------------------ forward rows
 
+__device__ int g_rows_error = 0;  // a TMA wait that gave up (sticky until read and cleared)
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Stages the CTA's frame rows with the tensor-memory accelerator: thread 0
+// arms the mbarrier with the byte count and issues one 2-D box copy (256
+// bytes x the map's box rows) per 256 bytes of the rows' span, x rounded
+// down to the 16-byte boundary the copy needs (the caller indexes from the
+// remainder); every thread then waits, up to ~2^31 cycles (~1 s), after
+// which the wait records g_rows_error and returns.
+__device__ __noinline__ void tma_stage_rows(const CUtensorMap *map, unsigned char *stage, uint64_t *bar, int xbase,
+                                            int y, int nb, int boxRows) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                     "r"((unsigned)(nb * 256 * boxRows))
+                     : "memory");
+        for (int i = 0; i < nb; i++)
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+                    "r"(smem_addr(stage + (size_t)i * 256 * boxRows)),
+                "l"(reinterpret_cast<unsigned long long>(map)), "r"(xbase + 256 * i), "r"(y), "r"(smem_addr(bar))
+                : "memory");
+    }
+    __syncthreads();
+    const uint32_t a = smem_addr(bar);
+    const long long t0 = clock64();
+    for (unsigned it = 0;; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(a)
+            : "memory");
+        if (ok) break;
+        if ((it & 255u) == 255u && clock64() - t0 > (1ll << 31)) {
+            atomicExch(&g_rows_error, 1);
+            break;
+        }
+    }
+}
+
 template <int LOG2N, bool F>
-__global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
+__global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a, const __grid_constant__ CUtensorMap map) {
     griddep_wait();
     griddep_launch();
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
@@ -280,6 +327,20 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
         for (int g = 0; g < 4; g++)
             subv[g] = a.subSums ? __fdiv_rn(__ull2float_rn(a.subSums[g]), a.subDiv) : a.sub[g];
     }
+    // TMA: the CTA's rows land in shared memory first (box i holds bytes
+    // [xbase + 256 i, +256) of each of the box's rows)
+    __shared__ __align__(8) uint64_t tmaBar;
+    const int boxRows = 2 * a.pairsPerCta;
+    // (128-byte aligned whatever the dynamic shared memory's base)
+    const unsigned char *stage = reinterpret_cast<const unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem) + a.tmaSmemOff + 127) & ~uintptr_t(127));
+    int tmaOff = 0;
+    if (a.tma) {
+        const int xbyte = b.x0 * a.step, xbase = xbyte & ~15;
+        tmaOff = xbyte - xbase;
+        const int nb = (tmaOff + b.loadW * a.step + 255) >> 8;
+        tma_stage_rows(&map, const_cast<unsigned char *>(stage), &tmaBar, xbase, b.y0 + 2 * pair0, nb, boxRows);
+    }
     // Pack rows r (real part) and r+1 (imaginary part) of every channel of
     // the group, each pixel read once for all of them.
     for (int it = tid; it < (P << LOG2N); it += nt) {
@@ -288,9 +349,15 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
         if (x < b.loadW) {
             const bool two = 2 * (pair0 + p) + 1 < b.loadH;
             const uint8_t *q = img0 + (long long)(2 * p) * istride + (long long)x * a.step;
+            long long qstride = istride;
+            if (a.tma) {
+                const int o = tmaOff + x * a.step;
+                q = stage + (size_t)(o >> 8) * 256 * boxRows + (size_t)(2 * p) * 256 + (o & 255);
+                qstride = 256;
+            }
             if (a.pix32) {
                 const unsigned int w0 = *reinterpret_cast<const unsigned int *>(q);
-                const unsigned int w1 = two ? *reinterpret_cast<const unsigned int *>(q + istride) : 0u;
+                const unsigned int w1 = two ? *reinterpret_cast<const unsigned int *>(q + qstride) : 0u;
 #pragma unroll
                 for (int g = 0; g < 4; g++) {
                     const int sh = 8 * (a.chanFirst + g);
@@ -302,7 +369,7 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a) {
                 for (int g = 0; g < 4; g++)
                     if (g < cn) {
                         va[g] = (float)q[a.chanFirst + g];
-                        if (two) vb[g] = (float)q[istride + a.chanFirst + g];
+                        if (two) vb[g] = (float)q[qstride + a.chanFirst + g];
                     }
             }
             // pixel * mul - sub: exact for the integer operands used (x1 - 0
@@ -654,13 +721,13 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
 }
 
 template <int L>
-void fwd_one(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
+void fwd_one(const FwdRowsArgs &a, const CUtensorMap &map, dim3 grid, int threads, size_t smem, cudaStream_t st) {
     if (a.fma) {
         set_smem(k_fwd_rows_t<L, true>, smem);
-        launch_k(k_fwd_rows_t<L, true>, grid, dim3(threads), smem, st, a);
+        launch_k(k_fwd_rows_t<L, true>, grid, dim3(threads), smem, st, a, map);
     } else {
         set_smem(k_fwd_rows_t<L, false>, smem);
-        launch_k(k_fwd_rows_t<L, false>, grid, dim3(threads), smem, st, a);
+        launch_k(k_fwd_rows_t<L, false>, grid, dim3(threads), smem, st, a, map);
     }
 }
 
@@ -679,17 +746,48 @@ void inv_one(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
 
 bool rows_fixed_length(int log2n) { return log2n >= 5 && log2n <= 12; }
 
-void launch_fwd_rows_fixed(const FwdRowsArgs &a, dim3 grid, int threads, size_t smem, cudaStream_t st) {
+void launch_fwd_rows_fixed(const FwdRowsArgs &a, const CUtensorMap &map, dim3 grid, int threads, size_t smem,
+                           cudaStream_t st) {
     switch (a.fc.log2n) {
-        case 5: fwd_one<5>(a, grid, threads, smem, st); break;
-        case 6: fwd_one<6>(a, grid, threads, smem, st); break;
-        case 7: fwd_one<7>(a, grid, threads, smem, st); break;
-        case 8: fwd_one<8>(a, grid, threads, smem, st); break;
-        case 9: fwd_one<9>(a, grid, threads, smem, st); break;
-        case 10: fwd_one<10>(a, grid, threads, smem, st); break;
-        case 11: fwd_one<11>(a, grid, threads, smem, st); break;
-        default: fwd_one<12>(a, grid, threads, smem, st); break;
+        case 5: fwd_one<5>(a, map, grid, threads, smem, st); break;
+        case 6: fwd_one<6>(a, map, grid, threads, smem, st); break;
+        case 7: fwd_one<7>(a, map, grid, threads, smem, st); break;
+        case 8: fwd_one<8>(a, map, grid, threads, smem, st); break;
+        case 9: fwd_one<9>(a, map, grid, threads, smem, st); break;
+        case 10: fwd_one<10>(a, map, grid, threads, smem, st); break;
+        case 11: fwd_one<11>(a, map, grid, threads, smem, st); break;
+        default: fwd_one<12>(a, map, grid, threads, smem, st); break;
     }
+}
+
+bool encode_frame_map(CUtensorMap *map, const void *img, long long istride, long long wBytes, int h, int boxRows) {
+    static PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    static int tried = 0;
+    if (!tried) {
+        tried = 1;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    }
+    if (!enc || boxRows < 1 || boxRows > 256) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)wBytes, (cuuint64_t)h};
+    const cuuint64_t strides[1] = {(cuuint64_t)istride};
+    const cuuint32_t box[2] = {256u, (cuuint32_t)boxRows};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(img), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int rows_error_read_clear() {
+    int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, g_rows_error, sizeof v) != cudaSuccess) return -1;
+    if (v) cudaMemcpyToSymbol(g_rows_error, &z, sizeof z);
+    return v;
 }
 
 void launch_inv_rows_fixed(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {

@@ -260,8 +260,10 @@ int cvm_get_form(void);
  * exact form always runs newGoPlan's plan, impl.go:246-295, since its bits
  * depend on it).  The first fast-form one-shot match or Matcher.Find of a
  * shape (frame size, template size, channel mode, form) times up to four
- * power-of-two tile plans on its own inputs -- newGoPlan's choice and the
- * best of a GPU cost proxy -- and keeps the fastest if it beats newGoPlan's
+ * power-of-two tile plans on its own inputs, each from a cold L2 (a
+ * transient device buffer of twice the L2's size is cleared before each
+ * timed run) -- newGoPlan's choice and the best of a GPU cost proxy -- and
+ * keeps the fastest if it beats newGoPlan's
  * by more than 3 %; every later call of that shape in the process runs the
  * cached plan (so results repeat exactly).  Calls made while their stream
  * is being captured do not tune.  cvm_set_autotune returns the previous
@@ -281,9 +283,11 @@ size_t cvm_autotune_report(char *buf, size_t len);
 int cvm_tc_selftest(double *dft_err, double *gemm_err);
 
 /* Sticky device-side failure flags since the last call (then cleared):
- * *tc_timeouts = 1 when a tensor-core kernel gave up waiting for its
- * matrix products (its results are invalid).  Waits are bounded, so a
- * failure there returns instead of hanging.  No reference counterpart. */
+ * *tc_timeouts = 1 when a kernel gave up waiting for its asynchronous
+ * hardware -- the tensor-core DFT for its matrix products, the forward
+ * rows for their TMA frame copies -- and its results are invalid.  Waits
+ * are bounded, so such a failure returns instead of hanging.  No reference
+ * counterpart. */
 int cvm_device_status(int *tc_timeouts);
 
 /* ------------------------------------------------------- frame streams */
