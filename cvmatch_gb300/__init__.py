@@ -104,6 +104,7 @@ def lib():
             L.cvm_fleet_set_roi.argtypes = [vp, i32, i32, i32, i32, i32]
             L.cvm_fleet_set_form.argtypes = [vp, i32]
             L.cvm_fleet_buckets.argtypes = [vp, i32, i32, vp, i32]
+            L.cvm_fleet_set_wave.argtypes = [vp, i32]
             L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
             L.cvm_get_form.argtypes = []
@@ -375,6 +376,11 @@ class Fleet:
         tensor cores) or FORM_FAST (zero-mean templates, channels summed in the
         frequency domain; see cvm_fleet_set_form)."""
         _check(lib().cvm_fleet_set_form(self._h, form))
+
+    def SetWave(self, members: int):
+        """At most `members` member tails per wave (0: by the workspace
+        budget); see cvm_fleet_set_wave."""
+        _check(lib().cvm_fleet_set_wave(self._h, members))
 
     def buckets(self, pw: int, ph: int):
         """[(tw, th, dftW, dftH, blockW, blockH, dh2, tiles, members)] per

@@ -1112,6 +1112,7 @@ struct cvm_fleet {
     std::vector<int32_t> roi;  // per member x, y, w, h in frame pixels (w <= 0: the whole frame)
     uint64_t roiGen = 0;       // bumped by every cvm_fleet_set_roi
     int form = CVM_FORM_EXACT; // arithmetic of the member tails (cvm_fleet_set_form)
+    int waveMembers = 0;       // members per wave of tails (0: by the 4 GB workspace budget)
     ~cvm_fleet() {
         if (dP) cudaFree(dP);
     }
@@ -1285,6 +1286,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         frameBytes = std::max(frameBytes, fb);
         partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
+        if (f->waveMembers > 0) w = std::min(w, f->waveMembers);
         w = std::min<int>(w, (int)bg.members.size());
         wave[b] = w;
         size_t wb = Arena::bytes((size_t)w * lanesPer, sizeof(float2));
@@ -2007,6 +2009,12 @@ int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap)
         o[8] = (int32_t)bk.members.size();
     }
     return nb;
+}
+
+int cvm_fleet_set_wave(cvm_fleet *f, int members) {
+    if (!f || members < 0) return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad wave size");
+    f->waveMembers = members;
+    return CVM_OK;
 }
 
 int cvm_fleet_bucket_members(const cvm_fleet *f, int b, int32_t *out, int cap) {

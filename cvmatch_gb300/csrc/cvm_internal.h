@@ -67,9 +67,6 @@ struct DevParams {
     int flat;
     long long varSum;
     float templNorm, numScale, varScale;
-    // the same two constants in double precision: the fast form's near-flat
-    // windows take their denominator from them
-    double templNormD, varScaleD;
 };
 
 // Per-frame flags written on the device.

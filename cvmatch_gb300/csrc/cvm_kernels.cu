@@ -305,10 +305,8 @@ __device__ void finalize_params(DevParams &p, const DevFrame &F, int *cnMax) {
     p.varSum = vs;
     p.flat = vs == 0;
     const double ad = __dmul_rn((double)p.tw, (double)p.th);
-    p.templNormD = __dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad));
-    p.varScaleD = __ddiv_rn(1.0, ad);
-    p.templNorm = __double2float_rn(p.templNormD);
-    p.varScale = __double2float_rn(p.varScaleD);
+    p.templNorm = __double2float_rn(__dsqrt_rn(__ddiv_rn(__ll2double_rn(vs), ad)));
+    p.varScale = __double2float_rn(__ddiv_rn(1.0, ad));
     p.numScale = cn == 1 ? __double2float_rn(__ddiv_rn(__ll2double_rn((long long)p.tsum[0]), ad)) : p.varScale;
     if (!p.flat) atomicMax(cnMax, cn);
 }
@@ -1705,13 +1703,10 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             if (FAST) {
                 // A near-flat window (variance below 2^-14 of the window's
                 // mean square: diff2 = idiff / area against the squared sum
-                // q, both from the exact integers) takes its denominator
-                // sqrt(varW varT) in double precision and is marked by the
-                // sign: the inverse rows then form its quotient in double
-                // precision too.
-                if (den > 0.f && diff2 < __ull2float_rn(q) * 6.103515625e-05f)
-                    den = -__double2float_rn(__dmul_rn(__dsqrt_rn(__dmul_rn(__ull2double_rn(idv), Pm.varScaleD)),
-                                                       Pm.templNormD));
+                // q, both from the exact integers) is marked by the sign of
+                // its den: the inverse rows form its quotient in double
+                // precision.
+                if (den > 0.f && diff2 < __ull2float_rn(q) * 6.103515625e-05f) den = -den;
                 dens[(size_t)y * m.rw] = den;
             } else {
                 const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);

@@ -25,8 +25,10 @@
 // largest magnitude just below 2^14 (FP16's range), then every operand is
 // split as hi = fp16(v), lo = fp16(v - hi), and the products are
 // accumulated as Ahi Bhi + Alo Bhi + Ahi Blo: ~22 significant bits per
-// operand, the FP32 cascade's order of error.  The scale is undone (exactly,
-// a power of two) when D is read back.  One thread issues the MMAs;
+// operand, the FP32 cascade's order of error.  The stage-2 operand keeps
+// that scale times 2^-6 (a 32-point stage grows magnitudes by less than
+// 2^6), and the scale is undone (exactly, a power of two) when D is read
+// back.  One thread issues the MMAs;
 // tcgen05.commit arrives on an mbarrier the CTA waits on (a bounded wait:
 // after ~2 s without the arrival it records a device error, frees its TMEM
 // and returns); D comes back from TMEM with tcgen05.ld.  Operands are staged
@@ -157,6 +159,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 16 consecutive TMEM columns (the same contract as tmem_ld32).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
 // The power of two that scales a transform whose largest magnitude is m
 // to just below 2^kTcScaleExp (1 for an all-zero transform), and its inverse.
 __device__ __forceinline__ float2 tc_scale(float m) {
@@ -268,40 +284,36 @@ __device__ void tc_stage(unsigned char *sm, uint64_t *bar, TcState &s) {
 
 // After stage 1: thread (warp w, lane k2) reads D[., k2] of transform w
 // (= Y scaled by sc1, columns (re, im) of n1 at 2 n1, 2 n1 + 1), applies
-// the twiddles w^(n1 k2), rescales for stage 2 and stores its operand:
-// row 32 w + n1, K = 2 k2 (re) and 2 k2 + 1 (im), one 4-byte store each
-// for hi and lo.  Returns the stage-2 unscale factor.
-__device__ float tc_twiddle_transpose(unsigned char *sm, const TcTables *__restrict__ tab, const TcState &s,
-                                      float inv1) {
+// the twiddles w^(n1 k2) and stores the stage-2 operand: row 32 w + n1,
+// K = 2 k2 (re) and 2 k2 + 1 (im), one 4-byte store each for hi and lo.
+// The stage-2 operand is Y w^(n1 k2) scaled by sc1 2^-6: the twiddles have
+// unit modulus and a 32-point stage grows magnitudes by at most 32 sqrt(2)
+// < 2^6, so it stays below 2^14 as stage 1's did, with no second search
+// for the maximum; 32 columns at a time.
+__device__ void tc_twiddle_transpose(unsigned char *sm, const TcTables *__restrict__ tab, const TcState &s) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float y[64];
     const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
-    tmem_ld32(ta, y);
-    tmem_ld32(ta + 32, y + 32);
-    float m = 0.f;
+#pragma unroll 1
+    for (int hf = 0; hf < 2; hf++) {
+        float y[32];
+        tmem_ld32(ta + 32 * hf, y);
 #pragma unroll
-    for (int n1 = 0; n1 < 32; n1++) {
-        float2 w = __ldg(tab->tw + n1 * lane);
-        w.x *= inv1;
-        w.y *= inv1;
-        const float yr = y[2 * n1], yi = y[2 * n1 + 1];
-        y[2 * n1] = fmaf(yr, w.x, -yi * w.y);
-        y[2 * n1 + 1] = fmaf(yr, w.y, yi * w.x);
-        m = fmaxf(m, fmaxf(fabsf(y[2 * n1]), fabsf(y[2 * n1 + 1])));
-    }
-    const float2 sc = tc_scale(warp_max(m));
-#pragma unroll
-    for (int n1 = 0; n1 < 32; n1++) {
-        __half2 h, l;
-        split_pair(y[2 * n1] * sc.x, y[2 * n1 + 1] * sc.x, h, l);
-        const uint32_t o = a_off(32 * warp + n1, 2 * lane);
-        *reinterpret_cast<__half2 *>(sm + OFF_AHI + o) = h;
-        *reinterpret_cast<__half2 *>(sm + OFF_ALO + o) = l;
+        for (int j = 0; j < 16; j++) {
+            const int n1 = 16 * hf + j;
+            float2 w = __ldg(tab->tw + n1 * lane);
+            w.x *= 0.015625f;  // 2^-6
+            w.y *= 0.015625f;
+            const float yr = y[2 * j], yi = y[2 * j + 1];
+            __half2 h, l;
+            split_pair(fmaf(yr, w.x, -yi * w.y), fmaf(yr, w.y, yi * w.x), h, l);
+            const uint32_t o = a_off(32 * warp + n1, 2 * lane);
+            *reinterpret_cast<__half2 *>(sm + OFF_AHI + o) = h;
+            *reinterpret_cast<__half2 *>(sm + OFF_ALO + o) = l;
+        }
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
-    return sc.y;
 }
 
 // ------------------------------------------------------------ self-test
@@ -348,7 +360,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_selftest(const TcTables *_
             d1[(32 * warp + lane) * 64 + 48 + i] = v[2 * i + 1] * sc1.y;
         }
     }
-    const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
+    tc_twiddle_transpose(sm, tab, s);
+    const float inv2 = sc1.y * 64.f;  // the stage-2 operand was scaled by sc1 2^-6
     tc_stage(sm, &bar, s);
     float v[32];
     const uint32_t ta = s.tmem + ((uint32_t)(32 * warp) << 16);
@@ -452,7 +465,8 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
             fence_async_smem();
             __syncthreads();
             tc_stage(sm, &bar, s);
-            const float inv2 = tc_twiddle_transpose(sm, tab, s, sc1.y);
+            tc_twiddle_transpose(sm, tab, s);
+            const float inv2 = sc1.y * 64.f;  // the stage-2 operand was scaled by sc1 2^-6
             tc_stage(sm, &bar, s);
             // x[lane + 32 n2] = (re, im) at columns 2 n2, 2 n2 + 1: re is
             // result row r, im row r + 1; 16 values of n2 per TMEM read, den
@@ -464,20 +478,21 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
             const bool on0 = live && r < bh && tb.y0 + r >= m.roiY0 && tb.y0 + r < m.roiY1;
             const bool on1 = live && r + 1 < bh && tb.y0 + r + 1 >= m.roiY0 && tb.y0 + r + 1 < m.roiY1;
 #pragma unroll 1
-            for (int hf = 0; hf < 2; hf++) {
-                float d0[16], d1[16];
+            for (int q = 0; q < 4; q++) {
+                // results x = lane + 32 n2, n2 = 8 q .. 8 q + 7 (TMEM columns 16 q ..)
+                float d0[8], d1[8];
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const int x = lane + 32 * (16 * hf + i);
+                for (int i = 0; i < 8; i++) {
+                    const int x = lane + 32 * (8 * q + i);
                     d0[i] = (on0 && x < bw) ? __ldg(dens + rowBase0 + x) : 0.f;
                     d1[i] = (on1 && x < bw) ? __ldg(dens + rowBase1 + x) : 0.f;
                 }
-                float xv[32];
-                tmem_ld32(ta + 32 * hf, xv);
+                float xv[16];
+                tmem_ld16(ta + 16 * q, xv);
                 if (s.ok) {
 #pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        const int x = lane + 32 * (16 * hf + i);
+                    for (int i = 0; i < 8; i++) {
+                        const int x = lane + 32 * (8 * q + i);
                         if (x < bw) {
                             const bool inx = x >= xlo && x < xhi;
                             if (on0) {

@@ -330,6 +330,14 @@ int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]);
  * th, dftW, dftH, blockW, blockH, dh2, tiles, members}.  Flat members are
  * in no bucket.  Host-only; no device. */
 int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap);
+/* At most `members` member tails per wave of a FindAll (0, the default:
+ * as many as a 4 GB workspace holds).  Each wave's tails write their
+ * column-pass spectra (~25 MB per member on a 2560x1440 frame) before the
+ * row pass reads them back: small waves bound the workspace and keep those
+ * spectra in L2, large waves need fewer launches.  Results do not depend
+ * on it.  Not to be called while a FindAll on the same fleet runs. */
+int cvm_fleet_set_wave(cvm_fleet *f, int members);
+
 /* Bucket b's members (construction-order indices, ascending): returns
  * their count (negative on error) and writes the first cap of them. */
 int cvm_fleet_bucket_members(const cvm_fleet *f, int b, int32_t *out, int cap);
