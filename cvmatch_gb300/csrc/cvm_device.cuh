@@ -238,20 +238,27 @@ __device__ __forceinline__ float score_exact(float num, float den) {
 }
 
 // The fast form's ladder: the hardware division (within 2 ulp), except on
-// near-flat windows (the statistics kernel stores their den negated: the
-// window variance below 2^-14 of its mean square), whose quotient num / den
-// is formed in double precision and rounded once (a call on the rare path,
-// so the epilogues keep their registers).
+// near-flat windows, whose quotient num / den is formed in double precision
+// and rounded once (a call on the rare path, so the epilogues keep their
+// registers).  Near-flat: the window's variance (summed over its channels,
+// from the exact integer sums) below one grey level squared, i.e.
+// idiff < area^2, i.e. 0 < den < denFlat = sqrt(area) * templNorm -- a
+// per-member constant (near_flat_den), so the test costs the epilogue one
+// comparison and the statistics kernel nothing.
 __device__ __noinline__ float score_near_flat(float num, float den) {
-    const double d = -(double)den, n = (double)num;
+    const double d = (double)den, n = (double)num;
     if (fabs(n) < d) return __double2float_rn(__ddiv_rn(n, d));
     if (fabs(n) < d * 1.125) return num > 0.f ? 1.f : -1.f;
     return 0.f;
 }
 
-__device__ __forceinline__ float score_fast(float num, float den) {
+__device__ __forceinline__ float near_flat_den(int tw, int th, float templNorm) {
+    return sqrtf((float)tw * (float)th) * templNorm;
+}
+
+__device__ __forceinline__ float score_fast(float num, float den, float denFlat) {
     const float an = fabsf(num);
-    if (den < 0.f) return score_near_flat(num, den);
+    if (den > 0.f && den < denFlat) return score_near_flat(num, den);
     if (an < den) return __fdividef(num, den);
     if (an < den * 1.125f) return num > 0.f ? 1.f : -1.f;
     return 0.f;

@@ -1699,14 +1699,8 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
             // FAST: the square root from the hardware reciprocal square root
             // (within 2 ulp) instead of the correctly rounded sequence
             const float sd = FAST ? __fmul_rn(diff2, rsqrtf(diff2)) : __fsqrt_rn(diff2);
-            float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
+            const float den = diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
             if (FAST) {
-                // A near-flat window (variance below 2^-14 of the window's
-                // mean square: diff2 = idiff / area against the squared sum
-                // q, both from the exact integers) is marked by the sign of
-                // its den: the inverse rows form its quotient in double
-                // precision.
-                if (den > 0.f && diff2 < __ull2float_rn(q) * 6.103515625e-05f) den = -den;
                 dens[(size_t)y * m.rw] = den;
             } else {
                 const float l0 = CN == 1 ? __uint2float_rn(s[0]) : f32_via_f64((long long)cross);

@@ -504,6 +504,7 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
     const int hwp = fc.hwp, log2H = fc.log2H;
     const int tid = threadIdx.x;
     const bool flat = Pm.flat != 0;
+    const float denFlat = near_flat_den(m.tw, m.th, Pm.templNorm);  // fast form: near-flat windows below it
     float *acc = reinterpret_cast<float *>(smem + (size_t)a.pairsPerCta * LD);  // [P][2][N]
     Ext e;
     ext_init(e);
@@ -640,7 +641,7 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
                             num = __fsub_rn(num, dv[half][i].x);
                         }
                         const float den = dv[half][i].y;
-                        const float score = FAST ? score_fast(num, den) : score_exact(num, den);
+                        const float score = FAST ? score_fast(num, den, denFlat) : score_exact(num, den);
                         if (map) map[rowBase[half] + x] = score;
                         if (x >= xlo && x < xhi) ext_add_inc(e, score, rowBase[half] + x);
                     }
@@ -682,7 +683,7 @@ __global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 
                             num = __fsub_rn(acc[(size_t)rr * N + x], td[q].x);
                         }
                         const float den = td[q].y;
-                        score = fast ? score_fast(num, den) : score_exact(num, den);
+                        score = fast ? score_fast(num, den, denFlat) : score_exact(num, den);
                     }
                     if (map) map[rowBase + x] = score;
                     // rows ascend, and x ascends within a row: increasing indices

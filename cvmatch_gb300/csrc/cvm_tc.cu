@@ -407,6 +407,7 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
         if (ya >= m.roiY1 || yb <= m.roiY0 || tb.x0 >= m.roiX1 || tb.x0 + bw <= m.roiX0) P = 0;
     }
     const bool flat = Pm.flat != 0;
+    const float denFlat = near_flat_den(m.tw, m.th, Pm.templNorm);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int log2H = fc.log2H, hwp = fc.hwp;
     const float2 *cb = a.ms.scratch[a.cls] + (size_t)slot * a.ms.scratchStride[a.cls] +
@@ -496,12 +497,12 @@ __global__ void __launch_bounds__(kTcThreads, 4) k_inv_rows_tc(InvArgs a) {
                         if (x < bw) {
                             const bool inx = x >= xlo && x < xhi;
                             if (on0) {
-                                const float score = score_fast(xv[2 * i] * inv2, d0[i]);
+                                const float score = score_fast(xv[2 * i] * inv2, d0[i], denFlat);
                                 if (map) map[rowBase0 + x] = score;
                                 if (inx) ext_add(e, score, rowBase0 + x);
                             }
                             if (on1) {
-                                const float score = score_fast(xv[2 * i + 1] * inv2, d1[i]);
+                                const float score = score_fast(xv[2 * i + 1] * inv2, d1[i], denFlat);
                                 if (map) map[rowBase1 + x] = score;
                                 if (inx) ext_add(e, score, rowBase1 + x);
                             }
