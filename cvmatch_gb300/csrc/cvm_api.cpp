@@ -1113,6 +1113,7 @@ struct cvm_fleet {
     uint64_t roiGen = 0;       // bumped by every cvm_fleet_set_roi
     int form = CVM_FORM_EXACT; // arithmetic of the member tails (cvm_fleet_set_form)
     int waveMembers = 0;       // members per wave of tails (0: by the 4 GB workspace budget)
+    Plan forcedPlan;           // every bucket's plan when dftW > 0 (the autotuner's trial fleets)
     ~cvm_fleet() {
         if (dP) cudaFree(dP);
     }
@@ -1157,7 +1158,140 @@ void table_roi(const cvm_fleet *f, const FleetBucketGeom &bg, std::vector<DevMem
 // Per parent size: every bucket's plan and every member's spectrum on its
 // bucket's plan (buildGeom, fleet.go:337-390), plus the device member
 // tables the tail kernels index.
-int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
+int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int pw, int ph, cvm_result *dOut,
+                   cudaStream_t st);
+
+// The fleet half of the autotuner: a bucket's plan in the fast forms.  The
+// cost of a plan is measured on trial fleets of the bucket's own members
+// (k and 2k of them, spread over the bucket) on the caller's frame, each
+// run from a cold L2: the difference gives the per-member tail cost, the
+// rest the frame's shared cost, and the bucket's cost is shared + n x
+// per-member.  newGoPlan's plan (fleet.go:356-365) is kept unless another
+// candidate beats it by more than 3 %.  Cached per (frame size, bucket
+// maxima, members, step, form) for the process.
+struct FleetTuneKey {
+    int pw, ph, tw, th, step, form, n;
+    bool operator<(const FleetTuneKey &o) const {
+        return std::tie(pw, ph, tw, th, step, form, n) < std::tie(o.pw, o.ph, o.tw, o.th, o.step, o.form, o.n);
+    }
+};
+struct FleetTuneEntry {
+    Plan plan;
+    int n = 0;
+    Plan cand[4];
+    float perMember[4] = {0, 0, 0, 0}, shared[4] = {0, 0, 0, 0}, total[4] = {0, 0, 0, 0};
+};
+std::map<FleetTuneKey, FleetTuneEntry> g_fleetTune;
+
+int tune_bucket_plan(cvm_fleet *f, const Bucket &b, const uint8_t *dParent, long long pstride, int pw, int ph,
+                     cudaStream_t st, Plan *out) {
+    const int rwF = pw - b.tw + 1, rhF = ph - b.th + 1;
+    *out = make_plan(b.tw, b.th, rwF, rhF);
+    const int nm = (int)b.members.size();
+    if (f->form == CVM_FORM_EXACT || !g_autotune.load() || nm < 4 || !dParent) return CVM_OK;
+    const FleetTuneKey key{pw, ph, b.tw, b.th, f->step, f->form, nm};
+    {
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        auto it = g_fleetTune.find(key);
+        if (it != g_fleetTune.end()) {
+            *out = it->second.plan;
+            return CVM_OK;
+        }
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return CVM_OK;
+    }
+    std::vector<Plan> cands = plan_candidates(b.tw, b.th, rwF, rhF, 4);
+    FleetTuneEntry ent;
+    ent.plan = *out;
+    if (cands.size() > 1) {
+        CVM_CUDA(cudaStreamSynchronize(st));  // the frame, written on the caller's stream
+        cudaStream_t ts = thread_stream();
+        thread_local cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (!e0) {
+            CVM_CUDA(cudaEventCreate(&e0));
+            CVM_CUDA(cudaEventCreate(&e1));
+        }
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev().device);
+        const size_t flushBytes = (size_t)2 * (l2 > 0 ? l2 : (64 << 20));
+        void *flush = nullptr;
+        if (cudaMalloc(&flush, flushBytes) != cudaSuccess) {
+            cudaGetLastError();
+            flush = nullptr;
+        }
+        const int k1 = std::max(2, std::min(8, nm / 2)), k2 = std::min(nm, 2 * k1);
+        cvm_result *dOut = nullptr;
+        if (cudaMalloc(&dOut, (size_t)k2 * sizeof(cvm_result)) != cudaSuccess) {
+            cudaGetLastError();
+            if (flush) cudaFree(flush);
+            return CVM_OK;  // nothing to time with: newGoPlan's plan
+        }
+        int rc = CVM_OK, best = 0;
+        for (size_t c = 0; c < cands.size() && rc == CVM_OK; c++) {
+            float t[2] = {0, 0};
+            for (int which = 0; which < 2 && rc == CVM_OK; which++) {
+                const int k = which ? k2 : k1;
+                cvm_fleet trial;
+                trial.step = f->step;
+                trial.form = f->form;
+                trial.forcedPlan = cands[c];
+                Bucket one;
+                one.tw = b.tw;
+                one.th = b.th;
+                for (int i = 0; i < k; i++) {
+                    trial.ms.push_back(f->ms[b.members[(size_t)i * nm / k]]);
+                    one.members.push_back(i);
+                }
+                trial.buckets.push_back(one);
+                if (cudaMalloc(&trial.dP, (size_t)k * sizeof(DevParams)) != cudaSuccess) {
+                    rc = fail(CVM_ERR_CUDA, "cvmatch_gpu: autotune workspace");
+                    break;
+                }
+                for (int i = 0; i < k && rc == CVM_OK; i++)
+                    if (cudaMemcpy(trial.dP + i, trial.ms[i]->dP, sizeof(DevParams), cudaMemcpyDeviceToDevice) !=
+                        cudaSuccess)
+                        rc = fail(CVM_ERR_CUDA, "cvmatch_gpu: autotune workspace");
+                if (rc == CVM_OK) rc = fleet_find_dev(&trial, dParent, pstride, pw, ph, dOut, ts);  // geometry + warm-up
+                float msBest = 0;
+                for (int r = 0; r < 2 && rc == CVM_OK; r++) {
+                    if (flush) cudaMemsetAsync(flush, 0, flushBytes, ts);
+                    cudaEventRecord(e0, ts);
+                    rc = fleet_find_dev(&trial, dParent, pstride, pw, ph, dOut, ts);
+                    cudaEventRecord(e1, ts);
+                    if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(CVM_ERR_CUDA, "cvmatch_gpu: autotune timing failed");
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (r == 0 || ms < msBest) msBest = ms;
+                }
+                if (rc == CVM_OK) cudaStreamSynchronize(ts);
+                t[which] = msBest;
+            }
+            const float per = k2 > k1 ? std::max(0.f, (t[1] - t[0]) / (float)(k2 - k1)) : t[0] / (float)k1;
+            const float shared = std::max(0.f, t[0] - per * (float)k1);
+            ent.cand[ent.n] = cands[c];
+            ent.perMember[ent.n] = per;
+            ent.shared[ent.n] = shared;
+            ent.total[ent.n] = shared + per * (float)nm;
+            if (ent.total[ent.n] < ent.total[best]) best = ent.n;
+            ent.n++;
+        }
+        cudaFree(dOut);
+        if (flush) cudaFree(flush);
+        if (rc != CVM_OK) return rc;
+        const bool baseFirst = cands[0].dftW == out->dftW && cands[0].dftH == out->dftH;
+        if (!baseFirst || ent.total[best] < 0.97f * ent.total[0]) ent.plan = cands[best];
+    }
+    std::lock_guard<std::mutex> lk(g_tuneMu);
+    auto ins = g_fleetTune.emplace(key, ent);
+    *out = ins.first->second.plan;
+    return CVM_OK;
+}
+
+int fleet_geom(cvm_fleet *f, const uint8_t *dParent, long long pstride, int pw, int ph, cudaStream_t cst,
+               std::shared_ptr<FleetGeom> &out) {
     std::lock_guard<std::mutex> lk(f->mu);
     if (f->geom && f->geom->pw == pw && f->geom->ph == ph) {
         out = f->geom;
@@ -1171,7 +1305,12 @@ int fleet_geom(cvm_fleet *f, int pw, int ph, std::shared_ptr<FleetGeom> &out) {
     for (const Bucket &b : f->buckets) {
         auto bg = std::make_unique<FleetBucketGeom>();
         const int rwF = pw - b.tw + 1, rhF = ph - b.th + 1;
-        CVM_TRY(make_geom(b.tw, b.th, rwF, rhF, b.th, bg->G));
+        Plan plan;
+        if (f->forcedPlan.dftW > 0)
+            plan = f->forcedPlan;
+        else
+            CVM_TRY(tune_bucket_plan(f, b, dParent, pstride, pw, ph, cst, &plan));
+        CVM_TRY(make_geom(b.tw, b.th, rwF, rhF, b.th, bg->G, &plan));
         bg->form = effective_form(f->form, bg->G);
         const bool bfast = bg->form != CVM_FORM_EXACT;
         bg->cnS = f->step;
@@ -1258,7 +1397,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         }
     if (f->buckets.empty()) return CVM_OK;
     std::shared_ptr<FleetGeom> fg;
-    CVM_TRY(fleet_geom(f, pw, ph, fg));
+    CVM_TRY(fleet_geom(f, dParent, pstride, pw, ph, st, fg));
     {
         // regions of interest changed since the member tables were built
         std::lock_guard<std::mutex> lk(f->mu);
@@ -1804,6 +1943,24 @@ size_t cvm_autotune_report(char *buf, size_t len) {
             for (int i = 0; i < e.n; i++) {
                 snprintf(b, sizeof b, "%s{\"plan\":[%d,%d],\"ms\":%.5f}", i ? "," : "", e.cand[i].dftW, e.cand[i].dftH,
                          (double)e.ms[i]);
+                j += b;
+            }
+            j += "]}";
+            first = false;
+        }
+        for (const auto &kv : g_fleetTune) {
+            const FleetTuneKey &k = kv.first;
+            const FleetTuneEntry &e = kv.second;
+            char b[256];
+            snprintf(b, sizeof b,
+                     "%s{\"fleet\":true,\"frame\":[%d,%d],\"bucket\":[%d,%d],\"members\":%d,\"step\":%d,"
+                     "\"form\":%d,\"plan\":[%d,%d],\"candidates\":[",
+                     first ? "" : ",", k.pw, k.ph, k.tw, k.th, k.n, k.step, k.form, e.plan.dftW, e.plan.dftH);
+            j += b;
+            for (int i = 0; i < e.n; i++) {
+                snprintf(b, sizeof b, "%s{\"plan\":[%d,%d],\"ms_per_member\":%.5f,\"ms_shared\":%.5f,\"ms\":%.5f}",
+                         i ? "," : "", e.cand[i].dftW, e.cand[i].dftH, (double)e.perMember[i], (double)e.shared[i],
+                         (double)e.total[i]);
                 j += b;
             }
             j += "]}";

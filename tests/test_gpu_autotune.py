@@ -1,7 +1,8 @@
 """The fast forms' tile-plan autotuner (cvm_set_autotune,
 cvm_autotune_report): the first fast-form call of a shape times candidate
-plans and caches the fastest; the exact form always keeps newGoPlan's plan
-(impl.go:246-295).  Whatever plan it picks, the scores meet the fast form's
+plans and caches the fastest; a fleet's buckets are tuned the same way on
+trial fleets of their own members; the exact form always keeps newGoPlan's
+plan (impl.go:246-295, fleet.go:356-365).  Whatever plan it picks, the scores meet the fast form's
 bar against FP64 (cvmatch_test.go:13-81), repeat exactly on later calls,
 and Matcher.Find equals the one-shot Match of the same shape.
 """
@@ -31,7 +32,7 @@ def _scene(seed, h, w):
 
 def _entry(frame_wh, tpl_wh, form):
     for e in cvm.autotune_report():
-        if e["frame"] == list(frame_wh) and e["template"] == list(tpl_wh) and e["form"] == form:
+        if e["frame"] == list(frame_wh) and e.get("template") == list(tpl_wh) and e["form"] == form:
             return e
     return None
 
@@ -92,3 +93,37 @@ def test_autotune_off_runs_newgoplan():
     finally:
         cvm.SetForm(prev)
         cvm.SetAutotune(prev_t)
+
+
+def test_fleet_buckets_tuned_meet_the_bar():
+    """A 24-member fleet on 2560 x 1440 in the fast form: each bucket with
+    four or more members is tuned (its entry lists the timed candidates,
+    newGoPlan's first), every member meets the bar against FP64 and the
+    second FindAll repeats the first exactly."""
+    import bench
+    frame, tpls, where = bench.scene_fleet_2560x1440(count=24)
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    prev_t = cvm.SetAutotune(True)
+    try:
+        fleet.SetForm(cvm.FORM_FAST)
+        r1 = fleet.FindAll(frame)
+        r2 = fleet.FindAll(frame)
+    finally:
+        cvm.SetAutotune(prev_t)
+    assert [tuple(r) for r in r1] == [tuple(r) for r in r2]
+    tuned = [e for e in cvm.autotune_report() if e.get("fleet") and e["frame"] == [2560, 1440]]
+    big = [b for b in fleet.buckets(2560, 1440) if b[8] >= 4]
+    for e in tuned:
+        base = oracle.plan(e["bucket"][0], e["bucket"][1], 2560 - e["bucket"][0] + 1, 1440 - e["bucket"][1] + 1)
+        assert e["candidates"][0]["plan"] == [base.dft_w, base.dft_h]
+        assert all(c["ms_per_member"] >= 0 and c["ms"] > 0 for c in e["candidates"])
+        print(f"\nbucket {e['bucket']} x{e['members']}: plan {e['plan']} from "
+              f"{[(c['plan'], round(c['ms'], 3)) for c in e['candidates']]}")
+    assert tuned or not big
+    _, ref_maps = oracle.fleet_find_all(tpls, frame, threads=16, want_maps=True)
+    F = fp64.Frame(frame, 3)
+    for i, t in enumerate(tpls):
+        fp64.check_extrema(tuple(r1[i]), F.match(t), TOL, ref_map=ref_maps[i], name=f"member {i}")
+        if where[i] is not None:
+            assert (r1[i].MaxX, r1[i].MaxY) == where[i]
+    assert cvm.device_status() == 0

@@ -33,9 +33,18 @@ def test_tensor_core_dft_selftest():
 @pytest.fixture
 def mixed_form():
     prev = cvm.SetForm(cvm.FORM_MIXED)
+    prev_t = cvm.SetAutotune(False)  # newGoPlan's 1024-wide tiles: the tensor-core rows
     yield
     cvm.SetForm(prev)
+    cvm.SetAutotune(prev_t)
     assert cvm.device_status() == 0
+
+
+@pytest.fixture
+def no_autotune():
+    prev_t = cvm.SetAutotune(False)
+    yield
+    cvm.SetAutotune(prev_t)
 
 
 def test_mixed_match_rgba_1920x1080_vs_fp64(mixed_form):
@@ -75,7 +84,7 @@ def test_mixed_equals_fast_where_rows_are_not_1024():
     assert np.array_equal(fast.view(np.uint32), mixed.view(np.uint32))
 
 
-def test_mixed_fleet_vs_fp64_and_fast():
+def test_mixed_fleet_vs_fp64_and_fast(no_autotune):
     """A fleet whose bucket plans 1024-wide tiles, in the mixed form: every
     member against FP64 and against the fast form."""
     import bench
@@ -99,7 +108,7 @@ def test_mixed_fleet_vs_fp64_and_fast():
     print(f"\nmixed fleet: worst extremum error against FP64 {worst:.2e}, against the fast form {worst_fast:.2e}")
 
 
-def test_mixed_stream_equals_mixed_find_all():
+def test_mixed_stream_equals_mixed_find_all(no_autotune):
     """The CUDA-graph frame stream replays the tensor-core kernels: the same
     results as FindAll."""
     import bench
