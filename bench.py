@@ -1068,6 +1068,7 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
+    cvm.SetAutotune(args.autotune == "on")
     key = args.workload
     if key == "fleet":
         W = FleetWorkload(cvm, torch, dev, stream, count=args.templates)
@@ -1153,6 +1154,7 @@ def run_stream(args):
     import cvmatch_gb300 as cvm
     frames, color, gray = scene_stream_1920x1080()
     H, W = frames[0].shape[:2]
+    cvm.SetAutotune(args.autotune == "on")
     cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in color])
     gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in gray])
     cf.SetForm(FORM[args.form])
@@ -1261,6 +1263,8 @@ def main():
                          "with its 1024-point inverse rows on the tensor cores) or exact (the reference's float32 "
                          "bits; cvm_set_form / cvm_fleet_set_form); every form is measured in each run")
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
+    ap.add_argument("--autotune", default="on", choices=["on", "off"],
+                    help="the fast forms' tile-plan autotuner (cvm_set_autotune); off runs newGoPlan's plans")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
