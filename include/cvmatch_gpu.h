@@ -265,14 +265,19 @@ int cvm_get_form(void);
  * timed run) -- newGoPlan's choice and the best of a GPU cost proxy -- and
  * keeps the fastest if it beats newGoPlan's
  * by more than 3 %; every later call of that shape in the process runs the
- * cached plan (so results repeat exactly).  Calls made while their stream
- * is being captured do not tune.  cvm_set_autotune returns the previous
- * setting.  No reference counterpart (the reference always plans with
- * newGoPlan). */
+ * cached plan (so results repeat exactly).  A fleet's first fast-form
+ * FindAll of a frame size does the same per bucket of four or more members
+ * (buildGeom's plan, fleet.go:356-365, against the candidates), timing
+ * trial fleets of k and 2k of the bucket's own members so that the cost is
+ * shared + members x per-member.  Calls made while their stream is being
+ * captured do not tune.  cvm_set_autotune returns the previous setting.
+ * No reference counterpart (the reference always plans with newGoPlan). */
 int cvm_set_autotune(int on);
 /* The tuned shapes as a JSON array (frame, template, mode, cn, step, form,
- * the chosen plan and each candidate's measured ms); returns the full
- * length, writes at most len - 1 characters and a terminating NUL. */
+ * the chosen plan and each candidate's measured ms; fleet buckets with
+ * "fleet": true, the bucket maxima, members and each candidate's per-member
+ * and shared ms); returns the full length, writes at most len - 1
+ * characters and a terminating NUL. */
 size_t cvm_autotune_report(char *buf, size_t len);
 
 /* Checks the tensor-core DFT path on this device: four inverse 1024-point
@@ -327,8 +332,10 @@ int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]);
 /* A fleet's buckets (bucketize, fleet.go:111-171) and each bucket's plan on
  * a pw x ph frame (buildGeom, fleet.go:356-365): returns the bucket count
  * (negative on error) and, for the first cap buckets, 9 ints each: {tw,
- * th, dftW, dftH, blockW, blockH, dh2, tiles, members}.  Flat members are
- * in no bucket.  Host-only; no device. */
+ * th, dftW, dftH, blockW, blockH, dh2, tiles, members} -- newGoPlan's
+ * plan (the exact form's; the fast forms may run a tuned one, listed by
+ * cvm_autotune_report).  Flat members are in no bucket.  Host-only; no
+ * device. */
 int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap);
 /* At most `members` member tails per wave of a FindAll (0, the default:
  * as many as a 4 GB workspace holds).  Each wave's tails write their
