@@ -2135,10 +2135,13 @@ SepGrid sep_grid(int rwMax, int rhMax) {
 
 // Band height of the vertical slide: every band first sums th rows, so
 // taller bands amortise that start over more results; the band stays at 16
-// rows unless the launch has CTAs to spare (~6 per SM at the taller band).
+// rows unless the launch has CTAs to spare (~6 per SM at the taller band),
+// and at most 256 (a 78-member wave of 2560x1440 statistics: bands of 128
+// rows 3.03 ms, 256 rows 2.91, 512 rows 3.09, 1024 rows 3.61 -- the
+// tallest leave too few CTAs per SM).
 static int vstat_band(const SepGrid &sg, int nmembers) {
     int BV = 16;
-    while (BV < 128 && (long long)sg.ncx * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) * nmembers >= 6 * 152) BV *= 2;
+    while (BV < 256 && (long long)sg.ncx * ((sg.rhMax + 2 * BV - 1) / (2 * BV)) * nmembers >= 6 * 152) BV *= 2;
     return BV;
 }
 
