@@ -28,6 +28,8 @@
 //   odd log2, last pass radix 16 (quarter S)    M = 16, two inverse heads (even / odd c)
 // where the inverse "head" is the radix-2 stage plus the h=2 radix-4 stage
 // on 8 contiguous logical slots.
+#include <type_traits>
+
 #include "cvm_device.cuh"
 
 namespace cvm {
@@ -544,36 +546,51 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
             // product the same way measured slower: it keeps mode 2's sweep.)
             const float2 *fr = a.in + (size_t)tileLocal * a.cnS * chanStride + c0;
             const float2 *tq = m->tspec[a.cls] + c0;
-            const int k0 = 0, k1 = cn;
-            constexpr int U = 8, TOTAL = N << LSC;
-            for (int i0 = threadIdx.x; i0 < TOTAL; i0 += U * kThreads) {
-                float2 acc[U];
-                size_t off[U];
-                bool ok[U];
+            // Each thread keeps one strip column c and visits rows
+            // r0 + RP*j: the column test is made once, every load is a
+            // 32-bit element offset from its channel's base, and the
+            // usual three channels are unrolled.
+            constexpr int RP = kThreads >> LSC, RPT = N / RP;  // rows per pass, rows per thread
+            constexpr int U = RPT < 8 ? RPT : 8;                 // rows in flight per channel
+            const int c = threadIdx.x & (SC - 1), r0 = threadIdx.x >> LSC;
+            float2 *sdst = smem + (r0 << LSC) + c;
+            if (c >= wv) {
+#pragma unroll 4
+                for (int j = 0; j < RPT; j++) sdst[(j * RP) << LSC] = make_float2(0.f, 0.f);
+            } else {
+                const unsigned rowStep = (unsigned)(RP * hwp);
+                const unsigned base0 = (unsigned)(r0 * hwp + c);
+                auto stage = [&](auto cnC) {
+                    constexpr int CNC = decltype(cnC)::value;
+                    const int nk = CNC > 0 ? CNC : cn;
+                    for (int j0 = 0; j0 < RPT; j0 += U) {
+                        float2 acc[U];
 #pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int idx = i0 + u * kThreads, c = idx & (SC - 1);
-                    ok[u] = idx < TOTAL && c < wv;
-                    off[u] = (size_t)(idx >> LSC) * hwp + c;
-                    acc[u] = make_float2(0.f, 0.f);
-                }
-                for (int kk = k0; kk < k1; kk++) {
-                    const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
-                    float2 f[U], t[U];
+                        for (int u = 0; u < U; u++) acc[u] = make_float2(0.f, 0.f);
+                        const unsigned o0 = base0 + (unsigned)j0 * rowStep;
+#pragma unroll(CNC > 0 ? CNC : 1)
+                        for (int kk = 0; kk < nk; kk++) {
+                            const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
+                            float2 f[U], t[U];
 #pragma unroll
-                    for (int u = 0; u < U; u++) {
-                        f[u] = ok[u] ? __ldg(fk + off[u]) : make_float2(0.f, 0.f);
-                        t[u] = ok[u] ? __ldg(tk + off[u]) : make_float2(0.f, 0.f);
+                            for (int u = 0; u < U; u++) {
+                                f[u] = __ldg(fk + (o0 + (unsigned)u * rowStep));
+                                t[u] = __ldg(tk + (o0 + (unsigned)u * rowStep));
+                            }
+#pragma unroll
+                            for (int u = 0; u < U; u++) {
+                                acc[u].x = fmaf(f[u].x, t[u].x, fmaf(f[u].y, t[u].y, acc[u].x));
+                                acc[u].y = fmaf(f[u].y, t[u].x, fmaf(-f[u].x, t[u].y, acc[u].y));
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; u++) sdst[((j0 + u) * RP) << LSC] = acc[u];
                     }
-#pragma unroll
-                    for (int u = 0; u < U; u++) {
-                        acc[u].x = fmaf(f[u].x, t[u].x, fmaf(f[u].y, t[u].y, acc[u].x));
-                        acc[u].y = fmaf(f[u].y, t[u].x, fmaf(-f[u].x, t[u].y, acc[u].y));
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < U; u++)
-                    if (i0 + u * kThreads < TOTAL) smem[i0 + u * kThreads] = acc[u];
+                };
+                if (cn == 3)
+                    stage(std::integral_constant<int, 3>{});
+                else
+                    stage(std::integral_constant<int, 0>{});
             }
             __syncthreads();
             auto ldx = [&](float2 *x, int c, int B) {
