@@ -1178,8 +1178,9 @@ struct FleetTuneKey {
 struct FleetTuneEntry {
     Plan plan;
     int n = 0;
-    Plan cand[4];
-    float perMember[4] = {0, 0, 0, 0}, shared[4] = {0, 0, 0, 0}, total[4] = {0, 0, 0, 0};
+    static constexpr int kCands = 8;
+    Plan cand[kCands];
+    float perMember[kCands] = {}, shared[kCands] = {}, total[kCands] = {};
 };
 std::map<FleetTuneKey, FleetTuneEntry> g_fleetTune;
 
@@ -1203,7 +1204,7 @@ int tune_bucket_plan(cvm_fleet *f, const Bucket &b, const uint8_t *dParent, long
         cudaGetLastError();
         return CVM_OK;
     }
-    std::vector<Plan> cands = plan_candidates(b.tw, b.th, rwF, rhF, 4);
+    std::vector<Plan> cands = plan_candidates(b.tw, b.th, rwF, rhF, FleetTuneEntry::kCands);
     FleetTuneEntry ent;
     ent.plan = *out;
     if (cands.size() > 1) {
