@@ -138,6 +138,8 @@ struct FwdRowsArgs {
 // The row transforms specialised on dftW = 2^5 .. 2^12 (cvm_rows.cu).
 // map: the frame's tensor map when a.tma (ignored otherwise).
 bool rows_fixed_length(int log2n);
+// Elements (pairs x length) per CTA of a fleet wave's fast-form inverse rows.
+int rows_fast_wave_elems(int log2n);
 void launch_fwd_rows_fixed(const FwdRowsArgs &a, const CUtensorMap &map, dim3 grid, int threads, size_t smem,
                            cudaStream_t st);
 // Encodes a 2-D tensor map over w x h bytes at img (row stride istride)

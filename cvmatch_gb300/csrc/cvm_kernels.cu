@@ -2007,8 +2007,9 @@ int inv_rows_ctas_per_tile(const FftClass &fc, int rowsMax, int *pairsPerCta, in
     // all 256 threads busy, ~68 KB of shared memory (three CTAs per SM);
     // wide: 8192 elements (two units per thread per pass), ~70 KB without
     // the accumulator; the tensor-core kernel takes the same
-    int P = (wide ? 8192 : 4096) / fc.n;
-    (void)tc;  // (32 pairs per CTA measured slower for it: 6.25 against 5.14 ms per 256-member frame)
+    // (the tensor-core kernel keeps 8192: 32 pairs per CTA measured slower
+    // for it, 6.25 against 5.14 ms per 256-member frame, and 4 pairs too)
+    int P = (wide ? (tc ? 8192 : rows_fast_wave_elems(fc.log2n)) : 4096) / fc.n;
     if (P < 1) P = 1;
     // A tile emits at most rowsMax rows, and never more than dftH (a fleet
     // member's last band extends to its own result edge, still inside the

@@ -476,7 +476,10 @@ __global__ void __launch_bounds__(256) k_fwd_rows_t(FwdRowsArgs a, const __grid_
 // the epilogue scores with the per-result (t, den) lanes and keeps
 // first-occurrence extrema merged by each member's last CTA.
 template <int LOG2N, bool FAST>
-__global__ void __launch_bounds__(256, (FAST && last_pass_r(LOG2N) == 16) ? 2 : 3) k_inv_rows_t(InvArgs a) {
+// Occupancy: the fast form's radix-16 last pass budgets two CTAs per SM;
+// its radix-4 last pass four (64 registers, with four row pairs per CTA in
+// fleets: rows_fast_pairs), the exact form three.
+__global__ void __launch_bounds__(256, FAST ? (last_pass_r(LOG2N) == 16 ? 2 : 4) : 3) k_inv_rows_t(InvArgs a) {
     griddep_wait();
     constexpr int N = 1 << LOG2N, LD = Line<LOG2N>::LD, HALF = N / 2;
     constexpr int XIT = (N + kThreads - 1) / kThreads;  // result columns per thread
@@ -746,6 +749,12 @@ void inv_one(const InvArgs &a, dim3 grid, size_t smem, cudaStream_t st) {
 }  // namespace
 
 bool rows_fixed_length(int log2n) { return log2n >= 5 && log2n <= 12; }
+
+// Elements per CTA of a fleet wave's fast-form inverse rows: a radix-4
+// last pass runs four CTAs per SM, whose shared memory holds 4096 elements
+// each (C4's 78-member waves of 1024-point rows: 3.56 -> 3.38 ms per frame
+// against 8192 at three CTAs); a radix-16 last pass keeps 8192 at two.
+int rows_fast_wave_elems(int log2n) { return log2n >= 5 && log2n <= 12 && last_pass_r(log2n) == 4 ? 4096 : 8192; }
 
 void launch_fwd_rows_fixed(const FwdRowsArgs &a, const CUtensorMap &map, dim3 grid, int threads, size_t smem,
                            cudaStream_t st) {
