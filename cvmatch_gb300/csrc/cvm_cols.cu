@@ -539,64 +539,44 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
             middle_sweep<false, L, LSC>(smem, ldx, ts, hwp, wv, tri);
         } else {
             // Mode 3 (the fast form) sums over the member's channels frame x
-            // conj(zero-mean template) from stored spectra: the sum is staged
-            // into the strip first, U items per thread at a time (many
-            // independent loads in flight), then the inverse's first pass
-            // runs from shared memory.  (Staging the exact form's one-channel
-            // product the same way measured slower: it keeps mode 2's sweep.)
+            // conj(zero-mean template) from stored spectra, straight into the
+            // registers of the inverse's first pass.  (A version that staged
+            // the sum into the strip first measured 3.63 against 3.50 ms per
+            // 256-member 2560x1440 frame: the strip's extra store and load
+            // are shared-memory traffic in a kernel bound by it.)
             const float2 *fr = a.in + (size_t)tileLocal * a.cnS * chanStride + c0;
             const float2 *tq = m->tspec[a.cls] + c0;
-            // Each thread keeps one strip column c and visits rows
-            // r0 + RP*j: the column test is made once, every load is a
-            // 32-bit element offset from its channel's base, and the
-            // usual three channels are unrolled.
-            constexpr int RP = kThreads >> LSC, RPT = N / RP;  // rows per pass, rows per thread
-            constexpr int U = RPT < 8 ? RPT : 8;                 // rows in flight per channel
-            const int c = threadIdx.x & (SC - 1), r0 = threadIdx.x >> LSC;
-            float2 *sdst = smem + (r0 << LSC) + c;
-            if (c >= wv) {
-#pragma unroll 4
-                for (int j = 0; j < RPT; j++) sdst[(j * RP) << LSC] = make_float2(0.f, 0.f);
-            } else {
-                const unsigned rowStep = (unsigned)(RP * hwp);
-                const unsigned base0 = (unsigned)(r0 * hwp + c);
-                auto stage = [&](auto cnC) {
-                    constexpr int CNC = decltype(cnC)::value;
-                    const int nk = CNC > 0 ? CNC : cn;
-                    for (int j0 = 0; j0 < RPT; j0 += U) {
-                        float2 acc[U];
+            // The channel sum formed in the registers of the inverse's first
+            // pass: each unit's M rows of every channel come from the stored
+            // spectra (32-bit element offsets from each channel's base), so
+            // the sum makes no round trip through shared memory.
+            const unsigned sStep = (unsigned)(S * hwp);
+            auto ldx = [&](float2 *x, int c, int B) {
 #pragma unroll
-                        for (int u = 0; u < U; u++) acc[u] = make_float2(0.f, 0.f);
-                        const unsigned o0 = base0 + (unsigned)j0 * rowStep;
-#pragma unroll(CNC > 0 ? CNC : 1)
-                        for (int kk = 0; kk < nk; kk++) {
-                            const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
-                            float2 f[U], t[U];
+                for (int ci = 0; ci < M; ci++) x[ci] = make_float2(0.f, 0.f);
+                if (c >= wv) return;
+                const unsigned o0 = (unsigned)(B * hwp + c);
+                auto chan = [&](int kk) {
+                    const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
+                    float2 f[M], t[M];
 #pragma unroll
-                            for (int u = 0; u < U; u++) {
-                                f[u] = __ldg(fk + (o0 + (unsigned)u * rowStep));
-                                t[u] = __ldg(tk + (o0 + (unsigned)u * rowStep));
-                            }
+                    for (int ci = 0; ci < M; ci++) {
+                        f[ci] = __ldg(fk + (o0 + (unsigned)ci * sStep));
+                        t[ci] = __ldg(tk + (o0 + (unsigned)ci * sStep));
+                    }
 #pragma unroll
-                            for (int u = 0; u < U; u++) {
-                                acc[u].x = fmaf(f[u].x, t[u].x, fmaf(f[u].y, t[u].y, acc[u].x));
-                                acc[u].y = fmaf(f[u].y, t[u].x, fmaf(-f[u].x, t[u].y, acc[u].y));
-                            }
-                        }
-#pragma unroll
-                        for (int u = 0; u < U; u++) sdst[((j0 + u) * RP) << LSC] = acc[u];
+                    for (int ci = 0; ci < M; ci++) {
+                        x[ci].x = fmaf(f[ci].x, t[ci].x, fmaf(f[ci].y, t[ci].y, x[ci].x));
+                        x[ci].y = fmaf(f[ci].y, t[ci].x, fmaf(-f[ci].x, t[ci].y, x[ci].y));
                     }
                 };
-                if (cn == 3)
-                    stage(std::integral_constant<int, 3>{});
-                else
-                    stage(std::integral_constant<int, 0>{});
-            }
-            __syncthreads();
-            auto ldx = [&](float2 *x, int c, int B) {
-                const float2 *p = smem + (B << LSC) + c;
-#pragma unroll
-                for (int ci = 0; ci < M; ci++) x[ci] = p[(S * ci) << LSC];
+                if (cn == 3) {
+                    chan(0);
+                    chan(1);
+                    chan(2);
+                } else {
+                    for (int kk = 0; kk < cn; kk++) chan(kk);
+                }
             };
             middle_sweep<false, L, LSC, decltype(ldx), false, true>(smem, ldx, nullptr, hwp, wv, tri);
         }
