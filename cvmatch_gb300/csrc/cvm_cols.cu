@@ -558,16 +558,21 @@ __global__ void __launch_bounds__(256, 3) k_cols_t(ColsArgs a) {
                 const unsigned o0 = (unsigned)(B * hwp + c);
                 auto chan = [&](int kk) {
                     const float2 *fk = fr + (size_t)kk * chanStride, *tk = tq + (size_t)kk * chanStride;
-                    float2 f[M], t[M];
+                    // eight rows' loads in flight at a time (16 would spill)
 #pragma unroll
-                    for (int ci = 0; ci < M; ci++) {
-                        f[ci] = __ldg(fk + (o0 + (unsigned)ci * sStep));
-                        t[ci] = __ldg(tk + (o0 + (unsigned)ci * sStep));
-                    }
+                    for (int h = 0; h < M; h += 8) {
+                        float2 f[8], t[8];
 #pragma unroll
-                    for (int ci = 0; ci < M; ci++) {
-                        x[ci].x = fmaf(f[ci].x, t[ci].x, fmaf(f[ci].y, t[ci].y, x[ci].x));
-                        x[ci].y = fmaf(f[ci].y, t[ci].x, fmaf(-f[ci].x, t[ci].y, x[ci].y));
+                        for (int i = 0; i < 8; i++) {
+                            f[i] = __ldg(fk + (o0 + (unsigned)(h + i) * sStep));
+                            t[i] = __ldg(tk + (o0 + (unsigned)(h + i) * sStep));
+                        }
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            float2 &xi = x[h + i];
+                            xi.x = fmaf(f[i].x, t[i].x, fmaf(f[i].y, t[i].y, xi.x));
+                            xi.y = fmaf(f[i].y, t[i].x, fmaf(-f[i].x, t[i].y, xi.y));
+                        }
                     }
                 };
                 if (cn == 3) {
