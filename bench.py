@@ -403,7 +403,7 @@ def tile_heights(rw, rh, plan):
 
 def solo_flops(L, tw, th, iw, ih, cn):
     """The reference algorithm's flops for one match on its own plan, per
-    kernel of this build that does that part of the work: two real 2-D
+    library kernel that does that part of the work: two real 2-D
     FFTs per tile and channel (forward, inverse), 6 per spectrum element
     for the conjugate product, 2 cn + 12 per result for normOne.  The
     template's own spectrum is not counted (cached by Matcher/Fleet)."""

@@ -60,7 +60,7 @@ enum {
     CVM_ERR_NIL_IMAGE = 5,   /* "cvmatch: nil image"  cvmatch.go:170-173 */
     CVM_ERR_EMPTY_IMAGE = 6, /* "cvmatch: empty image"  cvmatch.go:174-177 */
     CVM_ERR_CUDA = 10,       /* a CUDA runtime call failed (message names it) */
-    CVM_ERR_UNSUPPORTED = 11,/* a transform size beyond this build's limits */
+    CVM_ERR_UNSUPPORTED = 11,/* a transform size beyond the library's limits */
     CVM_ERR_NO_DEVICE = 12   /* no sm_103 device / the library was not built for it */
 };
 

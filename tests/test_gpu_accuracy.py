@@ -6,8 +6,8 @@ configurations, and agreement of the extremum locations.
   of the full map within 1e-4 of FP64, and each extremum located where the
   FP64 map puts it whenever that map's top-2 margin exceeds 1e-4, and where
   the reference's own map puts it whenever the reference map's margin does
-  (north star: "identical max/min locations wherever the reference's top-2
-  margin exceeds that tolerance").
+  (identical max/min locations wherever the reference's top-2 margin
+  exceeds the tolerance).
 - The exact form reproduces the reference's float32 pipeline bit for bit
   (test_gpu_parity.py), so its errors here are the reference's own: on
   UI-like scenes with near-flat windows they exceed 1e-4 (the reference's
