@@ -194,6 +194,19 @@ __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2
     const float2 tb = F ? cmul_fma(*pb, bw) : cmul_plain(*pb, bw);
     const float2 tc = F ? cmul_fma(*pc, cw) : cmul_plain(*pc, cw);
     const float2 td = F ? cmul_fma(*pd, dw) : cmul_plain(*pd, dw);
+    if constexpr (F) {
+        // the fast form's sums and differences on packed pairs: a - b as
+        // fma(b, -1, a) rounds exactly as the subtraction does
+        const float2 m1 = make_float2(-1.f, -1.f);
+        const float2 s0 = __fadd2_rn(av, tc), s1 = __ffma2_rn(tc, m1, av);
+        const float2 s2 = __fadd2_rn(tb, td), s3 = __ffma2_rn(td, m1, tb);
+        const float rr = INV ? -s3.y : s3.y, ri = INV ? s3.x : -s3.x;
+        *pa = __fadd2_rn(s0, s2);
+        *pb = __ffma2_rn(s2, m1, s0);
+        *pc = make_float2(__fadd_rn(s1.x, rr), __fadd_rn(s1.y, ri));
+        *pd = make_float2(__fsub_rn(s1.x, rr), __fsub_rn(s1.y, ri));
+        return;
+    }
     const float s0x = __fadd_rn(av.x, tc.x), s0y = __fadd_rn(av.y, tc.y);
     const float s1x = __fsub_rn(av.x, tc.x), s1y = __fsub_rn(av.y, tc.y);
     const float s2x = __fadd_rn(tb.x, td.x), s2y = __fadd_rn(tb.y, td.y);
@@ -218,6 +231,17 @@ __device__ __forceinline__ void bfly4(float2 *pa, float2 *pc, float2 *pb, float2
 template <bool INV>
 __device__ __forceinline__ void bfly4_one(float2 *pa, float2 *pc, float2 *pb, float2 *pd) {
     const float2 av = *pa, tb = *pb, tc = *pc, td = *pd;
+    {
+        const float2 m1 = make_float2(-1.f, -1.f);
+        const float2 s0 = __fadd2_rn(av, tc), s1 = __ffma2_rn(tc, m1, av);
+        const float2 s2 = __fadd2_rn(tb, td), s3 = __ffma2_rn(td, m1, tb);
+        const float rr = INV ? -s3.y : s3.y, ri = INV ? s3.x : -s3.x;
+        *pa = __fadd2_rn(s0, s2);
+        *pb = __ffma2_rn(s2, m1, s0);
+        *pc = make_float2(__fadd_rn(s1.x, rr), __fadd_rn(s1.y, ri));
+        *pd = make_float2(__fsub_rn(s1.x, rr), __fsub_rn(s1.y, ri));
+        return;
+    }
     const float s0x = av.x + tc.x, s0y = av.y + tc.y;
     const float s1x = av.x - tc.x, s1y = av.y - tc.y;
     const float s2x = tb.x + td.x, s2y = tb.y + td.y;

@@ -589,7 +589,64 @@ __global__ void __launch_bounds__(256, FAST ? (last_pass_r(LOG2N) == 16 ? 2 : 4)
         }
         return;
     }
-    if (fuse && P > 0 && !flat) {
+    if (FAST && fuse && P > 0 && !flat && !a.ms.map && !a.ms.anyRoi) {
+        // The fast form without a score map or regions of interest (every
+        // fleet FindAll): the same units, scores and visiting order as the
+        // general epilogue below, with the CTA-local raster index of a result
+        // (row within the CTA x N + x, ascending as the general epilogue's
+        // global index does) kept in 32 bits and widened once at the end.
+        constexpr int LH = last_pass_h(LOG2N), LR = last_pass_r(LOG2N);
+        constexpr int LLR = LR == 16 ? 4 : 2, LLH = ilog2c(LH), LU = LOG2N - LLR;
+        constexpr int OFF = (LOG2N & 1) ? LH - 2 : LH - 1;
+        const float *dens = reinterpret_cast<const float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride);
+        float minV = FLT_MAX, maxV = -FLT_MAX;
+        int minL = INT_MAX, maxL = INT_MAX;
+        for (int u = tid; u < (P << LU); u += kThreads) {
+            const int line = u >> LU, v = u & ((1 << LU) - 1);
+            const int j = v & (LH - 1), base = ((v >> LLH) << (LLH + LLR)) + j;
+            const int rl = 2 * line;                          // CTA-local row of the real part
+            const bool odd = 2 * (pair0 + line) + 1 < bh;     // the imaginary part's row exists
+            const float *d0 = dens + (long long)(tb.y0 + 2 * (pair0 + line)) * m.rw + tb.x0;
+            float den0[LR], den1[LR];
+#pragma unroll
+            for (int i = 0; i < LR; i++) {
+                const int x = base + LH * i;
+                den0[i] = x < bw ? __ldg(d0 + x) : 0.f;
+                den1[i] = (x < bw && odd) ? __ldg(d0 + m.rw + x) : 0.f;
+            }
+            float2 z[LR];
+            last_unit<true, LH, LR, FAST>(smem + line * LD + padi(base), fc.triW + OFF, j, z);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (h == 1 && !odd) break;
+                const int l0 = (rl + h) * N;
+#pragma unroll
+                for (int i = 0; i < LR; i++) {
+                    const int x = base + LH * i;
+                    if (x < bw) {
+                        const float sc = score_fast(h ? z[i].y : z[i].x, h ? den1[i] : den0[i], denFlat);
+                        if (sc < minV) {
+                            minV = sc;
+                            minL = l0 + x;
+                        }
+                        if (sc > maxV) {
+                            maxV = sc;
+                            maxL = l0 + x;
+                        }
+                    }
+                }
+            }
+        }
+        // widen: CTA-local (row, x) -> the member's raster index
+        auto widen = [&](int l) {
+            return l == INT_MAX ? LLONG_MAX
+                                : (long long)(tb.y0 + 2 * pair0 + (l >> LOG2N)) * m.rw + tb.x0 + (l & (N - 1));
+        };
+        e.minV = minV;
+        e.maxV = maxV;
+        e.minI = widen(minL);
+        e.maxI = widen(maxL);
+    } else if (fuse && P > 0 && !flat) {
         // The last pass of every line, each unit's outputs scored straight
         // from registers: x = base + H*i of line p are results x of rows 2p
         // (real part) and 2p+1 (imaginary part).  A thread owns at most one
