@@ -505,7 +505,11 @@ int run_solo(const SoloJob &J, cudaStream_t st) {
     const size_t hElems = (size_t)stat_pitch(cnS) * J.ih * sg.hp;
     // a tall template with a fixed channel count: 16-row block sums of the
     // window sums, from which every vertical band starts
-    const size_t bElems = (J.mode == 0 && J.th >= 64) ? (size_t)stat_pitch(J.cnFixed) * (J.ih / 16) * sg.hp : 0;
+    // (the block sums are u32: 16 rows of the squared window sum, 16 * tw *
+    // cn * 255^2, must stay below 2^32)
+    const size_t bElems = (J.mode == 0 && J.th >= 64 && 16ull * J.tw * J.cnFixed * 65025ull < (1ull << 32))
+                              ? (size_t)stat_pitch(J.cnFixed) * (J.ih / 16) * sg.hp
+                              : 0;
     size_t bytes = Arena::bytes(1, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                    Arena::bytes(nparts, sizeof(Partial)) + Arena::bytes(hElems, sizeof(unsigned int)) +
                    Arena::bytes((size_t)rw * rh, sizeof(float2)) + (bElems ? Arena::bytes(bElems, sizeof(unsigned int)) : 0);
@@ -1437,9 +1441,19 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     const int cnP = f->step == 4 ? 4 : 1;
     const int hpP = (int)align_up((size_t)pw + 1, 32);
     const size_t prefixElems = (size_t)(cnP == 4 ? 6 : stat_pitch(cnP)) * ph * hpP;
+    // and their 16-row block sums (the main block), from which each band of
+    // every member's vertical slide starts
+    // (u32 sums: 16 rows of a member's squared window sum over the main
+    // block's channels, 16 * tw * cn * 255^2, must stay below 2^32)
+    int twMax = 0;
+    for (const Bucket &b : f->buckets) twMax = std::max(twMax, b.tw);
+    const size_t prefixRow = (size_t)(cnP == 4 ? 4 : stat_pitch(cnP)) * hpP;
+    const bool blkOk = 16ull * (unsigned)twMax * (cnP == 4 ? 3u : 1u) * 65025ull < (1ull << 32);
+    const size_t blkElems = blkOk ? prefixRow * (size_t)(ph / 16) : 0;
     const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
-                         Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) + frameBytes +
-                         partBytes + waveBytes;
+                         Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) +
+                         (blkElems ? Arena::bytes(blkElems, sizeof(unsigned int)) : 0) + frameBytes + partBytes +
+                         waveBytes;
     PoolBuf buf;
     CVM_TRY(pool_alloc(buf, bytes, st));
     Arena A;
@@ -1448,6 +1462,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     DevFrame *F = A.take<DevFrame>(1);
     int *counters = A.take<int>(n);
     unsigned int *prefix = A.take<unsigned int>(prefixElems);
+    unsigned int *prefixBlk = blkElems ? A.take<unsigned int>(blkElems) : nullptr;
     char *frameBase = A.base + A.used;
     A.used += frameBytes;
     Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
@@ -1459,6 +1474,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     CVM_CUDA(launch_prep(nullptr, 0, 0, 0, f->step, 0, f->step == 4 ? dParent : nullptr, pstride, pw, ph, P, n, 0, 0,
                          0, F, st));
     CVM_CUDA(launch_row_prefix(dParent, pstride, f->step, pw, ph, cnP, prefix, hpP, st));
+    if (prefixBlk) CVM_CUDA(launch_vblock(prefix, prefixBlk, ph / 16, prefixRow, st));
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
@@ -1508,7 +1524,7 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             SepGrid sgP = bg.sg;
             sgP.hp = hpP;
             CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
-                                      cnP, prefix, 0, st, 1));
+                                      cnP, prefix, 0, st, 1, nullptr, nullptr, prefixBlk));
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(fast ? 3 : 2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw,
                                      st));

@@ -204,12 +204,17 @@ SepGrid sep_grid(int rwMax, int rhMax);
 // sharedPrefix: H holds launch_row_prefix's shared planes (no per-member
 // k_hsum; each member differences the prefix at its own width).  vst/vev
 // (optional): k_vstats runs on vst, ordered after k_hsum by the event vev.
-// blk (one match, optional): (ih/16) x hp x stat_pitch(cnMax) u32 for the
-// 16-row block sums of H, from which each band starts (tall templates).
+// blk (optional): one match, (ih/16) x hp x stat_pitch(cnMax) u32 for the
+// 16-row block sums of H, from which each band starts (tall templates),
+// built here; a fleet (sharedPrefix), the block sums of the prefix's main
+// block built by launch_vblock.
 cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, int iw, int ih, const MemberSet &ms,
                              int nmembers, int soloTw, int soloRw, const SepGrid &sg, int cnMin, int cnMax,
                              unsigned int *H, size_t slotStride, cudaStream_t st, int sharedPrefix = 0,
                              cudaStream_t vst = nullptr, cudaEvent_t vev = nullptr, unsigned int *blk = nullptr);
+// The 16-row block sums of rows of rowElems u32 (block b = rows 16b ..
+// 16b+15, the rows' layout), nblk blocks: a vertical slide starts from them.
+cudaError_t launch_vblock(const unsigned int *H, unsigned int *B, int nblk, size_t rowElems, cudaStream_t st);
 // Exclusive row prefixes P_q(x, r) (x = 0..iw), u32 modular, interleaved
 // [ih][hp][stat_pitch(cnP)] with hp >= iw + 1: the first cnP channel sums
 // and the squares of the first min(cnP,3) channels.  For cnP == 4 the main

@@ -1624,7 +1624,9 @@ __device__ __forceinline__ void vstat_cols(const VstatArgs &a, const DevMember &
 #pragma unroll
     for (int k = 0; k < CN; k++) s[k] = 0u;
     int dy0 = 0;
-    if (!PRE && a.blk) {
+    // (a fleet's block sums cover the main prefix block only: members whose
+    // squared sum needs the alpha block start row by row)
+    if (a.blk && !(PRE && PCN == 4 && CN == 4)) {
         // whole 16-row blocks first (Y0 is a multiple of 16: BV is)
         const unsigned int *Bx = a.blk + (size_t)x * NP;
 #pragma unroll 4
@@ -2220,7 +2222,8 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
         if (e != cudaSuccess) return e;
         st = vst;
     }
-    if (v.blk) {
+    if (sharedPrefix) v.blk = blk;  // a fleet's block sums, built once per frame (launch_vblock)
+    if (v.blk && !sharedPrefix) {
         ProfScope ps("k_vblock", st);
         const size_t rowElems = (size_t)sg.hp * stat_pitch(cnMax);
         const int nblk = ih / 16;
@@ -2271,6 +2274,14 @@ cudaError_t launch_sep_stats(const uint8_t *img, long long istride, int step, in
         }
     }
     count_launches(sharedPrefix ? 1 : 2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vblock(const unsigned int *H, unsigned int *B, int nblk, size_t rowElems, cudaStream_t st) {
+    if (nblk <= 0) return cudaSuccess;
+    ProfScope ps("k_vblock", st);
+    k_vblock<<<dim3((unsigned)((rowElems + kThreads - 1) / kThreads), nblk), kThreads, 0, st>>>(H, B, nblk, rowElems);
+    count_launches(1);
     return cudaGetLastError();
 }
 

@@ -571,6 +571,41 @@ def test_very_wide_colour_template_global_column_arrays():
     assert (t[4], t[5]) == (50, 11)
 
 
+def test_fleet_block_sums_and_a_member_too_wide_for_them():
+    """A fleet's vertical slides start from 16-row block sums of the shared
+    row prefix (u32).  Sixteen rows of a colour member's squared window sum
+    stay below 2^32 only for templates narrower than ~1376 px, so a fleet
+    holding a 1400-px member starts every slide row by row: both kinds of
+    fleet bit-exact against the oracle, and the fast form within 1e-4 of
+    FP64 on the wide fleet."""
+    from oracle import fp64
+    img = rgba(91, 150, 1500)
+    small = [img[20:60, 100:164].copy(), img[70:102, 900:940].copy(), img[5:125, 300:348].copy()]
+    wide = small + [img[10:90, 40:1440].copy()]
+    for tpls in (small, wide):
+        fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+        got = [tuple(r) for r in fleet.FindAll(img)]
+        want = oracle.fleet_find_all(tpls, img, threads=16)
+        assert all(same_tuple(g, w) for g, w in zip(got, want)), (len(tpls), got, want)
+    fleet.SetForm(cvm.FORM_FAST)
+    fast = fleet.FindAll(img)
+    F = fp64.Frame(img, 3)
+    for i, t in enumerate(wide):
+        fp64.check_extrema(tuple(fast[i]), F.match(t), 1e-4, name=f"member {i}")
+
+
+def test_very_wide_tall_gray_template_without_block_sums():
+    """A 4200 x 64 gray template: sixteen rows of its squared window sums
+    can exceed 2^32, so the vertical slide starts row by row instead of
+    from 16-row block sums; bit-exact against the oracle."""
+    g = image(607, 110, 4300, 1).copy()
+    tpl = g[30:94, 60:4260].copy()
+    t, m = cvm.match_u8(g, tpl, 1)
+    to, mo = oracle.match_u8(g, tpl, 1, threads=16)
+    assert np.array_equal(bits(m), bits(mo)) and same_tuple(t, to)
+    assert (t[4], t[5]) == (60, 30)
+
+
 # ------------------------------------------------------------ frame streams
 
 
