@@ -1168,14 +1168,17 @@ def run_stream(args):
         st.pull()
     torch.cuda.synchronize()
     lat = []
+    nvtx = _nvtx(torch)
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
         c0 = time.time()
+        nvtx.range_push("timed_stream")  # a profiler's launch list can select the timed frames by this range
         for i in range(nfr):
             st.push(frames[i % K])
             if i >= 1:
                 lat.append(st.pull()[2])
         lat.append(st.pull()[2])
+        nvtx.range_pop()
         wall = time.perf_counter() - t0
         c1 = time.time()
     fps = nfr / wall
