@@ -86,3 +86,64 @@ def test_random_fleet_exact_and_fast(case):
             continue
         fp64.check_extrema(tuple(fast[i]), F.match(t), TOL, ref_map=ref_maps[i], name=f"seed {seed} member {i}")
     assert cvm.device_status() == 0
+
+
+def _roi_box(roi, tw, th, rw, rh):
+    """Result positions [x0, x1) x [y0, y1) whose window lies inside roi."""
+    x, y, w, h = roi
+    x0, y0 = max(x, 0), max(y, 0)
+    return x0, y0, min(x + w - tw + 1, rw), min(y + h - th + 1, rh)
+
+
+@pytest.mark.parametrize("seed", [301, 302, 303, 304])
+def test_random_fleet_regions_of_interest(seed):
+    """Random regions of interest on random fleets: in the exact form each
+    restricted member's result is the first-occurrence extrema of the
+    oracle's FindAll map over its region (bit for bit); in the fast form
+    those extrema within 1e-4 of the FP64 map's over the region, located
+    where the FP64 and the reference's restricted maps determine them; an
+    empty region gives (NaN, -1, -1, NaN, -1, -1)."""
+    rng = np.random.default_rng(seed)
+    h, w = int(rng.integers(60, 400)), int(rng.integers(60, 600))
+    img = _frame(rng, h, w, False)
+    # (no flat members: every channel constant over the template, the
+    # reference's fixed answer, is covered with a region elsewhere)
+    tpls = [t for t in _members(rng, img, 8, min(w, 120), min(h, 100))
+            if t[..., :3].reshape(-1, 3).std(axis=0).max() > 0]
+    rois = {}
+    for i, t in enumerate(tpls):
+        if rng.integers(0, 3) == 0:
+            continue
+        rw_, rh_ = int(rng.integers(1, w + 1)), int(rng.integers(1, h + 1))
+        rois[i] = (int(rng.integers(-20, w)), int(rng.integers(-20, h)), rw_, rh_)
+    want, maps = oracle.fleet_find_all(tpls, img, threads=16, want_maps=True)
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    for i, r in rois.items():
+        fleet.SetROI(i, *r)
+    exact = fleet.FindAll(img)
+    fleet.SetForm(cvm.FORM_FAST)
+    fast = fleet.FindAll(img)
+    F = fp64.Frame(img, 3)
+    for i, t in enumerate(tpls):
+        th, tw = t.shape[:2]
+        m = maps[i]
+        if i not in rois:
+            g = tuple(exact[i])
+            assert np.float32(g[0]).view(np.uint32) == np.float32(want[i][0]).view(np.uint32) and g[1:3] == want[i][1:3]
+            assert np.float32(g[3]).view(np.uint32) == np.float32(want[i][3]).view(np.uint32) and g[4:6] == want[i][4:6]
+            continue
+        x0, y0, x1, y1 = _roi_box(rois[i], tw, th, m.shape[1], m.shape[0])
+        if x1 <= x0 or y1 <= y0:
+            for r in (exact[i], fast[i]):
+                assert np.isnan(r[0]) and np.isnan(r[3]) and tuple(r)[1:3] == (-1, -1) and tuple(r)[4:6] == (-1, -1)
+            continue
+        sub = m[y0:y1, x0:x1]
+        iy, ix = np.unravel_index(int(np.argmin(sub)), sub.shape)
+        jy, jx = np.unravel_index(int(np.argmax(sub)), sub.shape)
+        g = tuple(exact[i])
+        assert np.float32(g[0]).view(np.uint32) == np.float32(sub[iy, ix]).view(np.uint32), (i, g)
+        assert np.float32(g[3]).view(np.uint32) == np.float32(sub[jy, jx]).view(np.uint32), (i, g)
+        assert g[1:3] == (x0 + int(ix), y0 + int(iy)) and g[4:6] == (x0 + int(jx), y0 + int(jy)), (i, g)
+        m64 = F.match(t)[y0:y1, x0:x1]
+        fp64.check_extrema(tuple(fast[i]), m64, TOL, ref_map=sub, name=f"seed {seed} member {i}", off=(x0, y0))
+    assert cvm.device_status() == 0
