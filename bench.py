@@ -624,7 +624,8 @@ def _workload_config(key, ws, args):
         return {"workload": f"Fleet.FindAll, {args.templates} RGBA templates 16..192 x 16..128 (70% a*x+b shifted "
                             "crops, 30% absent) on a 2560x1440 RGBA frame", "parent": [2560, 1440],
                 "templates": args.templates, "channels": "RGBA (cn=3 after the alpha scans)", "l2": l2,
-                "parallelism": par}
+                "parallelism": par, **({"stats": "inverse-rows epilogue"} if getattr(args, "stats", "kernel")
+                                       == "epilogue" else {})}
     if key == "match":
         return {"workload": "Match RGBA 1920x1080, template 96x32 (UI-like synthetic, a*x+b shifted button)",
                 "parent": [1920, 1080], "template": [96, 32], "channels": "RGBA (cn=3 after the alpha scan)",
@@ -1072,6 +1073,8 @@ def run_gpu(args):
     key = args.workload
     if key == "fleet":
         W = FleetWorkload(cvm, torch, dev, stream, count=args.templates)
+        if args.stats == "epilogue":
+            W.fleet.SetStats(cvm.STATS_EPILOGUE)
     else:
         W = WORKLOADS[key](cvm, torch, dev, stream)
     W.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -1268,6 +1271,9 @@ def main():
     ap.add_argument("--timeline", action="store_true", help="print one profiled step's launch spans to stderr")
     ap.add_argument("--autotune", default="on", choices=["on", "off"],
                     help="the fast forms' tile-plan autotuner (cvm_set_autotune); off runs newGoPlan's plans")
+    ap.add_argument("--stats", default="kernel", choices=["kernel", "epilogue"],
+                    help="--workload fleet: window statistics from the statistics kernel (default) or formed in "
+                         "the inverse-rows epilogue from the frame's summed-area table (cvm_fleet_set_stats)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -105,6 +105,7 @@ def lib():
             L.cvm_fleet_set_form.argtypes = [vp, i32]
             L.cvm_fleet_buckets.argtypes = [vp, i32, i32, vp, i32]
             L.cvm_fleet_set_wave.argtypes = [vp, i32]
+            L.cvm_fleet_set_stats.argtypes = [vp, i32]
             L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
             L.cvm_get_form.argtypes = []
@@ -299,6 +300,8 @@ def NewGrayMatcher(sub) -> Matcher:
 FORM_EXACT = 0
 FORM_FAST = 1
 FORM_MIXED = 2
+STATS_KERNEL = 0
+STATS_EPILOGUE = 1
 
 
 def SetAutotune(on: bool) -> bool:
@@ -381,6 +384,13 @@ class Fleet:
         """At most `members` member tails per wave (0: by the workspace
         budget); see cvm_fleet_set_wave."""
         _check(lib().cvm_fleet_set_wave(self._h, members))
+
+    def SetStats(self, mode: int):
+        """STATS_KERNEL (the default: the statistics kernel) or
+        STATS_EPILOGUE (window statistics inside the inverse-rows epilogue
+        from the frame's summed-area table, where it applies); the results
+        are the same bits.  See cvm_fleet_set_stats."""
+        _check(lib().cvm_fleet_set_stats(self._h, mode))
 
     def buckets(self, pw: int, ph: int):
         """[(tw, th, dftW, dftH, blockW, blockH, dh2, tiles, members)] per

@@ -1117,6 +1117,7 @@ struct cvm_fleet {
     uint64_t roiGen = 0;       // bumped by every cvm_fleet_set_roi
     int form = CVM_FORM_EXACT; // arithmetic of the member tails (cvm_fleet_set_form)
     int waveMembers = 0;       // members per wave of tails (0: by the 4 GB workspace budget)
+    int statsMode = CVM_STATS_KERNEL;  // or CVM_STATS_EPILOGUE (cvm_fleet_set_stats)
     Plan forcedPlan;           // every bucket's plan when dftW > 0 (the autotuner's trial fleets)
     ~cvm_fleet() {
         if (dP) cudaFree(dP);
@@ -1242,6 +1243,7 @@ int tune_bucket_plan(cvm_fleet *f, const Bucket &b, const uint8_t *dParent, long
                 cvm_fleet trial;
                 trial.step = f->step;
                 trial.form = f->form;
+                trial.statsMode = f->statsMode;
                 trial.forcedPlan = cands[c];
                 Bucket one;
                 one.tw = b.tw;
@@ -1448,12 +1450,38 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     int twMax = 0;
     for (const Bucket &b : f->buckets) twMax = std::max(twMax, b.tw);
     const size_t prefixRow = (size_t)(cnP == 4 ? 4 : stat_pitch(cnP)) * hpP;
-    const bool blkOk = 16ull * (unsigned)twMax * (cnP == 4 ? 3u : 1u) * 65025ull < (1ull << 32);
+    // CVM_STATS_EPILOGUE: fast-form buckets without regions of interest take
+    // their window statistics from the frame's summed-area table inside the
+    // inverse-rows epilogue (no statistics kernel, no den written and read
+    // back) when every member's squared window sum can be restored from its
+    // residue modulo 2^32: area * cn * 16256 < 2^32, cn up to the frame's
+    // channels.
+    std::vector<char> satUse(fg->bg.size(), 0);
+    bool anySat = false, anyStatsKernel = false;
+    for (size_t b = 0; b < fg->bg.size(); b++) {
+        const FleetBucketGeom &bg = *fg->bg[b];
+        bool ok = f->statsMode == CVM_STATS_EPILOGUE && bg.form == CVM_FORM_FAST && f->roi.empty() && (f->step == 4 || f->step == 1);
+        for (int i : bg.members) {
+            if (!ok) break;
+            const cvm_matcher *m = f->ms[i];
+            ok = (unsigned long long)m->w * m->h * (unsigned)cnP * 16256ull < (1ull << 32);
+        }
+        satUse[b] = ok;
+        anySat |= ok;
+        anyStatsKernel |= !ok;
+    }
+    const size_t alphaRow = cnP == 4 ? (size_t)2 * hpP : 0;
+    const size_t satElems = anySat ? (size_t)(ph + 1) * (prefixRow + alphaRow) : 0;
+    const size_t satBlkElems = anySat ? (size_t)((ph + 15) / 16 + 1) * prefixRow : 0;
+    const bool blkOk = anyStatsKernel && 16ull * (unsigned)twMax * (cnP == 4 ? 3u : 1u) * 65025ull < (1ull << 32);
     const size_t blkElems = blkOk ? prefixRow * (size_t)(ph / 16) : 0;
     const size_t bytes = Arena::bytes(n, sizeof(DevParams)) + Arena::bytes(1, sizeof(DevFrame)) +
                          Arena::bytes(n, sizeof(int)) + Arena::bytes(prefixElems, sizeof(unsigned int)) +
-                         (blkElems ? Arena::bytes(blkElems, sizeof(unsigned int)) : 0) + frameBytes + partBytes +
-                         waveBytes;
+                         (blkElems ? Arena::bytes(blkElems, sizeof(unsigned int)) : 0) +
+                         (satElems ? Arena::bytes(satElems, sizeof(unsigned int)) +
+                                         Arena::bytes(satBlkElems, sizeof(unsigned int))
+                                   : 0) +
+                         frameBytes + partBytes + waveBytes;
     PoolBuf buf;
     CVM_TRY(pool_alloc(buf, bytes, st));
     Arena A;
@@ -1463,6 +1491,8 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     int *counters = A.take<int>(n);
     unsigned int *prefix = A.take<unsigned int>(prefixElems);
     unsigned int *prefixBlk = blkElems ? A.take<unsigned int>(blkElems) : nullptr;
+    unsigned int *sat = satElems ? A.take<unsigned int>(satElems) : nullptr;
+    unsigned int *satBlk = satElems ? A.take<unsigned int>(satBlkElems) : nullptr;
     char *frameBase = A.base + A.used;
     A.used += frameBytes;
     Partial *parts = reinterpret_cast<Partial *>(A.base + A.used);
@@ -1475,6 +1505,12 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
                          0, F, st));
     CVM_CUDA(launch_row_prefix(dParent, pstride, f->step, pw, ph, cnP, prefix, hpP, st));
     if (prefixBlk) CVM_CUDA(launch_vblock(prefix, prefixBlk, ph / 16, prefixRow, st));
+    if (sat) {
+        CVM_CUDA(launch_sat(prefix, ph, prefixRow, satBlk, sat, st));
+        if (alphaRow)  // the (s3, alpha squares) block after the main one, in both
+            CVM_CUDA(launch_sat(prefix + (size_t)ph * prefixRow, ph, alphaRow, satBlk, sat + (size_t)(ph + 1) * prefixRow,
+                                st));
+    }
     for (size_t b = 0; b < fg->bg.size(); b++) {
         const FleetBucketGeom &bg = *fg->bg[b];
         const Geom &G = bg.G;
@@ -1513,6 +1549,12 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         ms.lanesStride = (size_t)bg.rwMax * bg.rhMax;
         ms.anyRoi = !f->roi.empty();
         ms.form = bg.form;
+        if (satUse[b]) {
+            ms.sat = sat;
+            ms.satRow = prefixRow;
+            ms.satAlpha = alphaRow ? (size_t)(ph + 1) * prefixRow : 0;
+            ms.satNp = cnP == 4 ? 4 : 2;
+        }
         for (int c = 0; c < G.nclass; c++) {
             ms.scratch[c] = scratch[c];
             ms.scratchStride[c] = bg.memberScratch[c];
@@ -1523,8 +1565,9 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             ms.first = w0;
             SepGrid sgP = bg.sg;
             sgP.hp = hpP;
-            CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
-                                      cnP, prefix, 0, st, 1, nullptr, nullptr, prefixBlk));
+            if (!satUse[b])
+                CVM_CUDA(launch_sep_stats(dParent, pstride, f->step, pw, ph, ms, nw, 0, 0, sgP, f->step == 4 ? 3 : 1,
+                                          cnP, prefix, 0, st, 1, nullptr, nullptr, prefixBlk));
             for (int c = 0; c < G.nclass; c++)
                 CVM_CUDA(launch_cols(fast ? 3 : 2, frame[c], nullptr, cnS, G.g, G.fc[c], c, cnS, nullptr, 1.0f, ms, nw,
                                      st));
@@ -2188,6 +2231,13 @@ int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap)
 int cvm_fleet_set_wave(cvm_fleet *f, int members) {
     if (!f || members < 0) return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad wave size");
     f->waveMembers = members;
+    return CVM_OK;
+}
+
+int cvm_fleet_set_stats(cvm_fleet *f, int mode) {
+    if (!f || (mode != CVM_STATS_KERNEL && mode != CVM_STATS_EPILOGUE))
+        return fail(CVM_ERR_ARGS, "cvmatch_gpu: bad statistics mode");
+    f->statsMode = mode;
     return CVM_OK;
 }
 

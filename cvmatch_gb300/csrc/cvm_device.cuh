@@ -290,6 +290,65 @@ __device__ __forceinline__ float score_fast(float num, float den, float denFlat)
     return 0.f;
 }
 
+// The fast form's den of the window at result (x, y) of member m, formed
+// from the frame's summed-area table (MemberSet::sat) instead of read from
+// the statistics kernel's lanes.  Four corners give the window's channel
+// sums and its squared sum modulo 2^32; each channel sum is below 2^32,
+// and the squared sum q is restored from its residue as
+//   q = U - ((U - q) mod 2^32),   U = 255 * (sum of the channel sums),
+// exact while U - q = sum over the window's bytes of v (255 - v), at most
+// area * cn * 16256, stays below 2^32 (the host uses the table only
+// then).  The rest is the statistics kernel's fast den sequence on the same
+// integers (vstat_cols, FAST), so den has the same bits.
+__device__ __forceinline__ float sat_den(const MemberSet &ms, const DevMember &m, const DevParams &Pm, int y, int x) {
+    const size_t row = ms.satRow;
+    unsigned int s0, s1 = 0u, s2 = 0u, s3 = 0u, qm;
+    if (ms.satNp == 4) {
+        const unsigned int *r0 = ms.sat + (size_t)y * row + (size_t)x * 4;
+        const unsigned int *r1 = r0 + (size_t)m.th * row;
+        const int dx = 4 * m.tw;
+        const uint4 A = __ldg(reinterpret_cast<const uint4 *>(r1 + dx)), B = __ldg(reinterpret_cast<const uint4 *>(r1));
+        const uint4 C = __ldg(reinterpret_cast<const uint4 *>(r0 + dx)), D = __ldg(reinterpret_cast<const uint4 *>(r0));
+        s0 = A.x - B.x - C.x + D.x;
+        s1 = A.y - B.y - C.y + D.y;
+        s2 = A.z - B.z - C.z + D.z;
+        qm = A.w - B.w - C.w + D.w;
+        if (Pm.cn == 4) {
+            // the (s3, alpha squares) block: half the main block's lanes per row
+            const size_t arow = row >> 1;
+            const unsigned int *a0 = ms.sat + ms.satAlpha + (size_t)y * arow + (size_t)x * 2;
+            const unsigned int *a1 = a0 + (size_t)m.th * arow;
+            const int da = 2 * m.tw;
+            const uint2 A2 = __ldg(reinterpret_cast<const uint2 *>(a1 + da)), B2 = __ldg(reinterpret_cast<const uint2 *>(a1));
+            const uint2 C2 = __ldg(reinterpret_cast<const uint2 *>(a0 + da)), D2 = __ldg(reinterpret_cast<const uint2 *>(a0));
+            s3 = A2.x - B2.x - C2.x + D2.x;
+            qm += A2.y - B2.y - C2.y + D2.y;
+        }
+    } else {
+        const unsigned int *r0 = ms.sat + (size_t)y * row + (size_t)x * 2;
+        const unsigned int *r1 = r0 + (size_t)m.th * row;
+        const int dx = 2 * m.tw;
+        const uint2 A = __ldg(reinterpret_cast<const uint2 *>(r1 + dx)), B = __ldg(reinterpret_cast<const uint2 *>(r1));
+        const uint2 C = __ldg(reinterpret_cast<const uint2 *>(r0 + dx)), D = __ldg(reinterpret_cast<const uint2 *>(r0));
+        s0 = A.x - B.x - C.x + D.x;
+        qm = A.y - B.y - C.y + D.y;
+    }
+    const unsigned long long U = 255ull * ((unsigned long long)s0 + s1 + s2 + s3);
+    const unsigned long long q = U - (unsigned int)((unsigned int)U - qm);
+    const unsigned long long sq = (unsigned long long)s0 * s0 + (unsigned long long)s1 * s1 +
+                                  (unsigned long long)s2 * s2 + (unsigned long long)s3 * s3;
+    const unsigned long long idv = (unsigned long long)m.tw * m.th * q - sq;
+    const float id = fmaf(__uint2float_rn((unsigned int)(idv >> 32)), 4294967296.0f, __uint2float_rn((unsigned int)idv));
+    const float diff2 = __fmul_rn(id, Pm.varScale);
+    float lim = 0.5f;
+    if (q < (1ull << 24)) {
+        lim = __fmul_rn(1.1920928955078125e-06f, __uint2float_rn((unsigned int)q));  // 10 * 2^-23 * q
+        if (lim > 0.5f) lim = 0.5f;
+    }
+    const float sd = __fmul_rn(diff2, rsqrtf(diff2));
+    return diff2 > lim ? __fmul_rn(sd, Pm.templNorm) : 0.f;
+}
+
 // Padded shared-memory line layout: one spare slot every 16 elements keeps
 // the strided pass accesses free of bank conflicts.
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }

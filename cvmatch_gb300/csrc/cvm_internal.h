@@ -115,6 +115,15 @@ struct MemberSet {
     // form (the fast form with its 1024-point inverse rows on the tensor
     // cores).  Nonzero selects the fast form's arithmetic everywhere else.
     int form;
+    // Fast-form fleet waves without score maps or regions of interest: the
+    // frame's summed-area table of the shared row prefix (ih + 1 rows, the
+    // prefix's lanes; all sums modulo 2^32), from which the inverse-rows
+    // epilogue forms every window's statistics itself instead of reading
+    // den from `lanes` (nullptr: the statistics kernel filled `lanes`).
+    const unsigned int *sat;
+    size_t satRow;     // u32 per row of the main block (satNp * hp)
+    size_t satAlpha;   // u32 offset of the (s3, alpha squares) block; 0: none
+    int satNp;         // u32 per x in the main block: 4 (RGBA frame), 2 (gray)
 };
 
 struct Partial {
@@ -223,6 +232,11 @@ cudaError_t launch_vblock(const unsigned int *H, unsigned int *B, int nblk, size
 // launch_sep_stats with sharedPrefix reads it with cnMax == cnP.
 cudaError_t launch_row_prefix(const uint8_t *img, long long istride, int step, int iw, int ih, int cnP,
                               unsigned int *P, int hp, cudaStream_t st);
+// Summed-area table of `rows` rows of rowElems u32 lanes (one block of the
+// row prefix): S[y][e] = sum_{r<y} P[r][e], y = 0..rows, modulo 2^32.
+// B: scratch of ((rows + 15) / 16 + 1) * rowElems u32.
+cudaError_t launch_sat(const unsigned int *P, int rows, size_t rowElems, unsigned int *B, unsigned int *S,
+                       cudaStream_t st);
 
 // Stores small host values into device memory through kernel arguments
 // (stream ordered, no host buffer lifetime to manage).

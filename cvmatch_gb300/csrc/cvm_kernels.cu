@@ -1563,6 +1563,64 @@ __global__ void k_vblock(const unsigned int *__restrict__ H, unsigned int *__res
     B[(size_t)b * rowElems + e] = sum;
 }
 
+// The frame's summed-area table over the shared row prefix's lanes,
+// S[y][e] = sum_{r < y} P[r][e] for y = 0 .. rows (u32, modulo 2^32 like
+// the prefix), in three steps: 16-row block sums, their exclusive scan down
+// each lane (the total in block nb), then each block's rows from its start.
+__global__ void k_sat_blocks(const unsigned int *__restrict__ P, int rows, size_t rowElems,
+                             unsigned int *__restrict__ B) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= rowElems) return;
+    const int r0 = 16 * blockIdx.y, n = min(16, rows - r0);
+    const unsigned int *p = P + (size_t)r0 * rowElems + e;
+    unsigned int v[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = i < n ? __ldg(p + (size_t)i * rowElems) : 0u;
+    unsigned int sum = 0u;
+#pragma unroll
+    for (int i = 0; i < 16; i++) sum += v[i];
+    B[(size_t)blockIdx.y * rowElems + e] = sum;
+}
+
+__global__ void k_sat_scan(unsigned int *B, int nb, size_t rowElems) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= rowElems) return;
+    unsigned int run = 0u;
+    for (int b0 = 0; b0 < nb; b0 += 8) {
+        unsigned int v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = b0 + i < nb ? B[(size_t)(b0 + i) * rowElems + e] : 0u;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (b0 + i < nb) {
+                B[(size_t)(b0 + i) * rowElems + e] = run;
+                run += v[i];
+            }
+    }
+    B[(size_t)nb * rowElems + e] = run;
+}
+
+__global__ void k_sat_fill(const unsigned int *__restrict__ P, int rows, size_t rowElems,
+                           const unsigned int *__restrict__ B, unsigned int *__restrict__ S) {
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= rowElems) return;
+    const int r0 = 16 * blockIdx.y;
+    if (r0 > rows) return;
+    const int n = min(16, rows - r0);  // prefix rows added inside this block
+    const unsigned int *p = P + (size_t)r0 * rowElems + e;
+    unsigned int v[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = i < n ? __ldg(p + (size_t)i * rowElems) : 0u;
+    unsigned int run = B[(size_t)blockIdx.y * rowElems + e];
+    unsigned int *s = S + (size_t)r0 * rowElems + e;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        if (r0 + i > rows) break;
+        s[(size_t)i * rowElems] = run;
+        run += v[i];
+    }
+}
+
 // PRE: H is the shared row prefix built for PCN channels (window sum =
 // P[x+tw] - P[x]); its squares are plane PCN (PCN < 4) or planes 4 (RGB)
 // and 5 (alpha) when PCN == 4 (a cn = 3 member leaves alpha out).
@@ -2282,6 +2340,19 @@ cudaError_t launch_vblock(const unsigned int *H, unsigned int *B, int nblk, size
     ProfScope ps("k_vblock", st);
     k_vblock<<<dim3((unsigned)((rowElems + kThreads - 1) / kThreads), nblk), kThreads, 0, st>>>(H, B, nblk, rowElems);
     count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sat(const unsigned int *P, int rows, size_t rowElems, unsigned int *B, unsigned int *S,
+                       cudaStream_t st) {
+    if (rows <= 0 || rowElems == 0) return cudaSuccess;
+    const int nb = (rows + 15) / 16;
+    const unsigned gx = (unsigned)((rowElems + kThreads - 1) / kThreads);
+    ProfScope ps("k_sat", st);
+    k_sat_blocks<<<dim3(gx, nb), kThreads, 0, st>>>(P, rows, rowElems, B);
+    k_sat_scan<<<gx, kThreads, 0, st>>>(B, nb, rowElems);
+    k_sat_fill<<<dim3(gx, nb + 1), kThreads, 0, st>>>(P, rows, rowElems, B, S);
+    count_launches(3);
     return cudaGetLastError();
 }
 

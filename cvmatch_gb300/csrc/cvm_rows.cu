@@ -599,6 +599,9 @@ __global__ void __launch_bounds__(256, FAST ? (last_pass_r(LOG2N) == 16 ? 2 : 4)
         constexpr int LLR = LR == 16 ? 4 : 2, LLH = ilog2c(LH), LU = LOG2N - LLR;
         constexpr int OFF = (LOG2N & 1) ? LH - 2 : LH - 1;
         const float *dens = reinterpret_cast<const float *>(a.ms.lanes + (size_t)slot * a.ms.lanesStride);
+        // a fleet wave with the frame's summed-area table forms each
+        // window's den here (no statistics kernel ran for it)
+        const bool ownStats = a.ms.sat != nullptr;
         float minV = FLT_MAX, maxV = -FLT_MAX;
         int minL = INT_MAX, maxL = INT_MAX;
         for (int u = tid; u < (P << LU); u += kThreads) {
@@ -606,13 +609,23 @@ __global__ void __launch_bounds__(256, FAST ? (last_pass_r(LOG2N) == 16 ? 2 : 4)
             const int j = v & (LH - 1), base = ((v >> LLH) << (LLH + LLR)) + j;
             const int rl = 2 * line;                          // CTA-local row of the real part
             const bool odd = 2 * (pair0 + line) + 1 < bh;     // the imaginary part's row exists
-            const float *d0 = dens + (long long)(tb.y0 + 2 * (pair0 + line)) * m.rw + tb.x0;
+            const int y0 = tb.y0 + 2 * (pair0 + line);
+            const float *d0 = dens + (long long)y0 * m.rw + tb.x0;
             float den0[LR], den1[LR];
+            if (ownStats) {
 #pragma unroll
-            for (int i = 0; i < LR; i++) {
-                const int x = base + LH * i;
-                den0[i] = x < bw ? __ldg(d0 + x) : 0.f;
-                den1[i] = (x < bw && odd) ? __ldg(d0 + m.rw + x) : 0.f;
+                for (int i = 0; i < LR; i++) {
+                    const int x = base + LH * i;
+                    den0[i] = x < bw ? sat_den(a.ms, m, Pm, y0, tb.x0 + x) : 0.f;
+                    den1[i] = (x < bw && odd) ? sat_den(a.ms, m, Pm, y0 + 1, tb.x0 + x) : 0.f;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < LR; i++) {
+                    const int x = base + LH * i;
+                    den0[i] = x < bw ? __ldg(d0 + x) : 0.f;
+                    den1[i] = (x < bw && odd) ? __ldg(d0 + m.rw + x) : 0.f;
+                }
             }
             float2 z[LR];
             last_unit<true, LH, LR, FAST>(smem + line * LD + padi(base), fc.triW + OFF, j, z);

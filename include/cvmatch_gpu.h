@@ -345,6 +345,24 @@ int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap)
  * on it.  Not to be called while a FindAll on the same fleet runs. */
 int cvm_fleet_set_wave(cvm_fleet *f, int members);
 
+/* Where a fleet's window statistics are formed (no counterpart in the
+ * reference, which computes them in normalizeBandGo, impl.go:708-805).
+ * CVM_STATS_KERNEL (the default): the statistics kernel writes each
+ * window's den, which the inverse-rows epilogue reads back.
+ * CVM_STATS_EPILOGUE: fast-form buckets without regions of interest whose
+ * every member satisfies area * cn * 16256 < 2^32 (colour members up to
+ * 66,052 px, gray up to 264,208 px) form each window's den inside the
+ * inverse-rows epilogue from the frame's summed-area table, with no
+ * statistics launch and no den written or read; other buckets, and every
+ * exact- or mixed-form bucket, still run the statistics kernel.  Results
+ * are the same bits either way.  The epilogue form measured slower on a
+ * GB300 (256 RGBA templates on a 2560x1440 frame: 10.3 against 9.5 ms per
+ * FindAll), hence not the default.  Not to be called while a FindAll on
+ * the same fleet runs. */
+#define CVM_STATS_KERNEL 0
+#define CVM_STATS_EPILOGUE 1
+int cvm_fleet_set_stats(cvm_fleet *f, int mode);
+
 /* Bucket b's members (construction-order indices, ascending): returns
  * their count (negative on error) and writes the first cap of them. */
 int cvm_fleet_bucket_members(const cvm_fleet *f, int b, int32_t *out, int cap);
