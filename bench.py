@@ -279,7 +279,7 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
     NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
-    def __init__(self, index: int, period_ms: int = 50):
+    def __init__(self, index: int, period_ms: int = 20):
         self.index = index
         self.period_ms = period_ms
         self.lines = []
@@ -315,8 +315,8 @@ class ClockSampler:
     def summary(self, t0=None, t1=None):
         """Median SM clock and the throttle reasons seen over every sample
         taken under load; `samples_timed` counts those inside [t0, t1] (the
-        timed region), when given."""
-        sm, smax, reasons, timed = [], None, set(), 0
+        timed region), when given, and `sm_mhz_timed` is their median."""
+        sm, smax, reasons, timed = [], None, set(), []
         for entry in self.lines:
             ts, ln = entry if isinstance(entry, tuple) else (None, entry)
             parts = [p.strip() for p in ln.split(",")]
@@ -329,14 +329,16 @@ class ClockSampler:
             sm.append(v)
             smax = mx
             if t0 is not None and ts is not None and t0 <= ts <= t1:
-                timed += 1
+                timed.append(v)
             for nm, flag in zip(self.NAMES, parts[4:8]):
                 if flag.lower() == "active":
                     reasons.add(nm)
         out = {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
                "reasons": sorted(reasons), "samples": len(sm)}
         if t0 is not None:
-            out["samples_timed"] = timed
+            # the samples taken inside the timed region itself, and their median
+            out["samples_timed"] = len(timed)
+            out["sm_mhz_timed"] = float(np.median(timed)) if timed else None
         return out
 
 

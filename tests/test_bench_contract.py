@@ -64,6 +64,18 @@ def test_clock_record_flags_throttling():
     assert "hw_thermal_slowdown" in s.summary()["reasons"]
 
 
+def test_clock_record_splits_the_timed_region():
+    s = bench.ClockSampler(0)
+    s.lines = [(1.0, "2070, 2070, 900, 0x0, Not Active, Not Active, Not Active, Not Active"),
+               (2.0, "2055, 2070, 1300, 0x0, Not Active, Not Active, Not Active, Not Active"),
+               (2.5, "2040, 2070, 1300, 0x0, Not Active, Not Active, Not Active, Not Active"),
+               (3.0, "2025, 2070, 1300, 0x0, Not Active, Not Active, Not Active, Not Active"),
+               (9.0, "2070, 2070, 500, 0x0, Not Active, Not Active, Not Active, Not Active")]
+    r = s.summary(1.5, 3.2)
+    assert r["samples"] == 5 and r["samples_timed"] == 3 and r["sm_mhz_timed"] == 2040.0
+    assert bench.ClockSampler(0).period_ms <= 25  # several samples inside a C4 run's ~0.2 s of timed steps
+
+
 def test_peak_is_measured_or_the_stated_fallback():
     peak, kind = bench.measured_peaks()
     assert kind in ("measured", "fallback") and peak > 0
