@@ -431,6 +431,34 @@ def test_fleet_bit_exact_vs_oracle(gray):
     assert hits >= len(got) * 2 // 3
 
 
+@pytest.mark.parametrize("form", ["exact", "fast"])
+def test_fleet_agrees_with_solo_matches(form):
+    """fleet_test.go:50-88: every member of a multi-member fleet (run on its
+    bucket's plan) agrees with a one-shot Match of the same template (run on
+    its own plan) within 1e-3, at the same extremum locations on clear
+    matches; in the exact form the plans differ only in rounding, in the
+    fast form both sides are within 1e-4 of the FP64 definition."""
+    img = desk(49)
+    subs, at = crops(img, seed=13, n=12)
+    prev = cvm.SetForm(cvm.FORM_FAST if form == "fast" else cvm.FORM_EXACT)
+    try:
+        fleet = cvm.NewFleet(*[cvm.NewMatcher(s) for s in subs])
+        if form == "fast":
+            fleet.SetForm(cvm.FORM_FAST)
+        got = fleet.FindAll(img)
+        solo = [cvm.Match(img, s) for s in subs]
+    finally:
+        cvm.SetForm(prev)
+    assert len(got) == len(subs)
+    for i, (g, s) in enumerate(zip(got, solo)):
+        g, s = tuple(g), tuple(s)
+        if subs[i][..., :3].reshape(-1, 3).std(axis=0).max() == 0:  # flat: the fixed answer
+            assert g == s == (1.0, 0, 0, 1.0, 0, 0), (i, g, s)
+            continue
+        assert abs(g[0] - s[0]) <= 1e-3 and abs(g[3] - s[3]) <= 1e-3, (i, g, s)
+        assert s[3] > 0.999 and g[4:6] == s[4:6] == at[i], (i, g, s, at[i])  # the planted copy
+
+
 def test_fleet_single_member_equals_find():
     img = desk(43)
     sub = img[100:132, 200:296].copy()
