@@ -1591,7 +1591,9 @@ struct cvm_stream {
     size_t pitch = 0, gpitch = 0;
     int nColor = 0, nGray = 0;
     cudaStream_t cs = nullptr;  // matching
+    cudaStream_t gs = nullptr;  // the gray fleet, a branch forked from cs and joined back
     cudaStream_t xs = nullptr;  // frame uploads
+    cudaEvent_t fork = nullptr, join = nullptr;
     struct Slot {
         uint8_t *hFrame = nullptr;   // page-locked staging
         uint8_t *dFrame = nullptr, *dGray = nullptr;
@@ -1619,20 +1621,32 @@ struct cvm_stream {
                 if (e) cudaEventDestroy(e);
         }
         if (cs) cudaStreamDestroy(cs);
+        if (gs) cudaStreamDestroy(gs);
         if (xs) cudaStreamDestroy(xs);
+        for (cudaEvent_t e : {fork, join})
+            if (e) cudaEventDestroy(e);
     }
 };
 
 namespace {
 
-// The per-frame pipeline of one slot on s->cs: both FindAlls, the gray
-// conversion between them, the results back to page-locked memory.
+// The per-frame pipeline of one slot on s->cs: the colour FindAll, and
+// beside it on s->gs (forked from cs after the frame arrived, joined back
+// before the results leave) the gray conversion and the gray FindAll --
+// independent work (both read the frame, they write disjoint result
+// ranges, each takes its workspace from the stream-ordered pool), so the
+// gray fleet's short launches fill the colour fleet's launch tails; then
+// the results back to page-locked memory.
 int stream_pipeline(cvm_stream *s, cvm_stream::Slot &sl) {
-    CVM_TRY(fleet_find_dev(s->color, sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dOut, s->cs));
     if (s->gray) {
-        CVM_CUDA(launch_gray(sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dGray, (long long)s->gpitch, s->cs));
-        CVM_TRY(fleet_find_dev(s->gray, sl.dGray, (long long)s->gpitch, s->pw, s->ph, sl.dOut + s->nColor, s->cs));
+        CVM_CUDA(cudaEventRecord(s->fork, s->cs));
+        CVM_CUDA(cudaStreamWaitEvent(s->gs, s->fork, 0));
+        CVM_CUDA(launch_gray(sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dGray, (long long)s->gpitch, s->gs));
+        CVM_TRY(fleet_find_dev(s->gray, sl.dGray, (long long)s->gpitch, s->pw, s->ph, sl.dOut + s->nColor, s->gs));
+        CVM_CUDA(cudaEventRecord(s->join, s->gs));
     }
+    CVM_TRY(fleet_find_dev(s->color, sl.dFrame, (long long)s->pitch, s->pw, s->ph, sl.dOut, s->cs));
+    if (s->gray) CVM_CUDA(cudaStreamWaitEvent(s->cs, s->join, 0));
     CVM_CUDA(cudaMemcpyAsync(sl.hOut, sl.dOut, (size_t)(s->nColor + s->nGray) * sizeof(cvm_result),
                              cudaMemcpyDeviceToHost, s->cs));
     return CVM_OK;
@@ -2109,7 +2123,10 @@ int cvm_stream_new(cvm_fleet *color, cvm_fleet *gray, int pw, int ph, cvm_stream
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     CVM_CUDA(cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking));
+    CVM_CUDA(cudaStreamCreateWithFlags(&s->gs, cudaStreamNonBlocking));
     CVM_CUDA(cudaStreamCreateWithPriority(&s->xs, cudaStreamNonBlocking, greatest));
+    CVM_CUDA(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
+    CVM_CUDA(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming));
     const size_t nres = (size_t)(s->nColor + s->nGray);
     for (cvm_stream::Slot &sl : s->slot) {
         CVM_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&sl.hFrame), s->pitch * ph, cudaHostAllocDefault));
