@@ -627,7 +627,8 @@ def _workload_config(key, ws, args):
                             "crops, 30% absent) on a 2560x1440 RGBA frame", "parent": [2560, 1440],
                 "templates": args.templates, "channels": "RGBA (cn=3 after the alpha scans)", "l2": l2,
                 "parallelism": par, **({"stats": "inverse-rows epilogue"} if getattr(args, "stats", "kernel")
-                                       == "epilogue" else {})}
+                                       == "epilogue" else {}),
+                **({"overlap": "off"} if getattr(args, "overlap", "on") == "off" else {})}
     if key == "match":
         return {"workload": "Match RGBA 1920x1080, template 96x32 (UI-like synthetic, a*x+b shifted button)",
                 "parent": [1920, 1080], "template": [96, 32], "channels": "RGBA (cn=3 after the alpha scan)",
@@ -1077,6 +1078,7 @@ def run_gpu(args):
         W = FleetWorkload(cvm, torch, dev, stream, count=args.templates)
         if args.stats == "epilogue":
             W.fleet.SetStats(cvm.STATS_EPILOGUE)
+        W.fleet.SetOverlap(args.overlap == "on")
     else:
         W = WORKLOADS[key](cvm, torch, dev, stream)
     W.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -1276,6 +1278,9 @@ def main():
     ap.add_argument("--stats", default="kernel", choices=["kernel", "epilogue"],
                     help="--workload fleet: window statistics from the statistics kernel (default) or formed in "
                          "the inverse-rows epilogue from the frame's summed-area table (cvm_fleet_set_stats)")
+    ap.add_argument("--overlap", default="on", choices=["on", "off"],
+                    help="--workload fleet: a wave's inverse rows beside the next wave's statistics and columns "
+                         "(cvm_fleet_set_overlap)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

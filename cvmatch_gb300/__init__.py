@@ -105,6 +105,7 @@ def lib():
             L.cvm_fleet_set_form.argtypes = [vp, i32]
             L.cvm_fleet_buckets.argtypes = [vp, i32, i32, vp, i32]
             L.cvm_fleet_set_wave.argtypes = [vp, i32]
+            L.cvm_fleet_set_overlap.argtypes = [vp, i32]
             L.cvm_fleet_set_stats.argtypes = [vp, i32]
             L.cvm_fleet_bucket_members.argtypes = [vp, i32, vp, i32]
             L.cvm_set_form.argtypes = [i32]
@@ -384,6 +385,11 @@ class Fleet:
         """At most `members` member tails per wave (0: by the workspace
         budget); see cvm_fleet_set_wave."""
         _check(lib().cvm_fleet_set_wave(self._h, members))
+
+    def SetOverlap(self, on: bool):
+        """Overlapped waves of member tails (on, the default) or every wave
+        in sequence; see cvm_fleet_set_overlap."""
+        _check(lib().cvm_fleet_set_overlap(self._h, 1 if on else 0))
 
     def SetStats(self, mode: int):
         """STATS_KERNEL (the default: the statistics kernel) or

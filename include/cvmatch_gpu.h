@@ -344,6 +344,14 @@ int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap)
  * spectra in L2, large waves need fewer launches.  Results do not depend
  * on it.  Not to be called while a FindAll on the same fleet runs. */
 int cvm_fleet_set_wave(cvm_fleet *f, int members);
+/* Overlapped waves (on, the default): a fast-form FindAll with more than
+ * one wave of member tails runs the inverse rows of wave k on a second
+ * stream beside the window statistics and column pass of wave k + 1 (the
+ * waves alternate between two workspaces); off, and in the exact and mixed
+ * forms (slower overlapped), every wave's launches run in sequence on the
+ * caller's stream.  Results do not depend on it.  No reference
+ * counterpart.  Not to be called while a FindAll on the same fleet runs. */
+int cvm_fleet_set_overlap(cvm_fleet *f, int on);
 
 /* Where a fleet's window statistics are formed (no counterpart in the
  * reference, which computes them in normalizeBandGo, impl.go:708-805).
