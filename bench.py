@@ -638,7 +638,8 @@ def _workload_config(key, ws, args):
                 "templates": args.templates, "channels": "RGBA (cn=3 after the alpha scans)", "l2": l2,
                 "parallelism": par, **({"stats": "inverse-rows epilogue"} if getattr(args, "stats", "kernel")
                                        == "epilogue" else {}),
-                **({"overlap": "off"} if getattr(args, "overlap", "on") == "off" else {})}
+                **({"overlap": "off"} if getattr(args, "overlap", "on") == "off" else {}),
+                **({"wave": args.wave} if getattr(args, "wave", 0) else {})}
     if key == "match":
         return {"workload": "Match RGBA 1920x1080, template 96x32 (UI-like synthetic, a*x+b shifted button)",
                 "parent": [1920, 1080], "template": [96, 32], "channels": "RGBA (cn=3 after the alpha scan)",
@@ -1090,6 +1091,7 @@ def run_gpu(args):
             W.fleet.SetStats(cvm.STATS_EPILOGUE)
         W.overlap = args.overlap == "on"
         W.fleet.SetOverlap(W.overlap)
+        W.fleet.SetWave(args.wave)
     else:
         W = WORKLOADS[key](cvm, torch, dev, stream)
     W.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -1289,6 +1291,8 @@ def main():
     ap.add_argument("--stats", default="kernel", choices=["kernel", "epilogue"],
                     help="--workload fleet: window statistics from the statistics kernel (default) or formed in "
                          "the inverse-rows epilogue from the frame's summed-area table (cvm_fleet_set_stats)")
+    ap.add_argument("--wave", type=int, default=0,
+                    help="--workload fleet: member tails per wave (cvm_fleet_set_wave; 0: the workspace budget's)")
     ap.add_argument("--overlap", default="on", choices=["on", "off"],
                     help="--workload fleet: a wave's inverse rows beside the next wave's statistics and columns "
                          "(cvm_fleet_set_overlap)")

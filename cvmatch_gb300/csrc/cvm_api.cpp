@@ -1442,7 +1442,15 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
         partBytes = std::max(partBytes, Arena::bytes((size_t)bg.members.size() * nparts, sizeof(Partial)));
         int w = (int)std::max<size_t>(1, kWaveBytes / std::max<size_t>(per, 1));
         if (f->waveMembers > 0) w = std::min(w, f->waveMembers);
-        w = std::min<int>(w, (int)bg.members.size());
+        const int nmB = (int)bg.members.size();
+        w = std::min<int>(w, nmB);
+        // the budget's wave count with equal waves, not a short last one
+        // (C4's 256 members: 4 x 64 instead of 78 + 78 + 78 + 22, 9.44 ->
+        // 9.34 ms with the waves overlapped)
+        if (f->waveMembers == 0 && w > 0) {
+            const int nwv = (nmB + w - 1) / w;
+            w = (nmB + nwv - 1) / nwv;
+        }
         wave[b] = w;
         size_t wb = Arena::bytes((size_t)w * lanesPer, sizeof(float2));
         for (int c = 0; c < bg.G.nclass; c++) wb += Arena::bytes((size_t)w * bg.memberScratch[c], sizeof(float2));

@@ -338,7 +338,7 @@ int cvm_plan(int tw, int th, int rw, int rh, int32_t out[6]);
  * device. */
 int cvm_fleet_buckets(const cvm_fleet *f, int pw, int ph, int32_t *out, int cap);
 /* At most `members` member tails per wave of a FindAll (0, the default:
- * as many as a 4 GB workspace holds).  Each wave's tails write their
+ * as few waves as a 4 GB workspace allows, of equal size).  Each wave's tails write their
  * column-pass spectra (~25 MB per member on a 2560x1440 frame) before the
  * row pass reads them back: small waves bound the workspace and keep those
  * spectra in L2, large waves need fewer launches.  Results do not depend
