@@ -1532,6 +1532,19 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
     char *waveBase[2] = {A.base + A.used, A.base + A.used + (overlap ? waveBytes : 0)};
     SideStream *ss = overlap ? &side_stream() : nullptr;
     int gw = 0;  // waves issued so far (all buckets): the set a wave uses is gw & 1
+    // On every exit (an error return included) the caller's stream joins all
+    // the side stream's queued rows before the workspace (declared above, so
+    // released after this) returns to the pool in the caller's stream order.
+    struct SideJoin {
+        SideStream *ss;
+        cudaStream_t st;
+        ~SideJoin() {
+            if (ss) {
+                cudaEventRecord(ss->colsDone, ss->waveRows);
+                cudaStreamWaitEvent(st, ss->colsDone, 0);
+            }
+        }
+    } sideJoin{ss, st};
     CVM_CUDA(cudaMemcpyAsync(P, f->dP, n * sizeof(DevParams), cudaMemcpyDeviceToDevice, st));
     CVM_CUDA(cudaMemsetAsync(F, 0, sizeof(DevFrame), st));
     CVM_CUDA(cudaMemsetAsync(counters, 0, n * sizeof(int), st));
@@ -1623,9 +1636,6 @@ int fleet_find_dev(cvm_fleet *f, const uint8_t *dParent, long long pstride, int 
             if (overlap) CVM_CUDA(cudaEventRecord(ss->rowsDone[set], rst));
         }
     }
-    // the side stream's last rows (in its order, every earlier wave's too)
-    // before the workspace returns to the pool in st's order
-    if (overlap && gw > 0) CVM_CUDA(cudaStreamWaitEvent(st, ss->rowsDone[(gw - 1) & 1], 0));
     return CVM_OK;
 }
 
