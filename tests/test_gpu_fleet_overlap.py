@@ -85,3 +85,45 @@ def test_c4_overlapped_waves_equal_sequence():
         fleet.SetForm(cvm.FORM_EXACT)
     assert len(ovl) == 256 and ovl == seq
     assert cvm.device_status() == 0
+
+
+def test_stream_graph_with_overlapped_waves():
+    """A frame stream whose fast-form colour fleet runs in several
+    overlapped waves: the side stream's rows join the captured graph, and
+    every frame's results equal Fleet.FindAll's on that frame."""
+    rng = np.random.default_rng(77)
+    H, W = 320, 480
+    base = _frame(rng, H, W)
+    frames = []
+    for i in range(4):
+        f = base.copy()
+        y, x = int(rng.integers(0, H - 40)), int(rng.integers(0, W - 60))
+        f[y:y + 40, x:x + 60, :3] = rng.integers(0, 256, (40, 60, 3), dtype=np.uint8)
+        frames.append(f)
+    tc = []
+    for i in range(7):
+        tw, th = int(rng.integers(12, 90)), int(rng.integers(12, 70))
+        x, y = int(rng.integers(0, W - tw)), int(rng.integers(0, H - th))
+        tc.append(base[y:y + th, x:x + tw].copy())
+    tg = [cvm.rgba_to_gray(base[40:70, 60:100])]
+    cf = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tc])
+    gf = cvm.NewFleet(*[cvm.NewGrayMatcher(t) for t in tg])
+    cf.SetForm(cvm.FORM_FAST)
+    cf.SetWave(2)  # four waves of the colour fleet, overlapped
+    try:
+        st = cvm.NewStream(cf, gf, W, H)
+        graphed, launches = st.info()
+        assert graphed and launches > 0
+        got = []
+        for i, f in enumerate(frames):
+            st.push(f)
+            if i >= 1:
+                got.append(st.pull())
+        got.append(st.pull())
+        for f, (rc, rg, ms) in zip(frames, got):
+            assert [_bits(r) for r in rc] == [_bits(r) for r in cf.FindAll(f)]
+            assert [_bits(r) for r in rg] == [_bits(r) for r in gf.FindAll(cvm.rgba_to_gray(f))]
+    finally:
+        cf.SetWave(0)
+        cf.SetForm(cvm.FORM_EXACT)
+    assert cvm.device_status() == 0
