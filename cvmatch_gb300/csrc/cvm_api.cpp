@@ -1315,8 +1315,13 @@ int tune_bucket_plan(cvm_fleet *f, const Bucket &b, const uint8_t *dParent, long
 // its frame spectra about points x 3 (measured on C4: 6.4 us per frame tile
 // against 2.2 us per member tile); a bucket is split at the member height
 // that minimises the sum over both parts when that beats the whole bucket
-// by more than 3 %, the shorter part holding at least 8 members.  Members
-// keep their construction order within each part.  The exact form keeps
+// by more than 5 % and each part holds at least 32 members: the model
+// leaves out each bucket's fixed costs (its launches, its waves' tails, the
+// tuner's own plans), which smaller parts do not amortise (C4's 256
+// members split 73 + 183, predicted -6.2 %, measured 9.28 -> 9.16 ms; the
+// 1080p stream's 64 members split 29 + 35, predicted -3.5 %, measured
+// 1.45 -> 1.61 ms per frame).  Members keep their construction order
+// within each part.  The exact form keeps
 // the reference's buckets (its bits follow from the bucket's plan).
 std::vector<Bucket> fast_buckets(const cvm_fleet *f, int pw, int ph) {
     auto points = [&](int tw, int th) -> long long {
@@ -1350,14 +1355,14 @@ std::vector<Bucket> fast_buckets(const cvm_fleet *f, int pw, int ph) {
                     nB++;
                 }
             }
-            if (nA < 8 || nB < 1) continue;
+            if (nA < 32 || nB < 32) continue;
             const long long c = points(twA, T) * (nA + 3) + points(twB, thB) * (nB + 3);
             if (c < best) {
                 best = c;
                 bestT = T;
             }
         }
-        if (bestT < 0 || best * 100 > whole * 97) {
+        if (bestT < 0 || best * 100 > whole * 95) {
             out.push_back(b);
             continue;
         }
