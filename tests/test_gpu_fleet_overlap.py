@@ -127,3 +127,27 @@ def test_stream_graph_with_overlapped_waves():
         cf.SetWave(0)
         cf.SetForm(cvm.FORM_EXACT)
     assert cvm.device_status() == 0
+
+
+def test_c4_fast_form_splits_its_bucket():
+    """The fast form's own buckets (fast_buckets): C4's single bucket of the
+    reference (256 members up to 192 x 128) runs as two -- the members up
+    to 49 rows high on a grid of 9 tiles, the rest on 12 -- while the
+    exact form keeps the reference's bucket; both forms' results are held
+    to their bars by the full-size tests."""
+    import bench
+    frame, tpls, _ = bench.scene_fleet_2560x1440()
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    assert len(fleet.buckets(2560, 1440)) == 1  # the reference's bucketing
+    fleet.SetForm(cvm.FORM_FAST)
+    try:
+        fleet.FindAll(frame)
+    finally:
+        fleet.SetForm(cvm.FORM_EXACT)
+    tuned = [e for e in cvm.autotune_report()
+             if e.get("fleet") and e.get("frame") == [2560, 1440] and e.get("form") == cvm.FORM_FAST]
+    live = [t for t in tpls if t[..., :3].reshape(-1, 3).std(axis=0).max() > 0]  # flat members join no bucket
+    nshort = sum(1 for t in live if t.shape[0] <= 49)
+    assert 32 <= nshort <= len(live) - 32
+    assert any(e["bucket"][1] <= 49 and e["members"] == nshort for e in tuned), tuned
+    assert any(e["bucket"][1] > 49 and e["members"] == len(live) - nshort for e in tuned), tuned
