@@ -151,3 +151,53 @@ def test_c4_fast_form_splits_its_bucket():
     assert 32 <= nshort <= len(live) - 32
     assert any(e["bucket"][1] <= 49 and e["members"] == nshort for e in tuned), tuned
     assert any(e["bucket"][1] > 49 and e["members"] == len(live) - nshort for e in tuned), tuned
+
+
+def test_split_buckets_with_regions_of_interest_vs_fp64():
+    """A fleet whose fast form splits its bucket (short and tall members on
+    a tall frame), with regions of interest on every fifth member: every
+    sampled member's extrema within 1e-4 of the FP64 map (restricted to its
+    region where it has one), at the FP64 map's locations wherever its
+    top-2 margin exceeds 1e-4 (cvmatch_test.go:13-81)."""
+    from oracle import fp64
+    rng = np.random.default_rng(21)
+    H, W = 1400, 1200
+    frame = _frame(rng, H, W)
+    tpls, at = [], []
+    for i in range(90):
+        if i % 2 == 0:
+            tw, th = int(rng.integers(16, 150)), int(rng.integers(12, 40))
+        else:
+            tw, th = int(rng.integers(16, 150)), int(rng.integers(100, 170))
+        x, y = int(rng.integers(0, W - tw)), int(rng.integers(0, H - th))
+        tpls.append(frame[y:y + th, x:x + tw].copy())
+        at.append((x, y))
+    live = [i for i, t in enumerate(tpls) if t[..., :3].reshape(-1, 3).std(axis=0).max() > 0]
+    fleet = cvm.NewFleet(*[cvm.NewMatcher(t) for t in tpls])
+    rois = {}
+    for i in live[::5]:
+        x, y = at[i]
+        rois[i] = (x - 20, y - 20, tpls[i].shape[1] + 60, tpls[i].shape[0] + 60)
+        fleet.SetROI(i, *rois[i])
+    fleet.SetForm(cvm.FORM_FAST)
+    try:
+        got = [tuple(r) for r in fleet.FindAll(frame)]
+    finally:
+        fleet.SetForm(cvm.FORM_EXACT)
+    tuned = [e for e in cvm.autotune_report()
+             if e.get("fleet") and e.get("frame") == [W, H] and e.get("form") == cvm.FORM_FAST]
+    assert sum(1 for e in tuned if e["members"] >= 32) >= 2, tuned  # the bucket ran split
+    F = fp64.Frame(frame, 3)
+    for i in sorted(set(live[::7]) | set(list(rois)[:6])):
+        t = tpls[i]
+        th, tw = t.shape[:2]
+        m64 = F.match(t)
+        off = (0, 0)
+        if i in rois:
+            x, y, w, h = rois[i]
+            x0, y0 = max(x, 0), max(y, 0)
+            x1, y1 = min(x + w - tw + 1, m64.shape[1]), min(y + h - th + 1, m64.shape[0])
+            m64, off = m64[y0:y1, x0:x1], (x0, y0)
+        fp64.check_extrema(got[i], m64, 1e-4, name=f"member {i} {tw}x{th}", off=off)
+        assert got[i][4:6] == at[i], (i, got[i], at[i])  # the planted copy
+    assert cvm.device_status() == 0
