@@ -1374,8 +1374,10 @@ std::vector<Bucket> fast_buckets(const cvm_fleet *f, int pw, int ph) {
             d.th = std::max(d.th, m->h);
             d.members.push_back(i);
         }
-        out.push_back(lo);
+        // the taller part first: the last wave's inverse rows have nothing
+        // left to overlap, and the shorter part's waves carry fewer tiles
         out.push_back(hi);
+        out.push_back(lo);
     }
     return out;
 }
